@@ -1,0 +1,370 @@
+"""Throughput of the FALL3D transport step on GB300 (cell-class-steps/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the 400x300x50 grid with 16 particle classes (phi -2..6), seeded
+synthetic meteorology with a k^-5/3 wind perturbation and a precipitation
+band (wet deposition on), Suzuki column 15 km, MER 1e7 kg/s.  A step is one
+pass of Sources/Fall3d.f90:112-117 over all classes (setsrc, sizloop with
+setbcc, advection, diffusion, wet and dry deposition, clip, cmass2d).
+
+``value``    precision form (binary32 stencil, binary64 budgets/accum/finddt)
+             with inputs resident in HBM, timed with CUDA events on the
+             context's stream over K steps; the state (0.4 GB of c alone) is
+             larger than the 126 MB L2, so no flush is needed between steps.
+``e2e``      the same metric through the C ABI's time loop (f3d_run) from
+             host buffers: meteorology and sources uploaded by the loop when
+             their intervals begin, the deposit maps (LOAD, COL_MASS, C_GRND)
+             read back at the end, all inside the timed region.
+``forms``    the plain binary64 form on the same workload.
+``--impl reference`` times the CPU oracle (the restatement of the reference's
+Fortran path; the Fortran itself cannot be built here) on all host cores.
+Multi-GPU: classes and scenarios are independent, so N GPUs run N replicas
+of the workload with no collective ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "cfg1"
+METRIC = "cell-class-steps/s"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _scenario(max_snapshots=4):
+    from fall3d_gb300 import synth
+
+    return synth.make_scenario(WORKLOAD, seed=0, max_snapshots=max_snapshots)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "", 1).isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# Algorithmic bytes per cell-class of each transport kernel of the unfused
+# form (element size S): every operand read once and every output written
+# once, met fields counted per class because each class sweep reads them.
+def kernel_bytes_per_cell_class(S):
+    return {"advctzc": 4 * S, "advctx": 3 * S, "advcty": 3 * S, "diffz": 4 * S, "diffx": 4 * S,
+            "diffy": 4 * S, "clip": 2 * S, "step_fused": None}
+
+
+def cpu_baseline(threads, steps=2):
+    """The CPU oracle on this host's cores on a bounded sample: one meteo
+    update (timed separately) then ``steps`` full steps of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+
+    s = _scenario(max_snapshots=2)
+    o = oracle_lib.OracleCtx(s, nthreads=threads)
+    o.source(0)
+    t0 = time.perf_counter()
+    o.meteo(0)
+    t_met = time.perf_counter() - t0
+    o.step()  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.step()
+    t = time.perf_counter() - t0
+    units = s.cell_classes * steps
+    o.close()
+    return {"value": units / t, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{WORKLOAD} 400x300x50x16: {steps} full steps after one meteo update "
+                      f"(meteo update {t_met:.1f} s, not in the rate); oracle -O2 -ffp-contract=off, "
+                      f"OpenMP over classes"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+
+    s = _scenario(max_snapshots=2)
+    o = oracle_lib.OracleCtx(s, nthreads=threads)
+    o.source(0)
+    o.meteo(0)
+    for _ in range(args.warmup):
+        o.step()
+    done = 0
+    t0 = time.perf_counter()
+    while done < args.steps:
+        o.step()
+        done += 1
+        if time.perf_counter() - t0 > 150.0:
+            break
+    t = time.perf_counter() - t0
+    v = s.cell_classes * done / t
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world, "steps": done,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / done, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "grid": [400, 300, 50], "classes": 16,
+                       "form": "CPU oracle (binary64), all host cores"},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": f"{done} full steps of {WORKLOAD} after one meteo update"},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import fall3d_gb300 as F
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    s = _scenario()
+    units_per_step = s.cell_classes
+
+    # ---------------- precision form, inputs resident in HBM ----------------
+    g = F.Context(s, F.PREC_FP32)
+    g.source(0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.meteo(0)
+    meteo_s = time.perf_counter() - t0
+    for _ in range(max(args.warmup, 3)):
+        g.step()
+    g.sync()
+    ext = torch.cuda.ExternalStream(g.stream_handle())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local_rank)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    n0 = F.kernel_launches()
+    ev0.record(ext)
+    for _ in range(args.steps):
+        g.step()
+    ev1.record(ext)
+    ev1.synchronize()
+    n_launch = F.kernel_launches() - n0
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ms)
+    value = units_per_step * args.steps * world / (ms / 1e3)
+
+    # per-kernel durations with CUDA events on the same stream
+    g.profile(True)
+    for _ in range(args.steps):
+        g.step()
+    prof = g.profile_read()
+    g.profile(False)
+    g.close()
+
+    # ---------------- plain binary64 form ----------------
+    g64 = F.Context(s, F.PREC_FP64)
+    g64.source(0)
+    g64.meteo(0)
+    k64 = max(2, min(args.steps, 6))
+    for _ in range(2):
+        g64.step()
+    g64.sync()
+    ext64 = torch.cuda.ExternalStream(g64.stream_handle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext64)
+    for _ in range(k64):
+        g64.step()
+    e1.record(ext64)
+    e1.synchronize()
+    ms64 = e0.elapsed_time(e1)
+    value64 = units_per_step * k64 / (ms64 / 1e3)
+    g64.close()
+
+    # ---------------- end to end through the C ABI time loop ----------------
+    from fall3d_gb300 import _abi
+
+    met = _abi.make_met(s.met)
+    src = _abi.make_src(s.src)
+    ge = F.Context(s, F.PREC_FP32)
+    ge.run(max_steps=2, met=met, src=src)  # warm-up (allocations, first meteo)
+    ge.close()
+    ge = F.Context(s, F.PREC_FP32)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    log = ge.run(max_steps=args.steps, met=met, src=src)
+    outs = ge.outputs()
+    t_e2e = time.perf_counter() - t0
+    t_e2e = max_over_ranks(t_e2e)
+    st = ge.state()
+    ge.close()
+    nx, ny, nz, nc = s.grid["nx"], s.grid["ny"], s.grid["nz"], s.grid["nc"]
+    times = s.met["times"]
+    n_meteo = int(np.sum(times <= st["time"])) if len(times) else 1
+    n_meteo = max(1, min(n_meteo, len(times)))
+    met_bytes = (6 * nx * ny * nz + 6 * nx * ny) * 8
+    src_bytes = int(s.src["nsou"][0]) * (3 * 4 + nc * 8)
+    h2d = (n_meteo * met_bytes + src_bytes) / args.steps
+    d2h = (3 * nx * ny * 8 + len(log["iiter"]) * 5 * 8) / args.steps
+    e2e_value = units_per_step * args.steps * world / t_e2e
+
+    # ---------------- roofline of the dominant kernel ----------------
+    peak, peak_kind = _peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (1, 0.0))
+    dom_name, (dom_n, dom_ms) = dom
+    bpc = kernel_bytes_per_cell_class(4).get(dom_name)
+    roof = None
+    if bpc and dom_n:
+        cells = units_per_step if dom_name != "clip" else (nx + 2) * (ny + 2) * (nz + 2) * nc
+        alg_bytes = bpc * cells
+        avg_ms = dom_ms / dom_n
+        achieved = alg_bytes / (avg_ms / 1e3) / 1e9
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+        if os.path.exists(tpath):
+            try:
+                traffic = json.load(open(tpath)).get(WORKLOAD, {}).get(dom_name)
+            except Exception:
+                traffic = None
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "kernel": dom_name,
+                "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
+                "peak_source": f"{peak_kind} hbm_gbs"}
+    step_bytes = 12 + 28 / nc  # binary32 algorithmic bytes per cell-class-step
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [nx, ny, nz], "classes": nc,
+                   "form": "precision (binary32 stencil, binary64 budgets/accum/finddt)",
+                   "l2": "state larger than L2 (no flush needed)", "parallelism": f"replicas{world}"},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": args.steps, "meteo_updates": n_meteo},
+        "gpu_launches": int(n_launch),
+        "clocks": clk,
+        "roofline": roof,
+        "step_roofline": {"alg_bytes_per_cell_class_step": step_bytes,
+                          "achieved_gbs": value / world * step_bytes / 1e9,
+                          "frac": value / world * step_bytes / 1e9 / peak},
+        "forms": {"fp64_plain": {"value": value64, "ms_per_step": ms64 / k64, "steps": k64},
+                  "fp32_over_fp64": value / world / value64},
+        "kernels_ms_per_step": {k: v[1] / max(1, v[0]) for k, v in prof.items()},
+        "meteo_update_s": meteo_s,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
+        except Exception as e:  # reported, never silently replaced
+            line["cpu_baseline"] = {"error": str(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank)
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

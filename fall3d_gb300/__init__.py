@@ -1,0 +1,458 @@
+"""fall3d_gb300 -- GB300-native transport step of FALL3D 7.0.
+
+The compute path is the CUDA library ``libfall3d_gb300.so`` built in-tree for
+sm_103a (``fall3d_gb300/build.py``); this module is its Python host mirror.
+It exposes
+
+* the fine-grained entry points with the reference subroutines' names and
+  arguments (``setbcc``, ``advctzc``, ``advctx``, ... ``finddt``), which take
+  numpy arrays (host memory, staged by the library) or CUDA tensors (device
+  memory, used in place);
+* ``Context``: one scenario resident on the GPU (``f3d_ctx_*``), driven by
+  ``meteo``/``source``/``step`` or by the Fall3d.f90 time loop ``run``.
+
+There is no CPU fallback: every call goes through the CUDA library, and
+``load()`` raises if the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfall3d_gb300.so")
+
+PREC_FP64, PREC_FP32 = 64, 32
+
+
+class F3DError(RuntimeError):
+    """A non-zero status returned by the CUDA library."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+I = C.c_int
+D = C.c_double
+VP = C.c_void_p
+IP = C.POINTER(C.c_int)
+DP = C.POINTER(C.c_double)
+
+
+def load(build_if_missing: bool = False):
+    """Loads the CUDA library (raising if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if build_if_missing:
+            from . import build as _b
+
+            _b.build()
+        else:
+            raise ImportError(f"{LIB_PATH} is not built; run fall3d_gb300/build.py "
+                              "(there is no CPU fallback)")
+    lib = C.CDLL(LIB_PATH)
+    fine = {
+        "f3d_setbcc": [VP, IP, IP, IP, IP, IP, VP, VP, VP, VP, VP, VP, VP],
+        "f3d_advctzc": [VP, IP, IP, IP, IP, IP, VP, VP, VP, DP, IP],
+        "f3d_advctx": [VP, IP, IP, IP, IP, IP, VP, DP, DP, VP, IP],
+        "f3d_advcty": [VP, IP, IP, IP, IP, IP, VP, DP, DP, VP, IP],
+        "f3d_diffz": [VP, IP, IP, IP, IP, IP, VP, DP, VP, VP, VP],
+        "f3d_diffx": [VP, IP, IP, IP, IP, IP, DP, DP, VP, VP, VP],
+        "f3d_diffy": [VP, IP, IP, IP, IP, IP, DP, DP, VP, VP, VP],
+        "f3d_wetdep": [VP, VP, IP, IP, IP, IP, IP, IP, DP, VP, VP, VP, VP, VP],
+        "f3d_accum": [VP, VP, IP, IP, IP, IP, IP, IP, VP, DP, VP, VP],
+        "f3d_clip": [VP, IP, IP, IP, IP, IP, IP],
+        "f3d_cmass2d": [VP, VP, VP, VP, VP, IP, IP, IP, IP, IP, IP, IP, IP, DP, DP, VP, DP, DP],
+        "f3d_cmass3d": [VP, VP, VP, VP, IP, IP, IP, IP, DP, DP, VP, DP, DP, DP, DP],
+        "f3d_getc0": [VP, VP, VP, IP, IP, IP, IP],
+        "f3d_setsrc": [VP, IP, IP, IP, IP, IP, VP, VP, VP, VP, VP, VP, VP, DP, DP, DP],
+        "f3d_finddt": [IP, IP, IP, IP, DP, DP, VP, VP, VP, VP, VP, VP, VP, VP, DP, DP, DP],
+        "f3d_kappa3": [IP, IP, IP, IP, IP, IP, DP, DP, DP, DP, DP, DP, DP, VP, VP, VP, VP, VP, VP,
+                       VP, VP, VP, VP, VP],
+        "f3d_setvset": [IP, IP, IP, IP, IP, IP, VP, VP, VP, VP, VP, VP, IP, DP, VP, DP],
+        "f3d_setvdrydep": [IP, IP, IP, VP, VP, VP, VP, VP, VP, VP, VP, VP],
+        "f3d_meteo_scale": [IP, IP, IP, IP, DP, DP, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP],
+        "f3d_ctx_create": [VP, C.POINTER(VP)],
+        "f3d_ctx_destroy": [VP],
+        "f3d_ctx_footprint": [VP, C.POINTER(C.c_longlong)],
+        "f3d_meteo": [VP] + [VP] * 12,
+        "f3d_source": [VP, I, VP, VP, VP, VP],
+        "f3d_step": [VP],
+        "f3d_budget": [VP, DP, DP, DP, DP],
+        "f3d_get_state": [VP, IP, DP, DP, DP, DP, DP, DP],
+        "f3d_set_time": [VP, D, I],
+        "f3d_download": [VP, VP, VP, VP, VP, VP],
+        "f3d_upload_state": [VP, VP, VP, VP, D, D, D],
+        "f3d_download_coeffs": [VP] + [VP] * 7,
+        "f3d_download_iters": [VP, VP],
+        "f3d_get_cd": [VP, DP],
+        "f3d_outputs": [VP, VP, VP, VP],
+        "f3d_run": [VP, VP, VP, D, D, I, VP, I, IP],
+        "f3d_run_reset": [VP],
+        "f3d_sync": [VP],
+        "f3d_last_error": [C.c_char_p, I],
+        "f3d_ctx_stream": [VP, C.POINTER(VP)],
+        "f3d_profile_enable": [VP, I],
+        "f3d_profile_read": [VP, I, C.c_char_p, I, C.POINTER(C.c_longlong), DP, IP],
+    }
+    for name, args in fine.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = I
+    lib.f3d_version.restype = C.c_char_p
+    lib.f3d_version.argtypes = []
+    lib.f3d_kernel_launches.restype = C.c_longlong
+    lib.f3d_kernel_launches.argtypes = []
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    lib = load()
+    buf = C.create_string_buffer(1024)
+    lib.f3d_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc):
+    if rc != 0:
+        raise F3DError(rc, last_error())
+
+
+def kernel_launches() -> int:
+    return int(load().f3d_kernel_launches())
+
+
+def _addr(a):
+    """Address of a numpy array (host) or a CUDA tensor (device); None -> NULL."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags.c_contiguous, "arrays must be C-contiguous"
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        assert a.is_contiguous(), "tensors must be contiguous"
+        return a.data_ptr()
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def _i(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def _d(v):
+    return C.byref(C.c_double(float(v)))
+
+
+# ---------------------------------------------------------------------------
+# Fine-grained entry points (reference subroutine argument lists).
+# ---------------------------------------------------------------------------
+
+def setbcc(c, nx, ny, nz, nz_loc, iz_loc, vx, vy, vz, vset, vdep, rkver, dz):
+    """Sources/setbcc.f90:1 -- ghost layers of one class, in place."""
+    _check(load().f3d_setbcc(_addr(c), _i(nx), _i(ny), _i(nz), _i(nz_loc), _i(iz_loc), _addr(vx),
+                             _addr(vy), _addr(vz), _addr(vset), _addr(vdep), _addr(rkver), _addr(dz)))
+
+
+def advctzc(c, nx, ny, nz, nz_loc, iz_loc, vz, vset, dz, dt, lmeth=1):
+    """Sources/advctzc.f90:1 -- vertical advection + settling, in place."""
+    _check(load().f3d_advctzc(_addr(c), _i(nx), _i(ny), _i(nz), _i(nz_loc), _i(iz_loc), _addr(vz),
+                              _addr(vset), _addr(dz), _d(dt), _i(lmeth)))
+
+
+def advctx(c, nx, ny, nz, nz_loc, iz_loc, vx, dx, dt, work=None, lmeth=1):
+    """Sources/advctx.f90:1"""
+    _check(load().f3d_advctx(_addr(c), _i(nx), _i(ny), _i(nz), _i(nz_loc), _i(iz_loc), _addr(vx),
+                             _d(dx), _d(dt), None, _i(lmeth)))
+
+
+def advcty(c, nx, ny, nz, nz_loc, iz_loc, vy, dy, dt, work=None, lmeth=1):
+    """Sources/advcty.f90:1"""
+    _check(load().f3d_advcty(_addr(c), _i(nx), _i(ny), _i(nz), _i(nz_loc), _i(iz_loc), _addr(vy),
+                             _d(dy), _d(dt), None, _i(lmeth)))
+
+
+def diffz(c, nx, ny, nz, nz_loc, iz_loc, dz, dt, rkver, rho, work=None):
+    """Sources/diffz.f90:1"""
+    _check(load().f3d_diffz(_addr(c), _i(nx), _i(ny), _i(nz), _i(nz_loc), _i(iz_loc), _addr(dz),
+                            _d(dt), _addr(rkver), _addr(rho), None))
+
+
+def diffx(c, nx, ny, nz, nz_loc, iz_loc, dx, dt, rkhor, rho, work=None):
+    """Sources/diffx.f90:1"""
+    _check(load().f3d_diffx(_addr(c), _i(nx), _i(ny), _i(nz), _i(nz_loc), _i(iz_loc), _d(dx), _d(dt),
+                            _addr(rkhor), _addr(rho), None))
+
+
+def diffy(c, nx, ny, nz, nz_loc, iz_loc, dy, dt, rkhor, rho, work=None):
+    """Sources/diffy.f90:1"""
+    _check(load().f3d_diffy(_addr(c), _i(nx), _i(ny), _i(nz), _i(nz_loc), _i(iz_loc), _d(dy), _d(dt),
+                            _addr(rkhor), _addr(rho), None))
+
+
+def wetdep(c, cwet, ic, nx, ny, nz, nz_loc, iz_loc, dt, diam, zlayer, dz, zi, prate):
+    """Sources/wetdep.f90:1 (cwet is the whole (nx,ny,0:nc) array; ic 1-based)."""
+    _check(load().f3d_wetdep(_addr(c), _addr(cwet), _i(ic), _i(nx), _i(ny), _i(nz), _i(nz_loc),
+                             _i(iz_loc), _d(dt), _addr(diam), _addr(zlayer), _addr(dz), _addr(zi),
+                             _addr(prate)))
+
+
+def accum(c, cdry, ic, nx, ny, nz, nz_loc, iz_loc, vz, dt, vset, vdep):
+    """Sources/accum.f90:1 (cdry is the whole (nx,ny,0:nc) array; ic 1-based)."""
+    _check(load().f3d_accum(_addr(c), _addr(cdry), _i(ic), _i(nx), _i(ny), _i(nz), _i(nz_loc),
+                            _i(iz_loc), _addr(vz), _d(dt), _addr(vset), _addr(vdep)))
+
+
+def clip(c, nx, ny, nz, nc, ic_loc=1, nc_loc=None):
+    """Sources/sizloop.f90:77-78"""
+    _check(load().f3d_clip(_addr(c), _i(nx), _i(ny), _i(nz), _i(nc), _i(ic_loc),
+                           _i(nc if nc_loc is None else nc_loc)))
+
+
+def cmass2d(c, vx, vy, vz, vset, nx, ny, nz, nc, ic_loc, nc_loc, iz_loc, nz_loc, dx, dy, dz, dt,
+            outmass):
+    """Sources/cmass2d.f90:1 -- returns outmass + outflow of the step."""
+    om = C.c_double(float(outmass))
+    _check(load().f3d_cmass2d(_addr(c), _addr(vx), _addr(vy), _addr(vz), _addr(vset), _i(nx), _i(ny),
+                              _i(nz), _i(nc), _i(ic_loc), _i(nc_loc), _i(iz_loc), _i(nz_loc), _d(dx),
+                              _d(dy), _addr(dz), _d(dt), C.byref(om)))
+    return om.value
+
+
+def cmass3d(c, cload, cdry, cwet, nx, ny, nz, nc, dx, dy, dz):
+    """Sources/cmass3d.f90:1 -- (massvol, massdep, massdry, masswet)."""
+    out = [C.c_double() for _ in range(4)]
+    _check(load().f3d_cmass3d(_addr(c), _addr(cload), _addr(cdry), _addr(cwet), _i(nx), _i(ny), _i(nz),
+                              _i(nc), _d(dx), _d(dy), _addr(dz), *[C.byref(o) for o in out]))
+    return tuple(o.value for o in out)
+
+
+def getc0(cdry, cwet, cload, nx, ny, nc, np_):
+    """Sources/endstep.f90:80 getc0 + cload = cdry + cwet."""
+    _check(load().f3d_getc0(_addr(cdry), _addr(cwet), _addr(cload), _i(nx), _i(ny), _i(nc), _i(np_)))
+
+
+def setsrc(c, nx, ny, nz, nc, nsou, isrc, jsrc, ksrc, tmrat, dz, zlayer, Hm1, dX1, dX2, dt):
+    """Sources/setsrc.f90:1 (tmrat already scaled by Hm1)."""
+    _check(load().f3d_setsrc(_addr(c), _i(nx), _i(ny), _i(nz), _i(nc), _i(nsou), _addr(isrc),
+                             _addr(jsrc), _addr(ksrc), _addr(tmrat), _addr(dz), _addr(zlayer),
+                             _addr(Hm1), _d(dX1), _d(dX2), _d(dt)))
+
+
+def finddt(nx, ny, nz, nc, dX1, dX2, dz, vx, vy, vz, vset, rkh1, rkhor, rkver, safety_factor=0.9):
+    """Sources/finddt.f90:1 -- returns (dt, dtc)."""
+    dt, dtc = C.c_double(), C.c_double()
+    _check(load().f3d_finddt(_i(nx), _i(ny), _i(nz), _i(nc), _d(dX1), _d(dX2), _addr(dz), _addr(vx),
+                             _addr(vy), _addr(vz), _addr(vset), _addr(rkh1), _addr(rkhor), _addr(rkver),
+                             _d(safety_factor), C.byref(dt), C.byref(dtc)))
+    return dt.value, dtc.value
+
+
+def kappa3(nx, ny, nz, modkv, modkh, coord_sys, rkv0, rkh0, Csh, dX1, dX2, dx, dy, dz, zlayer, Hm1,
+           vx, vy, vptemp, ustar, zi, rl, rkver, rkhor):
+    """Sources/kappa3.f90:1 (rkver, rkhor in/out)."""
+    _check(load().f3d_kappa3(_i(nx), _i(ny), _i(nz), _i(modkv), _i(modkh), _i(coord_sys), _d(rkv0),
+                             _d(rkh0), _d(Csh), _d(dX1), _d(dX2), _d(dx), _d(dy), _addr(dz),
+                             _addr(zlayer), _addr(Hm1), _addr(vx), _addr(vy), _addr(vptemp),
+                             _addr(ustar), _addr(zi), _addr(rl), _addr(rkver), _addr(rkhor)))
+
+
+def setvset(nx, ny, nz, nc, np_, modv, diam, rhop, psi, sphe, tempe, rho, aggregate, vset_factor,
+            vset, cd):
+    """Sources/setvset.f90:1 with the SAVEd cd made explicit; returns the exit cd."""
+    cdv = C.c_double(float(cd))
+    _check(load().f3d_setvset(_i(nx), _i(ny), _i(nz), _i(nc), _i(np_), _i(modv), _addr(diam),
+                              _addr(rhop), _addr(psi), _addr(sphe), _addr(tempe), _addr(rho),
+                              _i(aggregate), _d(vset_factor), _addr(vset), C.byref(cdv)))
+    return cdv.value
+
+
+def setvdrydep(nx, ny, nc, diam, zlayer, ldu, rl, znt, ustar, tempe, rho, vdep):
+    """Sources/setvdrydep.f90:1 (tempe, rho: the k=1 plane)."""
+    _check(load().f3d_setvdrydep(_i(nx), _i(ny), _i(nc), _addr(diam), _addr(zlayer), _addr(ldu),
+                                 _addr(rl), _addr(znt), _addr(ustar), _addr(tempe), _addr(rho),
+                                 _addr(vdep)))
+
+
+def meteo_scale(nx, ny, nz, coord_sys, dX1, dX2, dz, Hm1, topg, vx, vy, vz, rho, rkhor, rkh1, divu):
+    """Sources/meteo.f90:108-123 + corvver.f90 + setdivu.f90 (in place)."""
+    _check(load().f3d_meteo_scale(_i(nx), _i(ny), _i(nz), _i(coord_sys), _d(dX1), _d(dX2), _addr(dz),
+                                  _addr(Hm1), _addr(topg), _addr(vx), _addr(vy), _addr(vz), _addr(rho),
+                                  _addr(rkhor), _addr(rkh1), _addr(divu)))
+
+
+# ---------------------------------------------------------------------------
+# Coarse context.
+# ---------------------------------------------------------------------------
+
+class Context:
+    """One scenario resident on the GPU (the coarse C API, f3d_ctx_*)."""
+
+    def __init__(self, scen, precision: int = PREC_FP64):
+        self.lib = load()
+        self.s = scen
+        g = scen.grid
+        self.nx, self.ny, self.nz, self.nc = g["nx"], g["ny"], g["nz"], g["nc"]
+        self.precision = precision
+        self._grid = _abi.make_grid(g, precision)
+        h = VP()
+        _check(self.lib.f3d_ctx_create(C.addressof(self._grid.struct), C.byref(h)))
+        self.h = h
+
+    @staticmethod
+    def footprint(scen, precision=PREC_FP64) -> int:
+        g = _abi.make_grid(scen.grid, precision)
+        b = C.c_longlong()
+        _check(load().f3d_ctx_footprint(C.addressof(g.struct), C.byref(b)))
+        return int(b.value)
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.f3d_ctx_destroy(self.h)
+            self.h = VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- meteorology / sources / step -----------------------------------
+    def meteo(self, it=0, fields=None):
+        """meteo.f90:19-149 for DBS snapshot ``it`` of the scenario (or for an
+        explicit dict of raw fields, numpy or CUDA tensors)."""
+        if fields is None:
+            m = self.s.met
+            fields = {k: np.ascontiguousarray(m[k][it]) for k in
+                      ("u", "v", "w", "t", "tp", "rho", "ust", "pblh", "rmol", "znt", "prate")}
+            fields["ldu"] = np.ascontiguousarray(m["ldu"])
+        keys = ("u", "v", "w", "t", "tp", "rho", "ust", "pblh", "rmol", "znt", "prate", "ldu")
+        _check(self.lib.f3d_meteo(self.h, *[_addr(fields.get(k)) for k in keys]))
+
+    def source(self, iint=0):
+        """source.f90 for interval ``iint`` of the scenario's source series."""
+        sr = self.s.src
+        off = int(np.sum(sr["nsou"][:iint]))
+        n = int(sr["nsou"][iint])
+        arrs = [np.ascontiguousarray(sr[k][off:off + n], dtype=np.int32) for k in ("isrc", "jsrc", "ksrc")]
+        tm = np.ascontiguousarray(sr["tmrat"][off * self.nc:(off + n) * self.nc])
+        _check(self.lib.f3d_source(self.h, n, *[_addr(a) for a in arrs], _addr(tm)))
+
+    def step(self, n=1):
+        for _ in range(n):
+            _check(self.lib.f3d_step(self.h))
+
+    def sync(self):
+        _check(self.lib.f3d_sync(self.h))
+
+    def set_time(self, time, iiter):
+        _check(self.lib.f3d_set_time(self.h, float(time), int(iiter)))
+
+    # -- state -------------------------------------------------------------
+    def state(self):
+        it = C.c_int()
+        v = [C.c_double() for _ in range(6)]
+        _check(self.lib.f3d_get_state(self.h, C.byref(it), *[C.byref(x) for x in v]))
+        cd = C.c_double()
+        _check(self.lib.f3d_get_cd(self.h, C.byref(cd)))
+        t, dt, dtc, eru, out, fr = (x.value for x in v)
+        return dict(iiter=it.value, time=t, dt=dt, dtc=dtc, erumass=eru, outmass=out, flowrate=fr,
+                    cd=cd.value)
+
+    def fields(self):
+        nx, ny, nz, nc = self.nx, self.ny, self.nz, self.nc
+        c = np.zeros((nc, nz + 2, ny + 2, nx + 2))
+        cdry = np.zeros((nc + 1, ny, nx))
+        cwet = np.zeros((nc + 1, ny, nx))
+        vset = np.zeros((nc, nz, ny, nx))
+        vdep = np.zeros((nc, ny, nx))
+        _check(self.lib.f3d_download(self.h, _addr(c), _addr(cdry), _addr(cwet), _addr(vset),
+                                     _addr(vdep)))
+        return dict(c=c, cdry=cdry, cwet=cwet, vset=vset, vdep=vdep)
+
+    def download_c(self, out):
+        """Concentrations into ``out`` (numpy or CUDA float64, (nc,nz+2,ny+2,nx+2))."""
+        _check(self.lib.f3d_download(self.h, _addr(out), None, None, None, None))
+
+    def coeffs(self):
+        arrs = [np.zeros((self.nz, self.ny, self.nx)) for _ in range(7)]
+        _check(self.lib.f3d_download_coeffs(self.h, *[_addr(a) for a in arrs]))
+        return dict(zip(("vx", "vy", "vz", "rho", "rkhor", "rkh1", "rkver"), arrs))
+
+    def iters(self):
+        it = np.zeros((self.nc, self.nz, self.ny, self.nx), np.int32)
+        _check(self.lib.f3d_download_iters(self.h, _addr(it)))
+        return it
+
+    def budget(self):
+        v = [C.c_double() for _ in range(4)]
+        _check(self.lib.f3d_budget(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("massvol", "massdep", "massdry", "masswet"), (x.value for x in v)))
+
+    def outputs(self):
+        a = [np.zeros((self.ny, self.nx)) for _ in range(3)]
+        _check(self.lib.f3d_outputs(self.h, *[_addr(x) for x in a]))
+        return dict(load=a[0], col_mass=a[1], c_grnd=a[2])
+
+    def upload_state(self, c=None, cdry=None, cwet=None, erumass=0.0, outmass=0.0, cd=1.0):
+        _check(self.lib.f3d_upload_state(self.h, _addr(c), _addr(cdry), _addr(cwet), float(erumass),
+                                         float(outmass), float(cd)))
+
+    # -- the Fall3d.f90 time loop -------------------------------------------
+    def run(self, beg_time=None, end_time=None, max_steps=0, log_cap=4096, met=None, src=None):
+        """Sources/Fall3d.f90:73-121 on the device; returns the mass-budget log."""
+        met = met or _abi.make_met(self.s.met)
+        src = src or _abi.make_src(self.s.src)
+        recs = (_abi.F3DLogRecord * log_cap)()
+        n = C.c_int()
+        _check(self.lib.f3d_run(self.h, C.addressof(met.struct), C.addressof(src.struct),
+                                self.s.beg_time if beg_time is None else float(beg_time),
+                                self.s.end_time if end_time is None else float(end_time),
+                                int(max_steps), C.addressof(recs), log_cap, C.byref(n)))
+        return _abi.log_array(recs, n.value)
+
+    def run_reset(self):
+        _check(self.lib.f3d_run_reset(self.h))
+
+    # -- timing ------------------------------------------------------------
+    def stream_handle(self) -> int:
+        """The cudaStream_t of this context (for CUDA events on it)."""
+        p = VP()
+        _check(self.lib.f3d_ctx_stream(self.h, C.byref(p)))
+        return int(p.value or 0)
+
+    def profile(self, enable: bool = True):
+        _check(self.lib.f3d_profile_enable(self.h, int(enable)))
+
+    def profile_read(self):
+        """{kernel: (launches, total_ms)} recorded with CUDA events on the
+        context's stream since profile(True)."""
+        cap, nl = 64, 32
+        names = C.create_string_buffer(cap * nl)
+        cnt = (C.c_longlong * cap)()
+        ms = (C.c_double * cap)()
+        nk = C.c_int()
+        _check(self.lib.f3d_profile_read(self.h, cap, names, nl, cnt, ms, C.byref(nk)))
+        out = {}
+        for i in range(min(nk.value, cap)):
+            nm = names.raw[i * nl:(i + 1) * nl].split(b"\0", 1)[0].decode()
+            out[nm] = (int(cnt[i]), float(ms[i]))
+        return out
+
+
+def version() -> str:
+    return load().f3d_version().decode()

@@ -1,0 +1,351 @@
+// f3d_budget.cu -- mass budgets, CFL step and output fields.
+//
+// The reference accumulates its budgets sequentially in binary64
+// (Sources/cmass2d.f90:42-104, Sources/cmass3d.f90:29-47).  Here each sum is
+// a deterministic two-level reduction in double-double (TwoSum), i.e. the
+// exact sum rounded once; it differs from the reference's sequential
+// rounding by at most (N-1)*u*sum|terms| (all cmass2d/cmass3d terms are >= 0
+// after the clip, so that bound is relative to the result).  The grid shape
+// depends only on the problem size, so results are reproducible run to run.
+#include <algorithm>
+
+#include "f3d_internal.h"
+
+namespace f3d {
+
+namespace {
+constexpr int RB = 256;   // threads per reduction block
+constexpr int RMAXB = 1024;  // reduction blocks
+
+int reduce_blocks(long long n) {
+  return (int)std::max<long long>(1, std::min<long long>((n + RB - 1) / RB, RMAXB));
+}
+
+template <int NS>
+__device__ void block_store_dd(DD (&v)[NS], DD* partial) {
+  __shared__ DD sh[RB / 32][NS];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < NS; ++s)
+    for (int off = 16; off > 0; off >>= 1) v[s] = dd_add(v[s], dd_shfl_down(v[s], off));
+  if (lane == 0)
+#pragma unroll
+    for (int s = 0; s < NS; ++s) sh[wid][s] = v[s];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      DD a = sh[0][s];
+      for (int w = 1; w < RB / 32; ++w) a = dd_add(a, sh[w][s]);
+      partial[(long long)blockIdx.x * NS + s] = a;
+    }
+  }
+}
+
+// Sums nblk partials of NS sums; out[s] = (hi(sum_s) * f0) * f1, or with
+// accum, out[s] = out[s] + hi(sum_s) (outmass = outmass + sum(mymass),
+// cmass2d.f90:104).
+template <int NS>
+__global__ void k_reduce_finish(const DD* partial, int nblk, double f0, double f1, double* out,
+                                int accum) {
+  DD v[NS];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) v[s] = dd_zero();
+  for (int b = threadIdx.x; b < nblk; b += RB)
+#pragma unroll
+    for (int s = 0; s < NS; ++s) v[s] = dd_add(v[s], partial[(long long)b * NS + s]);
+  __shared__ DD sh[RB / 32][NS];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int s = 0; s < NS; ++s)
+    for (int off = 16; off > 0; off >>= 1) v[s] = dd_add(v[s], dd_shfl_down(v[s], off));
+  if (lane == 0)
+#pragma unroll
+    for (int s = 0; s < NS; ++s) sh[wid][s] = v[s];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      DD a = sh[0][s];
+      for (int w = 1; w < RB / 32; ++w) a = dd_add(a, sh[w][s]);
+      if (accum)
+        out[s] = out[s] + a.hi;
+      else
+        out[s] = a.hi * f0 * f1;
+    }
+  }
+}
+}  // namespace
+
+size_t reduce_scratch_bytes(long long nterms, int nsums) {
+  return sizeof(DD) * (size_t)reduce_blocks(nterms) * nsums + 256;
+}
+
+// ----------------------------------------------------------- cmass2d
+// Terms of Sources/cmass2d.f90:42-102: x faces (ic, j, k, left/right),
+// y faces (ic, i, k, down/up), top (ic, i, j).
+template <class T>
+__global__ void k_cmass2d(const T* c, const double* vx, const double* vy, const double* vz,
+                          const double* vset, Dims d, int ic_loc, int nc_loc, int iz_loc,
+                          int nz_loc, double dx, double dy, const double* dz, double dt,
+                          long long n1, long long n2, long long n3, DD* partial) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long hb = d.halo(), s3 = d.cells();
+  DD acc[1] = {dd_zero()};
+  const long long ntot = n1 + n2 + n3;
+  for (long long t = blockIdx.x * (long long)RB + threadIdx.x; t < ntot;
+       t += (long long)gridDim.x * RB) {
+    double term;
+    if (t < n1) {
+      const int side = (int)(t & 1);
+      long long r = t >> 1;
+      const int k = (int)(r % nz_loc) + iz_loc;
+      r /= nz_loc;
+      const int j = (int)(r % ny) + 1;
+      const int ic = (int)(r / ny) + ic_loc;
+      double faty = 1.0;
+      if (j == 1 || j == ny) faty = 0.5;
+      const double area = faty * dy * 0.5 * (dz[k] + dz[k - 1]);
+      const T* cc = c + (long long)(ic - 1) * hb;
+      if (side == 0) {
+        const double velo = vx[d.M(1, j, k)], conc = (double)cc[d.C(0, j, k)];
+        term = -(dt * area * velo * conc);
+      } else {
+        const double velo = vx[d.M(nx, j, k)], conc = (double)cc[d.C(nx + 1, j, k)];
+        term = dt * area * velo * conc;
+      }
+    } else if (t < n1 + n2) {
+      const long long u = t - n1;
+      const int side = (int)(u & 1);
+      long long r = u >> 1;
+      const int k = (int)(r % nz_loc) + iz_loc;
+      r /= nz_loc;
+      const int i = (int)(r % nx) + 1;
+      const int ic = (int)(r / nx) + ic_loc;
+      double fatx = 1.0;
+      if (i == 1 || i == nx) fatx = 0.5;
+      const double area = fatx * dx * 0.5 * (dz[k] + dz[k - 1]);
+      const T* cc = c + (long long)(ic - 1) * hb;
+      if (side == 0) {
+        const double velo = vy[d.M(i, 1, k)], conc = (double)cc[d.C(i, 0, k)];
+        term = -(dt * area * velo * conc);
+      } else {
+        const double velo = vy[d.M(i, ny, k)], conc = (double)cc[d.C(i, ny + 1, k)];
+        term = dt * area * velo * conc;
+      }
+    } else {
+      long long r = t - n1 - n2;
+      const int i = (int)(r % nx) + 1;
+      r /= nx;
+      const int j = (int)(r % ny) + 1;
+      const int ic = (int)(r / ny) + ic_loc;
+      double faty = 1.0;
+      if (j == 1 || j == ny) faty = 0.5;
+      double fatx = 1.0;
+      if (i == 1 || i == nx) fatx = 0.5;
+      const double area = fatx * faty * dx * dy;
+      const double velo = vz[d.M(i, j, nz)] + vset[(long long)(ic - 1) * s3 + d.M(i, j, nz)];
+      const double conc = (double)c[(long long)(ic - 1) * hb + d.C(i, j, nz + 1)];
+      term = dt * area * velo * conc;
+    }
+    acc[0] = dd_add_d(acc[0], term);
+  }
+  block_store_dd<1>(acc, partial);
+}
+
+template <class T>
+void launch_cmass2d(const T* c, const double* vx, const double* vy, const double* vz,
+                    const double* vset, Dims d, int ic_loc, int nc_loc, int iz_loc, int nz_loc,
+                    double dx, double dy, const double* dz, double dt, void* scratch,
+                    double* out, cudaStream_t s) {
+  const long long n1 = 2LL * nc_loc * d.ny * nz_loc;
+  const long long n2 = 2LL * nc_loc * d.nx * nz_loc;
+  const long long n3 = (iz_loc + nz_loc - 1 == d.nz) ? (long long)nc_loc * d.nx * d.ny : 0;
+  const int nb = reduce_blocks(n1 + n2 + n3);
+  DD* partial = reinterpret_cast<DD*>(scratch);
+  k_cmass2d<T><<<nb, RB, 0, s>>>(c, vx, vy, vz, vset, d, ic_loc, nc_loc, iz_loc, nz_loc, dx, dy, dz,
+                                 dt, n1, n2, n3, partial);
+  k_reduce_finish<1><<<1, RB, 0, s>>>(partial, nb, 1.0, 1.0, out, 1);
+  count_launch(2);
+}
+
+// ----------------------------------------------------------- cmass3d
+// Sources/cmass3d.f90:29-53: per (i,j,ic) the column trapezoid zmass is
+// accumulated sequentially in k exactly as the reference does; the sums
+// over (i,j,ic) are the reductions.
+template <class T>
+__global__ void k_cmass3d(const T* c, const double* cload, const double* cdry, const double* cwet,
+                          Dims d, int nc, const double* dz, DD* partial) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long hb = d.halo(), pl = d.plane();
+  DD acc[4] = {dd_zero(), dd_zero(), dd_zero(), dd_zero()};
+  const long long ntot = pl * nc;
+  for (long long t = blockIdx.x * (long long)RB + threadIdx.x; t < ntot;
+       t += (long long)gridDim.x * RB) {
+    const long long p = t % pl;
+    const int ic = (int)(t / pl) + 1;
+    const int i = (int)(p % nx) + 1, j = (int)(p / nx) + 1;
+    double fatx = 1.0;
+    if (i == 1 || i == nx) fatx = 0.5;
+    double faty = 1.0;
+    if (j == 1 || j == ny) faty = 0.5;
+    const T* cc = c + (long long)(ic - 1) * hb;
+    double zmass = 0.0;
+    double ck = (double)cc[d.C(i, j, 1)];
+    for (int k = 1; k <= nz - 1; ++k) {
+      const double ck1 = (double)cc[d.C(i, j, k + 1)];
+      zmass = zmass + 0.5 * dz[k] * (ck + ck1);
+      ck = ck1;
+    }
+    acc[0] = dd_add_d(acc[0], fatx * faty * zmass);
+    if (ic == 1) {
+      acc[1] = dd_add_d(acc[1], fatx * faty * cload[p]);
+      acc[2] = dd_add_d(acc[2], fatx * faty * cdry[p]);
+      acc[3] = dd_add_d(acc[3], fatx * faty * cwet[p]);
+    }
+  }
+  block_store_dd<4>(acc, partial);
+}
+
+template <class T>
+void launch_cmass3d(const T* c, const double* cload, const double* cdry, const double* cwet,
+                    Dims d, int nc, double dx, double dy, const double* dz, void* scratch,
+                    double* out, cudaStream_t s) {
+  const long long n = d.plane() * nc;
+  const int nb = reduce_blocks(n);
+  DD* partial = reinterpret_cast<DD*>(scratch);
+  k_cmass3d<T><<<nb, RB, 0, s>>>(c, cload, cdry, cwet, d, nc, dz, partial);
+  k_reduce_finish<4><<<1, RB, 0, s>>>(partial, nb, dx, dy, out, 0);
+  count_launch(2);
+}
+
+// ------------------------------------------------------------- getc0
+// Sources/endstep.f90:94-104 then cload = cdry + cwet (endstep.f90:35,60).
+__global__ void k_getc0(double* cdry, double* cwet, double* cload, Dims d, int nc, int np) {
+  const long long pl = d.plane();
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= pl) return;
+  double sd = 0.0, sw = 0.0;
+  for (int ic = 1; ic <= np; ++ic) {
+    sd = sd + cdry[ic * pl + p];
+    sw = sw + cwet[ic * pl + p];
+  }
+  cdry[p] = sd;
+  cwet[p] = sw;
+  for (int ic = 0; ic <= nc; ++ic) cload[ic * pl + p] = cdry[ic * pl + p] + cwet[ic * pl + p];
+}
+
+void launch_getc0(double* cdry, double* cwet, double* cload, Dims d, int nc, int np,
+                  cudaStream_t s) {
+  const long long pl = d.plane();
+  k_getc0<<<(unsigned)((pl + 255) / 256), 256, 0, s>>>(cdry, cwet, cload, d, nc, np);
+  count_launch();
+}
+
+// ------------------------------------------------------------ finddt
+// Sources/finddt.f90:26-57.  MAX is exact and order independent, so the
+// largest dtcni is found with a bitwise atomicMax on the (non-negative)
+// binary64 patterns; NaN terms are skipped as MAX(dtcn,NaN) keeps dtcn.
+__global__ void k_finddt(Dims d, int nc, double dX1, double dX2, const double* dz,
+                         const double* vx, const double* vy, const double* vz,
+                         const double* vset, const double* rkh1, const double* rkhor,
+                         const double* rkver, unsigned long long* dtcn_bits) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long s3 = d.cells();
+  double best = 0.0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < s3 * nc;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long m = t % s3;
+    const int ic = (int)(t / s3);
+    const int i = (int)(m % nx) + 1;
+    const long long r = m / nx;
+    const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
+    const double* vs = vset + (long long)ic * s3;
+    const double ddz = fmin2(dz[k - 1], dz[k]);
+    double dvsetdz;
+    if (k == 1)
+      dvsetdz = (vs[d.M(i, j, 2)] - vs[d.M(i, j, 1)]) / (dz[1]);
+    else if (k == nz)
+      dvsetdz = (vs[d.M(i, j, nz)] - vs[d.M(i, j, nz - 1)]) / (dz[nz - 1]);
+    else
+      dvsetdz = (vs[d.M(i, j, k + 1)] - vs[d.M(i, j, k - 1)]) / (dz[k] + dz[k - 1]);
+    const double dtcni = (2.0 * rkh1[m] / (dX1 * dX1)) + (fabs(vx[m]) / dX1) +
+                         (2.0 * rkhor[m] / (dX2 * dX2)) + (fabs(vy[m]) / dX2) +
+                         (2.0 * rkver[m] / (ddz * ddz)) + (fabs((vz[m] + vs[m])) / ddz) +
+                         (fabs(dvsetdz));
+    best = fmax2(best, dtcni);
+  }
+  for (int off = 16; off > 0; off >>= 1) best = fmax2(best, __shfl_down_sync(0xffffffffu, best, off));
+  if ((threadIdx.x & 31) == 0 && best > 0.0)
+    atomicMax(dtcn_bits, (unsigned long long)__double_as_longlong(best));
+}
+
+void launch_finddt(Dims d, int nc, double dX1, double dX2, const double* dz, const double* vx,
+                   const double* vy, const double* vz, const double* vset, const double* rkh1,
+                   const double* rkhor, const double* rkver, unsigned long long* dtcn_bits,
+                   cudaStream_t s) {
+  const long long n = d.cells() * nc;
+  const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 8);
+  k_finddt<<<nb, 256, 0, s>>>(d, nc, dX1, dX2, dz, vx, vy, vz, vset, rkh1, rkhor, rkver, dtcn_bits);
+  count_launch();
+}
+
+// ----------------------------------------------------------- outputs
+// Sources/printres_nc.f90:104-122 (LOAD), :218-246 (COL_MASS),
+// :391-410 (C_GRND).
+template <class T>
+__global__ void k_outputs(const T* c, const double* cload, Dims d, int np, const double* dz,
+                          const double* Hm1, double* load, double* col_mass, double* c_grnd) {
+  const long long pl = d.plane();
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= pl) return;
+  const int i = (int)(p % d.nx) + 1, j = (int)(p / d.nx) + 1;
+  const long long hb = d.halo();
+  const double h = Hm1[p];
+  if (load) load[p] = cload[p] / h;
+  if (col_mass) {
+    double colm = 0.0, wprev = 0.0;
+    for (int ic = 1; ic <= np; ++ic) wprev = wprev + (double)c[(ic - 1) * hb + d.C(i, j, 1)] / h;
+    for (int k = 1; k <= d.nz - 1; ++k) {
+      double wnext = 0.0;
+      for (int ic = 1; ic <= np; ++ic) wnext = wnext + (double)c[(ic - 1) * hb + d.C(i, j, k + 1)] / h;
+      colm = colm + dz[k] * 0.5 * (wprev + wnext);
+      wprev = wnext;
+    }
+    col_mass[p] = 1e3 * colm;
+  }
+  if (c_grnd) {
+    double sum = 0.0;
+    for (int ic = 1; ic <= np; ++ic) sum = sum + (double)c[(ic - 1) * hb + d.C(i, j, 1)] / h;
+    c_grnd[p] = 1e3 * sum;
+  }
+}
+
+template <class T>
+void launch_outputs(const T* c, const double* cload, Dims d, int np, const double* dz,
+                    const double* Hm1, double* load, double* col_mass, double* c_grnd,
+                    cudaStream_t s) {
+  const long long pl = d.plane();
+  k_outputs<T><<<(unsigned)((pl + 127) / 128), 128, 0, s>>>(c, cload, d, np, dz, Hm1, load, col_mass,
+                                                           c_grnd);
+  count_launch();
+}
+
+template void launch_cmass2d<double>(const double*, const double*, const double*, const double*,
+                                     const double*, Dims, int, int, int, int, double, double,
+                                     const double*, double, void*, double*, cudaStream_t);
+template void launch_cmass2d<float>(const float*, const double*, const double*, const double*,
+                                    const double*, Dims, int, int, int, int, double, double,
+                                    const double*, double, void*, double*, cudaStream_t);
+template void launch_cmass3d<double>(const double*, const double*, const double*, const double*,
+                                     Dims, int, double, double, const double*, void*, double*,
+                                     cudaStream_t);
+template void launch_cmass3d<float>(const float*, const double*, const double*, const double*,
+                                    Dims, int, double, double, const double*, void*, double*,
+                                    cudaStream_t);
+template void launch_outputs<double>(const double*, const double*, Dims, int, const double*,
+                                     const double*, double*, double*, double*, cudaStream_t);
+template void launch_outputs<float>(const float*, const double*, Dims, int, const double*,
+                                    const double*, double*, double*, double*, cudaStream_t);
+
+}  // namespace f3d

@@ -1,0 +1,919 @@
+// f3d_ctx.cu -- the coarse context API: one scenario resident in HBM.
+//
+// Device layout of one context (all sizes in elements):
+//   c        nc * (nx+2)(ny+2)(nz+2)  binary64 (plain form) or binary32
+//   cdry, cwet, cload   (nc+1) * nx*ny binary64 (ground deposit, all forms)
+//   met      vx vy vz tempe vptemp rho rkhor rkh1 rkver divu: nx*ny*nz each
+//   vset     nc * nx*ny*nz, vdep nc * nx*ny          binary64
+//   2-D      ustar zi rl znt prate ldu                binary64
+//   FP32 form: binary32 copies of vx vy vz rho rkhor rkh1 rkver vset vdep dz
+//   scratch  reduction partials, setvset chain buffers, small results.
+// Everything of one step is enqueued on the context's stream without a host
+// synchronisation; the host keeps only the scalars of the time loop.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fall3d_gpu.h"
+#include "f3d_internal.h"
+
+namespace f3d {
+int ctx_error(int code, const char* msg);
+}
+using namespace f3d;
+
+struct f3d_ctx {
+  f3d_grid g{};
+  Dims d{};
+  int prec = 64;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  // static
+  double *dz = nullptr, *zlayer = nullptr, *Hm1 = nullptr, *topg = nullptr;
+  double *diam = nullptr, *rhop = nullptr, *psi = nullptr, *sphe = nullptr;
+  // met and coefficients (binary64)
+  double *vx = nullptr, *vy = nullptr, *vz = nullptr, *tempe = nullptr, *vptemp = nullptr;
+  double *rho = nullptr, *rkhor = nullptr, *rkh1 = nullptr, *rkver = nullptr, *divu = nullptr;
+  double *vset = nullptr, *vdep = nullptr;
+  double *ustar = nullptr, *zi = nullptr, *rl = nullptr, *znt = nullptr, *prate = nullptr,
+         *ldu = nullptr;
+  int* iters = nullptr;
+  // state
+  double* c64 = nullptr;
+  float* c32 = nullptr;
+  double *cdry = nullptr, *cwet = nullptr, *cload = nullptr;
+  // FP32 copies
+  float *vx32 = nullptr, *vy32 = nullptr, *vz32 = nullptr, *rho32 = nullptr, *rkhor32 = nullptr,
+        *rkh132 = nullptr, *rkver32 = nullptr, *vset32 = nullptr, *vdep32 = nullptr,
+        *dz32 = nullptr;
+  // sources
+  int *isrc = nullptr, *jsrc = nullptr, *ksrc = nullptr;
+  double* tmrat = nullptr;
+  int src_cap = 0, nsou = 0;
+  // scratch
+  void* red_scratch = nullptr;
+  void* vset_scratch = nullptr;
+  double* small = nullptr;  // [0] outmass, [1..4] budget, [8] cd, [16] dtcn bits, [24] status
+  // host scalars of the time loop
+  double time = 0.0, dt = 1.0, dtc = 0.0, erumass = 0.0, flowrate = 0.0;
+  int iiter = 0, have_met = 0;
+  // f3d_run loop state (Fall3d.f90:73-78)
+  int run_started = 0, meteotime = 1, sourcetime = 1;
+  double meteo_time = 0.0, source_time = 0.0;
+  // per-kernel event profiler (f3d_profile_*)
+  int prof = 0;
+  struct ProfRec {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<ProfRec> prof_pending;
+  std::vector<cudaEvent_t> prof_pool;
+  std::vector<std::string> prof_names;
+  std::vector<long long> prof_count;
+  std::vector<double> prof_ms;
+};
+
+namespace {
+
+#define CK(call)                                                                             \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      std::string m_ = std::string(#call) + ": " + cudaGetErrorString(e_);                   \
+      return f3d::ctx_error(F3D_ERR_CUDA, m_.c_str());                                       \
+    }                                                                                        \
+  } while (0)
+
+double* small_outmass(f3d_ctx* x) { return x->small; }
+double* small_budget(f3d_ctx* x) { return x->small + 1; }
+double* small_cd(f3d_ctx* x) { return x->small + 8; }
+unsigned long long* small_dtcn(f3d_ctx* x) {
+  return reinterpret_cast<unsigned long long*>(x->small + 16);
+}
+int* small_status(f3d_ctx* x) { return reinterpret_cast<int*>(x->small + 24); }
+
+template <class T>
+int dalloc(f3d_ctx* x, T** p, size_t n) {
+  if (n == 0) n = 1;
+  void* q = nullptr;
+  if (cudaMalloc(&q, n * sizeof(T)) != cudaSuccess) {
+    cudaGetLastError();
+    return f3d::ctx_error(F3D_ERR_OOM, "device allocation failed");
+  }
+  x->allocs.push_back(q);
+  if (cudaMemsetAsync(q, 0, n * sizeof(T), x->stream) != cudaSuccess)
+    return f3d::ctx_error(F3D_ERR_CUDA, "cudaMemsetAsync failed");
+  *p = reinterpret_cast<T*>(q);
+  return F3D_OK;
+}
+
+int is_dev(const void* p) {
+  if (!p) return 0;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) ? 1 : 0;
+}
+
+int upload(f3d_ctx* x, double* dst, const double* src, size_t n) {
+  CK(cudaMemcpyAsync(dst, src, n * sizeof(double),
+                     is_dev(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, x->stream));
+  return F3D_OK;
+}
+
+long long footprint_bytes(const f3d_grid* g) {
+  const long long nx = g->nx, ny = g->ny, nz = g->nz, nc = g->nc;
+  const long long s3 = nx * ny * nz, pl = nx * ny, halo = (nx + 2) * (ny + 2) * (nz + 2);
+  long long b = 0;
+  b += 8LL * (nz + 1 + nz + 2 * pl + 4 * nc);  // static
+  b += 8LL * 10 * s3;                          // met + coefficients
+  b += 8LL * (s3 * nc + pl * nc + 6 * pl);     // vset, vdep, 2-D
+  b += 4LL * s3 * nc;                          // vsettl iteration counts
+  b += 8LL * 3 * pl * (nc + 1);                // cdry cwet cload
+  if (g->precision == F3D_PREC_FP32) {
+    b += 4LL * halo * nc;
+    b += 4LL * (7 * s3 + s3 * nc + pl * nc + nz + 1);
+  } else {
+    b += 8LL * halo * nc;
+  }
+  b += (long long)f3d::reduce_scratch_bytes(2LL * nc * (nx + ny) * nz + nc * pl, 4);
+  b += (long long)f3d::setvset_scratch_bytes(Dims{g->nx, g->ny, g->nz}, g->np);
+  b += 4096;
+  return b;
+}
+
+// Brackets one launch with events when profiling is on.
+struct ProfScope {
+  f3d_ctx* x;
+  int kind = -1;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEvent_t take() {
+    if (!x->prof_pool.empty()) {
+      cudaEvent_t e = x->prof_pool.back();
+      x->prof_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  ProfScope(f3d_ctx* xx, const char* name) : x(xx) {
+    if (!x->prof) return;
+    for (size_t i = 0; i < x->prof_names.size(); ++i)
+      if (x->prof_names[i] == name) kind = (int)i;
+    if (kind < 0) {
+      kind = (int)x->prof_names.size();
+      x->prof_names.push_back(name);
+      x->prof_count.push_back(0);
+      x->prof_ms.push_back(0.0);
+    }
+    a = take();
+    b = take();
+    cudaEventRecord(a, x->stream);
+  }
+  ~ProfScope() {
+    if (!x->prof) return;
+    cudaEventRecord(b, x->stream);
+    x->prof_pending.push_back({kind, a, b});
+  }
+};
+
+void prof_drain(f3d_ctx* x) {
+  if (x->prof_pending.empty()) return;
+  cudaStreamSynchronize(x->stream);
+  for (auto& r : x->prof_pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    x->prof_ms[r.kind] += ms;
+    x->prof_count[r.kind] += 1;
+    x->prof_pool.push_back(r.a);
+    x->prof_pool.push_back(r.b);
+  }
+  x->prof_pending.clear();
+}
+
+template <class T>
+struct Fields;  // per-precision views of the stencil inputs
+
+template <>
+struct Fields<double> {
+  static double* c(f3d_ctx* x) { return x->c64; }
+  static const double* vx(f3d_ctx* x) { return x->vx; }
+  static const double* vy(f3d_ctx* x) { return x->vy; }
+  static const double* vz(f3d_ctx* x) { return x->vz; }
+  static const double* rho(f3d_ctx* x) { return x->rho; }
+  static const double* rkhor(f3d_ctx* x) { return x->rkhor; }
+  static const double* rkh1(f3d_ctx* x) { return x->rkh1; }
+  static const double* rkver(f3d_ctx* x) { return x->rkver; }
+  static const double* vset(f3d_ctx* x) { return x->vset; }
+  static const double* vdep(f3d_ctx* x) { return x->vdep; }
+  static const double* dz(f3d_ctx* x) { return x->dz; }
+};
+template <>
+struct Fields<float> {
+  static float* c(f3d_ctx* x) { return x->c32; }
+  static const float* vx(f3d_ctx* x) { return x->vx32; }
+  static const float* vy(f3d_ctx* x) { return x->vy32; }
+  static const float* vz(f3d_ctx* x) { return x->vz32; }
+  static const float* rho(f3d_ctx* x) { return x->rho32; }
+  static const float* rkhor(f3d_ctx* x) { return x->rkhor32; }
+  static const float* rkh1(f3d_ctx* x) { return x->rkh132; }
+  static const float* rkver(f3d_ctx* x) { return x->rkver32; }
+  static const float* vset(f3d_ctx* x) { return x->vset32; }
+  static const float* vdep(f3d_ctx* x) { return x->vdep32; }
+  static const float* dz(f3d_ctx* x) { return x->dz32; }
+};
+
+// Sources/sizloop.f90:31-83 for all classes, class-batched sweeps.
+template <class T>
+void sizloop(f3d_ctx* x) {
+  using F = Fields<T>;
+  const Dims d = x->d;
+  const int nz = d.nz, nc = x->g.nc, np = x->g.np;
+  const long long hb = d.halo(), s3 = d.cells(), pl = d.plane();
+  cudaStream_t s = x->stream;
+  T* c = F::c(x);
+  const T dt = (T)x->dt;
+  const T dX1 = (T)x->g.dX1, dX2 = (T)x->g.dX2;
+  auto advx = [&] {
+    ProfScope ps(x, "advctx");
+    launch_advctx<T>(c, hb, d, nz, 1, F::vx(x), dX1, dt, nc, s);
+  };
+  auto advy = [&] {
+    ProfScope ps(x, "advcty");
+    launch_advcty<T>(c, hb, d, nz, 1, F::vy(x), dX2, dt, nc, s);
+  };
+  auto difx = [&] {
+    ProfScope ps(x, "diffx");
+    launch_diffx<T>(c, hb, d, nz, 1, dX1, dt, F::rkh1(x), F::rho(x), nc, s);
+  };
+  auto dify = [&] {
+    ProfScope ps(x, "diffy");
+    launch_diffy<T>(c, hb, d, nz, 1, dX2, dt, F::rkhor(x), F::rho(x), nc, s);
+  };
+  {
+    ProfScope ps(x, "setbcc");
+    launch_setbcc<T>(c, hb, d, nz, 1, F::vx(x), F::vy(x), F::vz(x), F::vset(x), s3, F::vdep(x), pl,
+                     F::rkver(x), F::dz(x), nc, s);
+  }
+  {
+    ProfScope ps(x, "advctzc");
+    launch_advctzc<T>(c, hb, d, nz, 1, F::vz(x), F::vset(x), s3, F::dz(x), dt, nc, s);
+  }
+  // sizloop.f90:42-48: x/y order alternates with the parity of iiter
+  if (x->iiter % 2 == 0) {
+    advx();
+    advy();
+  } else {
+    advy();
+    advx();
+  }
+  {
+    ProfScope ps(x, "diffz");
+    launch_diffz<T>(c, hb, d, nz, 1, F::dz(x), dt, F::rkver(x), F::rho(x), nc, s);
+  }
+  if (x->iiter % 2 == 0) {
+    difx();
+    dify();
+  } else {
+    dify();
+    difx();
+  }
+  if (x->g.wetdep && np > 0) {
+    ProfScope ps(x, "wetdep");
+    launch_wetdep<T>(c, hb, x->cwet, 0, d, nz, 1, x->dt, x->diam, x->zlayer, x->dz, x->zi, x->prate,
+                     np, s);
+  }
+  {
+    ProfScope ps(x, "accum");
+    launch_accum<T>(c, hb, x->cdry, 0, d, 1, x->dt, x->vset, s3, x->vdep, pl, nc, s);
+  }
+  {
+    ProfScope ps(x, "clip");
+    launch_clip<T>(c, hb * nc, s);
+  }
+  {
+    ProfScope ps(x, "cmass2d");
+    launch_cmass2d<T>(c, x->vx, x->vy, x->vz, x->vset, d, 1, nc, 1, nz, x->g.dX1, x->g.dX2, x->dz,
+                      x->dt, x->red_scratch, small_outmass(x), s);
+  }
+}
+
+
+}  // namespace
+
+namespace f3d {
+int ctx_error(int code, const char* msg);
+}
+
+extern "C" {
+
+int f3d_ctx_footprint(const f3d_grid* g, long long* bytes) {
+  if (!g || !bytes) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  *bytes = footprint_bytes(g);
+  return F3D_OK;
+}
+
+int f3d_ctx_destroy(f3d_ctx* x) {
+  if (!x) return F3D_OK;
+  if (x->stream) cudaStreamSynchronize(x->stream);
+  for (auto& r : x->prof_pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (auto e : x->prof_pool) cudaEventDestroy(e);
+  for (void* p : x->allocs) cudaFree(p);
+  if (x->stream) cudaStreamDestroy(x->stream);
+  delete x;
+  return F3D_OK;
+}
+
+int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
+  if (!g || !out) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  if (g->nx < 3 || g->ny < 3 || g->nz < 3) return f3d::ctx_error(F3D_ERR_ARG, "nx, ny, nz must be >= 3");
+  if (g->nc < 1 || g->np < 0 || g->np > g->nc) return f3d::ctx_error(F3D_ERR_ARG, "invalid nc/np");
+  if (g->precision != F3D_PREC_FP64 && g->precision != F3D_PREC_FP32)
+    return f3d::ctx_error(F3D_ERR_ARG, "precision must be 64 or 32");
+  if (g->modv < 1 || g->modv > 4 || g->modkv < 0 || g->modkv > 2 || g->modkh < 0 || g->modkh > 2)
+    return f3d::ctx_error(F3D_ERR_ARG, "invalid model selector");
+  if (!g->dz || !g->zlayer || !g->Hm1 || !g->topg || !g->diam || !g->rhop || !g->psi || !g->sphe)
+    return f3d::ctx_error(F3D_ERR_ARG, "NULL grid array");
+  f3d_ctx* x = new f3d_ctx();
+  x->g = *g;
+  x->g.dz = x->g.zlayer = x->g.Hm1 = x->g.topg = nullptr;
+  x->g.diam = x->g.rhop = x->g.psi = x->g.sphe = nullptr;
+  x->d = Dims{g->nx, g->ny, g->nz};
+  x->prec = g->precision;
+  if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete x;
+    return f3d::ctx_error(F3D_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  const Dims d = x->d;
+  const size_t s3 = (size_t)d.cells(), pl = (size_t)d.plane(), hb = (size_t)d.halo();
+  const size_t nc = (size_t)g->nc, nz = (size_t)g->nz;
+  int rc = 0;
+#define A(p, n) \
+  if (!rc) rc = dalloc(x, &x->p, (n))
+  A(dz, nz + 1);
+  A(zlayer, nz);
+  A(Hm1, pl);
+  A(topg, pl);
+  A(diam, nc);
+  A(rhop, nc);
+  A(psi, nc);
+  A(sphe, nc);
+  A(vx, s3);
+  A(vy, s3);
+  A(vz, s3);
+  A(tempe, s3);
+  A(vptemp, s3);
+  A(rho, s3);
+  A(rkhor, s3);
+  A(rkh1, s3);
+  A(rkver, s3);
+  A(divu, s3);
+  A(vset, s3 * nc);
+  A(vdep, pl * nc);
+  A(ustar, pl);
+  A(zi, pl);
+  A(rl, pl);
+  A(znt, pl);
+  A(prate, pl);
+  A(ldu, pl);
+  A(iters, s3 * nc);
+  A(cdry, pl * (nc + 1));
+  A(cwet, pl * (nc + 1));
+  A(cload, pl * (nc + 1));
+  A(small, 64);
+  if (x->prec == F3D_PREC_FP32) {
+    A(c32, hb * nc);
+    A(vx32, s3);
+    A(vy32, s3);
+    A(vz32, s3);
+    A(rho32, s3);
+    A(rkhor32, s3);
+    A(rkh132, s3);
+    A(rkver32, s3);
+    A(vset32, s3 * nc);
+    A(vdep32, pl * nc);
+    A(dz32, nz + 1);
+  } else {
+    A(c64, hb * nc);
+  }
+#undef A
+  if (!rc) {
+    unsigned char* p = nullptr;
+    rc = dalloc(x, &p, f3d::reduce_scratch_bytes(2LL * g->nc * (g->nx + g->ny) * g->nz +
+                                                      (long long)g->nc * g->nx * g->ny, 4));
+    x->red_scratch = p;
+  }
+  if (!rc) {
+    unsigned char* p = nullptr;
+    rc = dalloc(x, &p, f3d::setvset_scratch_bytes(d, g->np));
+    x->vset_scratch = p;
+  }
+  if (rc) {
+    f3d_ctx_destroy(x);
+    return rc;
+  }
+  // static fields
+  if (!rc) rc = upload(x, x->dz, g->dz, nz + 1);
+  if (!rc) rc = upload(x, x->zlayer, g->zlayer, nz);
+  if (!rc) rc = upload(x, x->Hm1, g->Hm1, pl);
+  if (!rc) rc = upload(x, x->topg, g->topg, pl);
+  if (!rc) rc = upload(x, x->diam, g->diam, nc);
+  if (!rc) rc = upload(x, x->rhop, g->rhop, nc);
+  if (!rc) rc = upload(x, x->psi, g->psi, nc);
+  if (!rc) rc = upload(x, x->sphe, g->sphe, nc);
+  const double cd0 = 1.0;  // setvset.f90:89
+  if (!rc && cudaMemcpyAsync(small_cd(x), &cd0, sizeof cd0, cudaMemcpyHostToDevice, x->stream) != cudaSuccess)
+    rc = f3d::ctx_error(F3D_ERR_CUDA, "upload failed");
+  // LDU defaults to -99 (Master.f90:176)
+  if (!rc) {
+    std::vector<double> l(pl, -99.0);
+    rc = upload(x, x->ldu, l.data(), pl);
+    if (!rc && cudaStreamSynchronize(x->stream) != cudaSuccess) rc = f3d::ctx_error(F3D_ERR_CUDA, "sync failed");
+  }
+  if (!rc && x->prec == F3D_PREC_FP32) {
+    launch_d2f(x->dz32, x->dz, (long long)nz + 1, x->stream);
+    if (cudaStreamSynchronize(x->stream) != cudaSuccess) rc = f3d::ctx_error(F3D_ERR_CUDA, "sync failed");
+  }
+  if (rc) {
+    f3d_ctx_destroy(x);
+    return rc;
+  }
+  *out = x;
+  return F3D_OK;
+}
+
+int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, const double* t,
+              const double* tp, const double* rho, const double* ust, const double* pblh,
+              const double* rmol, const double* znt, const double* prate, const double* ldu) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  if (!u || !v || !w || !t || !tp || !rho || !ust || !pblh || !rmol || !znt)
+    return f3d::ctx_error(F3D_ERR_ARG, "NULL meteorological field");
+  const Dims d = x->d;
+  const size_t s3 = (size_t)d.cells(), pl = (size_t)d.plane();
+  cudaStream_t s = x->stream;
+  int rc = 0;
+  // reamet.f90:20-153
+  if (!rc) rc = upload(x, x->vx, u, s3);
+  if (!rc) rc = upload(x, x->vy, v, s3);
+  if (!rc) rc = upload(x, x->vz, w, s3);
+  if (!rc) rc = upload(x, x->tempe, t, s3);
+  if (!rc) rc = upload(x, x->vptemp, tp, s3);
+  if (!rc) rc = upload(x, x->rho, rho, s3);
+  if (!rc) rc = upload(x, x->ustar, ust, pl);
+  if (!rc) rc = upload(x, x->zi, pblh, pl);
+  if (!rc) rc = upload(x, x->rl, rmol, pl);
+  if (!rc) rc = upload(x, x->znt, znt, pl);
+  if (!rc && ldu) rc = upload(x, x->ldu, ldu, pl);
+  if (!rc && x->g.wetdep) {
+    if (!prate) return f3d::ctx_error(F3D_ERR_ARG, "PRATE required with wet deposition");
+    rc = upload(x, x->prate, prate, pl);
+  }
+  if (rc) return rc;
+  const f3d_grid& g = x->g;
+  launch_reamet_fix(d, g.wetdep, x->vz, x->prate, s);
+  // meteo.f90:27 kappa3 (unscaled vx, vy)
+  launch_kappa3(d, g.modkv, g.modkh, g.coord_sys, g.rkv0, g.rkh0, g.Csh, g.dX1, g.dX2, g.dx, g.dy,
+                x->dz, x->zlayer, x->Hm1, x->vx, x->vy, x->vptemp, x->ustar, x->zi, x->rl, x->rkver,
+                x->rkhor, s);
+  // meteo.f90:81 setvset (unscaled rho), continuing the cd chain
+  launch_setvset(d, g.nc, g.np, g.modv, x->diam, x->rhop, x->psi, x->sphe, x->tempe, x->rho,
+                 g.aggregate, g.vset_factor, x->vset, x->iters, small_cd(x), x->vset_scratch,
+                 small_status(x), s);
+  // meteo.f90:100 setvdrydep (tempe(:,:,1), unscaled rho(:,:,1))
+  launch_setvdrydep(d, g.nc, x->diam, x->zlayer, x->ldu, x->rl, x->znt, x->ustar, x->tempe, x->rho,
+                    x->vdep, s);
+  // meteo.f90:108-145 scaling, corvver, setdivu
+  launch_meteo_scale(d, g.coord_sys, g.dX1, g.dX2, x->dz, x->Hm1, x->topg, x->vx, x->vy, x->vz,
+                     x->rho, x->rkhor, x->rkh1, x->divu, s);
+  // meteo.f90:149 finddt
+  CK(cudaMemsetAsync(small_dtcn(x), 0, sizeof(unsigned long long), s));
+  launch_finddt(d, g.nc, g.dX1, g.dX2, x->dz, x->vx, x->vy, x->vz, x->vset, x->rkh1, x->rkhor,
+                x->rkver, small_dtcn(x), s);
+  if (x->prec == F3D_PREC_FP32) {
+    launch_d2f(x->vx32, x->vx, (long long)s3, s);
+    launch_d2f(x->vy32, x->vy, (long long)s3, s);
+    launch_d2f(x->vz32, x->vz, (long long)s3, s);
+    launch_d2f(x->rho32, x->rho, (long long)s3, s);
+    launch_d2f(x->rkhor32, x->rkhor, (long long)s3, s);
+    launch_d2f(x->rkh132, x->rkh1, (long long)s3, s);
+    launch_d2f(x->rkver32, x->rkver, (long long)s3, s);
+    launch_d2f(x->vset32, x->vset, (long long)(s3 * g.nc), s);
+    launch_d2f(x->vdep32, x->vdep, (long long)(pl * g.nc), s);
+  }
+  CK(cudaGetLastError());
+  struct {
+    unsigned long long dtcn;
+    int status;
+  } h{};
+  CK(cudaMemcpyAsync(&h.dtcn, small_dtcn(x), sizeof h.dtcn, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&h.status, small_status(x), sizeof h.status, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (h.status) return f3d::ctx_error(F3D_ERR_NOCONV, "No convergence in vsettl routine");
+  double dtcn;
+  memcpy(&dtcn, &h.dtcn, sizeof dtcn);
+  dtcn = fmax2(dtcn, 1e-13);  // finddt.f90:58-66
+  x->dtc = 1.0 / dtcn;
+  x->dt = g.safety_factor * x->dtc;
+  x->have_met = 1;
+  return F3D_OK;
+}
+
+int f3d_source(f3d_ctx* x, int nsou, const int* isrc, const int* jsrc, const int* ksrc,
+               const double* tmrat) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  if (nsou < 0) return f3d::ctx_error(F3D_ERR_ARG, "nsou < 0");
+  const int nc = x->g.nc, nx = x->g.nx, ny = x->g.ny, nz = x->g.nz;
+  // host copies (reasrc.f90:76-80 checks, source.f90:136-185 sums and scaling)
+  std::vector<int> hi(nsou), hj(nsou), hk(nsou);
+  std::vector<double> ht((size_t)nsou * nc);
+  if (nsou > 0) {
+    const cudaMemcpyKind k = is_dev(isrc) ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+    CK(cudaMemcpy(hi.data(), isrc, sizeof(int) * nsou, k));
+    CK(cudaMemcpy(hj.data(), jsrc, sizeof(int) * nsou, k));
+    CK(cudaMemcpy(hk.data(), ksrc, sizeof(int) * nsou, k));
+    CK(cudaMemcpy(ht.data(), tmrat, sizeof(double) * nsou * nc,
+                  is_dev(tmrat) ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+  }
+  for (int s = 0; s < nsou; ++s)
+    if (hi[s] < 1 || hi[s] > nx || hj[s] < 1 || hj[s] > ny || hk[s] > nz) {
+      char m[160];
+      snprintf(m, sizeof m, "Inconsistence between dbs and src files: source %d at (%d,%d,%d)", s + 1,
+               hi[s], hj[s], hk[s]);
+      return f3d::ctx_error(F3D_ERR_RANGE, m);
+    }
+  double fr = 0.0;  // SUM(tmrat(1:nsou,1:nc)) in element order
+  for (int ic = 0; ic < nc; ++ic)
+    for (int s = 0; s < nsou; ++s) fr = fr + ht[(size_t)s + (size_t)nsou * ic];
+  x->flowrate = fr;
+  // tmrat(isou,:) = tmrat(isou,:)*Hm1(isrc,jsrc): Hm1 lives on the device;
+  // the host needs only the 2-D plane values at the source cells.
+  std::vector<double> hm(nsou);
+  for (int s = 0; s < nsou; ++s)
+    CK(cudaMemcpy(&hm[s], x->Hm1 + (size_t)(hi[s] - 1) + (size_t)nx * (hj[s] - 1), sizeof(double),
+                  cudaMemcpyDeviceToHost));
+  for (int s = 0; s < nsou; ++s)
+    for (int ic = 0; ic < nc; ++ic) ht[(size_t)s + (size_t)nsou * ic] *= hm[s];
+  if (nsou > x->src_cap) {
+    int cap = nsou;
+    int rc = dalloc(x, &x->isrc, cap);
+    if (!rc) rc = dalloc(x, &x->jsrc, cap);
+    if (!rc) rc = dalloc(x, &x->ksrc, cap);
+    if (!rc) rc = dalloc(x, &x->tmrat, (size_t)cap * nc);
+    if (rc) return rc;
+    x->src_cap = cap;
+  }
+  x->nsou = nsou;
+  if (nsou > 0) {
+    CK(cudaMemcpyAsync(x->isrc, hi.data(), sizeof(int) * nsou, cudaMemcpyHostToDevice, x->stream));
+    CK(cudaMemcpyAsync(x->jsrc, hj.data(), sizeof(int) * nsou, cudaMemcpyHostToDevice, x->stream));
+    CK(cudaMemcpyAsync(x->ksrc, hk.data(), sizeof(int) * nsou, cudaMemcpyHostToDevice, x->stream));
+    CK(cudaMemcpyAsync(x->tmrat, ht.data(), sizeof(double) * nsou * nc, cudaMemcpyHostToDevice,
+                       x->stream));
+    CK(cudaStreamSynchronize(x->stream));  // host vectors go out of scope
+  }
+  return F3D_OK;
+}
+
+int f3d_step(f3d_ctx* x) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  if (!x->have_met) return f3d::ctx_error(F3D_ERR_STATE, "f3d_step before f3d_meteo");
+  // Fall3d.f90:112-114
+  x->time = x->time + x->dt;
+  x->iiter = x->iiter + 1;
+  x->erumass = x->erumass + x->flowrate * x->dt;
+  const Dims d = x->d;
+  // setsrc.f90:20-35
+  if (x->prof) prof_drain(x);  // bounded event backlog: resolve the previous step
+  if (x->prec == F3D_PREC_FP32) {
+    ProfScope ps(x, "setsrc");
+    launch_setsrc<float>(x->c32, d.halo(), d, x->g.nc, x->nsou, x->isrc, x->jsrc, x->ksrc, x->tmrat,
+                         x->dz, x->zlayer, x->Hm1, x->g.dX1, x->g.dX2, x->dt, x->stream);
+  } else {
+    ProfScope ps(x, "setsrc");
+    launch_setsrc<double>(x->c64, d.halo(), d, x->g.nc, x->nsou, x->isrc, x->jsrc, x->ksrc, x->tmrat,
+                          x->dz, x->zlayer, x->Hm1, x->g.dX1, x->g.dX2, x->dt, x->stream);
+  }
+  if (x->prec == F3D_PREC_FP32)
+    sizloop<float>(x);
+  else
+    sizloop<double>(x);
+  CK(cudaGetLastError());
+  return F3D_OK;
+}
+
+int f3d_sync(f3d_ctx* x) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  CK(cudaStreamSynchronize(x->stream));
+  return F3D_OK;
+}
+
+int f3d_budget(f3d_ctx* x, double* massvol, double* massdep, double* massdry, double* masswet) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  const Dims d = x->d;
+  launch_getc0(x->cdry, x->cwet, x->cload, d, x->g.nc, x->g.np, x->stream);
+  if (x->prec == F3D_PREC_FP32)
+    launch_cmass3d<float>(x->c32, x->cload, x->cdry, x->cwet, d, x->g.nc, x->g.dX1, x->g.dX2, x->dz,
+                          x->red_scratch, small_budget(x), x->stream);
+  else
+    launch_cmass3d<double>(x->c64, x->cload, x->cdry, x->cwet, d, x->g.nc, x->g.dX1, x->g.dX2, x->dz,
+                           x->red_scratch, small_budget(x), x->stream);
+  double h[4];
+  CK(cudaMemcpyAsync(h, small_budget(x), sizeof h, cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  if (massvol) *massvol = h[0];
+  if (massdep) *massdep = h[1];
+  if (massdry) *massdry = h[2];
+  if (masswet) *masswet = h[3];
+  return F3D_OK;
+}
+
+int f3d_get_state(const f3d_ctx* cx, int* iiter, double* time, double* dt, double* dtc,
+                  double* erumass, double* outmass, double* flowrate) {
+  f3d_ctx* x = const_cast<f3d_ctx*>(cx);
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  if (outmass) {
+    CK(cudaMemcpyAsync(outmass, small_outmass(x), sizeof(double), cudaMemcpyDeviceToHost, x->stream));
+    CK(cudaStreamSynchronize(x->stream));
+  }
+  if (iiter) *iiter = x->iiter;
+  if (time) *time = x->time;
+  if (dt) *dt = x->dt;
+  if (dtc) *dtc = x->dtc;
+  if (erumass) *erumass = x->erumass;
+  if (flowrate) *flowrate = x->flowrate;
+  return F3D_OK;
+}
+
+int f3d_get_cd(const f3d_ctx* cx, double* cd) {
+  f3d_ctx* x = const_cast<f3d_ctx*>(cx);
+  if (!x || !cd) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  CK(cudaMemcpyAsync(cd, small_cd(x), sizeof(double), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  return F3D_OK;
+}
+
+int f3d_set_time(f3d_ctx* x, double time, int iiter) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  x->time = time;
+  x->iiter = iiter;
+  return F3D_OK;
+}
+
+int f3d_download(f3d_ctx* x, double* c, double* cdry, double* cwet, double* vset, double* vdep) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  const Dims d = x->d;
+  const size_t hb = (size_t)d.halo() * x->g.nc, pl = (size_t)d.plane(), nc = (size_t)x->g.nc;
+  cudaStream_t s = x->stream;
+  auto kind = [](const void* p) { return is_dev(p) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost; };
+  if (c) {
+    if (x->prec == F3D_PREC_FP32) {
+      if (is_dev(c)) {
+        launch_f2d(c, x->c32, (long long)hb, s);
+      } else {
+        double* tmp = nullptr;
+        CK(cudaMallocAsync((void**)&tmp, hb * sizeof(double), s));
+        launch_f2d(tmp, x->c32, (long long)hb, s);
+        CK(cudaMemcpyAsync(c, tmp, hb * sizeof(double), cudaMemcpyDeviceToHost, s));
+        CK(cudaFreeAsync(tmp, s));
+      }
+    } else {
+      CK(cudaMemcpyAsync(c, x->c64, hb * sizeof(double), kind(c), s));
+    }
+  }
+  if (cdry) CK(cudaMemcpyAsync(cdry, x->cdry, pl * (nc + 1) * sizeof(double), kind(cdry), s));
+  if (cwet) CK(cudaMemcpyAsync(cwet, x->cwet, pl * (nc + 1) * sizeof(double), kind(cwet), s));
+  if (vset) CK(cudaMemcpyAsync(vset, x->vset, (size_t)d.cells() * nc * sizeof(double), kind(vset), s));
+  if (vdep) CK(cudaMemcpyAsync(vdep, x->vdep, pl * nc * sizeof(double), kind(vdep), s));
+  CK(cudaStreamSynchronize(s));
+  return F3D_OK;
+}
+
+int f3d_upload_state(f3d_ctx* x, const double* c, const double* cdry, const double* cwet,
+                     double erumass, double outmass, double cd) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  const Dims d = x->d;
+  const size_t hb = (size_t)d.halo() * x->g.nc, pl = (size_t)d.plane(), nc = (size_t)x->g.nc;
+  cudaStream_t s = x->stream;
+  int rc = 0;
+  if (c) {
+    if (x->prec == F3D_PREC_FP32) {
+      double* tmp = nullptr;
+      CK(cudaMallocAsync((void**)&tmp, hb * sizeof(double), s));
+      rc = upload(x, tmp, c, hb);
+      launch_d2f(x->c32, tmp, (long long)hb, s);
+      CK(cudaFreeAsync(tmp, s));
+    } else {
+      rc = upload(x, x->c64, c, hb);
+    }
+  }
+  if (!rc && cdry) rc = upload(x, x->cdry, cdry, pl * (nc + 1));
+  if (!rc && cwet) rc = upload(x, x->cwet, cwet, pl * (nc + 1));
+  if (rc) return rc;
+  x->erumass = erumass;
+  CK(cudaMemcpyAsync(small_outmass(x), &outmass, sizeof outmass, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(small_cd(x), &cd, sizeof cd, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  return F3D_OK;
+}
+
+int f3d_download_coeffs(f3d_ctx* x, double* vx, double* vy, double* vz, double* rho, double* rkhor,
+                        double* rkh1, double* rkver) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  const size_t b = (size_t)x->d.cells() * sizeof(double);
+  cudaStream_t s = x->stream;
+  auto cp = [&](double* dst, const double* src) -> int {
+    if (!dst) return F3D_OK;
+    CK(cudaMemcpyAsync(dst, src, b, is_dev(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    return F3D_OK;
+  };
+  int rc = cp(vx, x->vx);
+  if (!rc) rc = cp(vy, x->vy);
+  if (!rc) rc = cp(vz, x->vz);
+  if (!rc) rc = cp(rho, x->rho);
+  if (!rc) rc = cp(rkhor, x->rkhor);
+  if (!rc) rc = cp(rkh1, x->rkh1);
+  if (!rc) rc = cp(rkver, x->rkver);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(s));
+  return F3D_OK;
+}
+
+// vsettl iteration counts of the last f3d_meteo (nx*ny*nz*nc int32).
+int f3d_download_iters(f3d_ctx* x, int* iters) {
+  if (!x || !iters) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  CK(cudaMemcpyAsync(iters, x->iters, (size_t)x->d.cells() * x->g.nc * sizeof(int),
+                     is_dev(iters) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  return F3D_OK;
+}
+
+int f3d_outputs(f3d_ctx* x, double* load, double* col_mass, double* c_grnd) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  const Dims d = x->d;
+  const size_t pl = (size_t)d.plane();
+  cudaStream_t s = x->stream;
+  launch_getc0(x->cdry, x->cwet, x->cload, d, x->g.nc, x->g.np, s);
+  double* tmp = nullptr;
+  CK(cudaMallocAsync((void**)&tmp, 3 * pl * sizeof(double), s));
+  if (x->prec == F3D_PREC_FP32)
+    launch_outputs<float>(x->c32, x->cload, d, x->g.np, x->dz, x->Hm1, tmp, tmp + pl, tmp + 2 * pl, s);
+  else
+    launch_outputs<double>(x->c64, x->cload, d, x->g.np, x->dz, x->Hm1, tmp, tmp + pl, tmp + 2 * pl, s);
+  if (load) CK(cudaMemcpyAsync(load, tmp, pl * sizeof(double), cudaMemcpyDefault, s));
+  if (col_mass) CK(cudaMemcpyAsync(col_mass, tmp + pl, pl * sizeof(double), cudaMemcpyDefault, s));
+  if (c_grnd) CK(cudaMemcpyAsync(c_grnd, tmp + 2 * pl, pl * sizeof(double), cudaMemcpyDefault, s));
+  CK(cudaFreeAsync(tmp, s));
+  CK(cudaStreamSynchronize(s));
+  return F3D_OK;
+}
+
+int f3d_ctx_stream(f3d_ctx* x, void** stream) {
+  if (!x || !stream) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  *stream = (void*)x->stream;
+  return F3D_OK;
+}
+
+int f3d_profile_enable(f3d_ctx* x, int enable) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  prof_drain(x);
+  x->prof = enable ? 1 : 0;
+  for (auto& v : x->prof_ms) v = 0.0;
+  for (auto& v : x->prof_count) v = 0;
+  return F3D_OK;
+}
+
+int f3d_profile_read(f3d_ctx* x, int cap, char* names, int name_len, long long* launches,
+                     double* total_ms, int* nkinds) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  prof_drain(x);
+  const int n = (int)x->prof_names.size();
+  if (nkinds) *nkinds = n;
+  for (int i = 0; i < n && i < cap; ++i) {
+    if (names && name_len > 0) {
+      strncpy(names + (size_t)i * name_len, x->prof_names[i].c_str(), (size_t)name_len - 1);
+      names[(size_t)i * name_len + name_len - 1] = 0;
+    }
+    if (launches) launches[i] = x->prof_count[i];
+    if (total_ms) total_ms[i] = x->prof_ms[i];
+  }
+  return F3D_OK;
+}
+
+int f3d_run_reset(f3d_ctx* x) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  x->run_started = 0;
+  return F3D_OK;
+}
+
+// Sources/Fall3d.f90:73-121 with the interval selection of
+// libMaster/get_dbs_value_plane.f90:100-114 and get_source_nsrc.f90:41-59.
+int f3d_run(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, double beg_time,
+            double end_time, int max_steps, f3d_log_record* log, int log_cap, int* nlog) {
+  if (!x || !met || !src) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  if (met->nt < 1) return f3d::ctx_error(F3D_ERR_ARG, "no meteorological snapshot");
+  const size_t s3 = (size_t)x->d.cells(), pl = (size_t)x->d.plane();
+  const int nc = x->g.nc;
+  if (nlog) *nlog = 0;
+  bool go_on = true;  // the reference's do-while runs at least one step
+  if (!x->run_started) {
+    x->time = beg_time;
+    x->meteo_time = beg_time;
+    x->source_time = beg_time;
+    x->iiter = 0;
+    x->meteotime = 1;
+    x->sourcetime = 1;
+    x->run_started = 1;
+  } else {
+    go_on = x->time < end_time;
+  }
+  int steps = 0;
+  while (go_on) {
+    if (x->source_time <= x->time) {
+      if (x->sourcetime) {
+        const int ts = (int)x->time;
+        int found = -1;
+        size_t off = 0, off_found = 0, roff = 0, roff_found = 0;
+        for (int it = 0; it < src->nint; ++it) {
+          if (found < 0 && ts >= src->t1[it] && ts < src->t2[it]) {
+            found = it;
+            off_found = off;
+            roff_found = roff;
+          }
+          off += (size_t)src->nsou[it];
+          roff += (size_t)src->nsou[it] * nc;
+        }
+        if (found < 0) {
+          char m[128];
+          snprintf(m, sizeof m, "get_source_nsrc: no source interval at time %d", ts);
+          return f3d::ctx_error(F3D_ERR_RANGE, m);
+        }
+        const int rc = f3d_source(x, src->nsou[found], src->isrc + off_found, src->jsrc + off_found,
+                                  src->ksrc + off_found, src->tmrat + roff_found);
+        if (rc) return rc;
+        x->source_time = (double)src->t2[found];
+      }
+      if (x->source_time >= end_time) x->sourcetime = 0;
+    }
+    if (x->meteo_time <= x->time) {
+      if (x->meteotime) {
+        const int ts = (int)(met->time_lag + x->time);
+        const int nt = met->nt;
+        if (ts < met->times[0] || ts > met->times[nt - 1]) {
+          char m[128];
+          snprintf(m, sizeof m, "get_dbs_value_plane: time %d outside the DBS interval", ts);
+          return f3d::ctx_error(F3D_ERR_RANGE, m);
+        }
+        int itime = nt - 1, endsec = met->times[nt - 1];
+        for (int it = 0; it < nt - 1; ++it)
+          if (ts >= met->times[it] && ts < met->times[it + 1]) {
+            itime = it;
+            endsec = met->times[it + 1];
+          }
+        const size_t o3 = (size_t)itime * s3, o2 = (size_t)itime * pl;
+        const int rc = f3d_meteo(x, met->u + o3, met->v + o3, met->w + o3, met->t + o3, met->tp + o3,
+                                 met->rho + o3, met->ust + o2, met->pblh + o2, met->rmol + o2,
+                                 met->znt + o2, met->prate ? met->prate + o2 : nullptr, met->ldu);
+        if (rc) return rc;
+        x->meteo_time = (double)endsec - met->time_lag;
+      }
+      if (x->meteo_time >= end_time) x->meteotime = 0;
+    }
+    const int rc = f3d_step(x);
+    if (rc) return rc;
+    ++steps;
+    // endstep.f90:51: mass budget every 10 minutes of simulated time
+    if (x->iiter == 1 || std::fmod(x->time, 600.0) <= x->dt) {
+      if (log && nlog && *nlog < log_cap) {
+        double b[4];
+        int r2 = f3d_budget(x, &b[0], &b[1], &b[2], &b[3]);
+        if (r2) return r2;
+        f3d_log_record& r = log[(*nlog)++];
+        r.iiter = x->iiter;
+        r.time = x->time;
+        r.dt = x->dt;
+        r.dtc = x->dtc;
+        r.massvol = b[0];
+        r.massdep = b[1];
+        r.massdry = b[2];
+        r.masswet = b[3];
+        r2 = f3d_get_state(x, nullptr, nullptr, nullptr, nullptr, nullptr, &r.outmass, nullptr);
+        if (r2) return r2;
+        r.erumass = x->erumass;
+      }
+    }
+    if (x->time >= end_time) go_on = false;
+    if (max_steps > 0 && steps >= max_steps) go_on = false;
+  }
+  CK(cudaStreamSynchronize(x->stream));
+  return F3D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+// f3d_internal.h -- launchers shared by the C-ABI layer and the kernels.
+// All pointers are device pointers; every launcher enqueues on `s` and
+// returns without synchronising.  Class-batched launchers process classes
+// 0..ncls-1 whose blocks are `cstride` (concentration), `vstride` (vset)
+// and `dstride` (vdep) elements apart.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "f3d_common.cuh"
+
+namespace f3d {
+
+// Incremented by every launcher (diagnostic count of kernel launches).
+void count_launch(int n = 1);
+
+template <class T>
+void launch_setbcc(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vx,
+                   const T* vy, const T* vz, const T* vset, long long vstride, const T* vdep,
+                   long long dstride, const T* rkver, const T* dz, int ncls, cudaStream_t s);
+template <class T>
+void launch_advctzc(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vz,
+                    const T* vset, long long vstride, const T* dz, T dt, int ncls,
+                    cudaStream_t s);
+template <class T>
+void launch_advctx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vx, T dx,
+                   T dt, int ncls, cudaStream_t s);
+template <class T>
+void launch_advcty(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vy, T dy,
+                   T dt, int ncls, cudaStream_t s);
+template <class T>
+void launch_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* dz, T dt,
+                  const T* rkver, const T* rho, int ncls, cudaStream_t s);
+template <class T>
+void launch_diffx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dx, T dt,
+                  const T* rkh, const T* rho, int ncls, cudaStream_t s);
+template <class T>
+void launch_diffy(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dy, T dt,
+                  const T* rkh, const T* rho, int ncls, cudaStream_t s);
+// wetdep for classes ic0..ic0+ncls-1 (0-based, all particle classes);
+// cwet points at cwet(1,1,0) and is binary64 in every form.
+template <class T>
+void launch_wetdep(T* c, long long cstride, double* cwet, int ic0, Dims d, int nz_loc, int iz_loc,
+                   double dt, const double* diam, const double* zlayer, const double* dz,
+                   const double* zi, const double* prate, int ncls, cudaStream_t s);
+// accum in binary64 (vset/vdep binary64, c widened).
+template <class T>
+void launch_accum(const T* c, long long cstride, double* cdry, int ic0, Dims d, int iz_loc,
+                  double dt, const double* vset, long long vstride, const double* vdep,
+                  long long dstride, int ncls, cudaStream_t s);
+template <class T>
+void launch_clip(T* c, long long n, cudaStream_t s);
+template <class T>
+void launch_setsrc(T* c, long long cstride, Dims d, int nc, int nsou, const int* isrc,
+                   const int* jsrc, const int* ksrc, const double* tmrat, const double* dz,
+                   const double* zlayer, const double* Hm1, double dX1, double dX2, double dt,
+                   cudaStream_t s);
+
+// Budget reductions.  `scratch` holds at least reduce_scratch_bytes(...)
+// bytes; results are written as binary64 to device memory `out`.
+size_t reduce_scratch_bytes(long long nterms, int nsums);
+// Outflow of one step: *out = *out + sum of the terms of cmass2d.f90:42-102
+// (out is the device copy of outmass).
+template <class T>
+void launch_cmass2d(const T* c, const double* vx, const double* vy, const double* vz,
+                    const double* vset, Dims d, int ic_loc, int nc_loc, int iz_loc, int nz_loc,
+                    double dx, double dy, const double* dz, double dt, void* scratch,
+                    double* out, cudaStream_t s);
+// out[0..3] = massvol, massdep, massdry, masswet of cmass3d.f90:29-58.
+template <class T>
+void launch_cmass3d(const T* c, const double* cload, const double* cdry, const double* cwet,
+                    Dims d, int nc, double dx, double dy, const double* dz, void* scratch,
+                    double* out, cudaStream_t s);
+void launch_getc0(double* cdry, double* cwet, double* cload, Dims d, int nc, int np,
+                  cudaStream_t s);
+// Largest dtcni of finddt.f90:26-57 as a binary64 bit pattern in *dtcn_bits
+// (which must hold +0.0 on entry).
+void launch_finddt(Dims d, int nc, double dX1, double dX2, const double* dz, const double* vx,
+                   const double* vy, const double* vz, const double* vset, const double* rkh1,
+                   const double* rkhor, const double* rkver, unsigned long long* dtcn_bits,
+                   cudaStream_t s);
+template <class T>
+void launch_outputs(const T* c, const double* cload, Dims d, int np, const double* dz,
+                    const double* Hm1, double* load, double* col_mass, double* c_grnd,
+                    cudaStream_t s);
+
+// Coefficient chain (binary64).
+void launch_kappa3(Dims d, int modkv, int modkh, int coord_sys, double rkv0, double rkh0,
+                   double Csh, double dX1, double dX2, double dx, double dy, const double* dz,
+                   const double* zlayer, const double* Hm1, const double* vx, const double* vy,
+                   const double* vptemp, const double* ustar, const double* zi, const double* rl,
+                   double* rkver, double* rkhor, cudaStream_t s);
+void launch_setvdrydep(Dims d, int nc, const double* diam, const double* zlayer,
+                       const double* ldu, const double* rl, const double* znt,
+                       const double* ustar, const double* tempe, const double* rho,
+                       double* vdep, cudaStream_t s);
+void launch_meteo_scale(Dims d, int coord_sys, double dX1, double dX2, const double* dz,
+                        const double* Hm1, const double* topg, double* vx, double* vy,
+                        double* vz, double* rho, const double* rkhor, double* rkh1,
+                        double* divu, cudaStream_t s);
+void launch_reamet_fix(Dims d, int wetdep, double* vz, double* prate, cudaStream_t s);
+
+// setvset with the cd chain.  Work buffers come from setvset_scratch_bytes.
+size_t setvset_scratch_bytes(Dims d, int np);
+// Returns non-zero through *status (device int): 1 = vsettl/get_gama did not
+// converge.  cd_state is a device double (entry value in, exit value out).
+void launch_setvset(Dims d, int nc, int np, int modv, const double* diam, const double* rhop,
+                    const double* psi, const double* sphe, const double* tempe,
+                    const double* rho, int aggregate, double vset_factor, double* vset,
+                    int* iters, double* cd_state, void* scratch, int* status, cudaStream_t s);
+
+// Conversions for the FP32 form.
+void launch_d2f(float* dst, const double* src, long long n, cudaStream_t s);
+void launch_f2d(double* dst, const float* src, long long n, cudaStream_t s);
+
+}  // namespace f3d

@@ -1,0 +1,732 @@
+// f3d_transport.cu -- one kernel per reference transport routine.
+//
+// Each kernel restates one subroutine of Sources/ in the reference's own
+// operation order (compiled with --fmad=false, so the binary64 instances
+// round every operation as the Fortran does) and is batched over classes:
+// classes are independent within a step (Sources/sizloop.f90:31-72), so
+// running a sweep for all classes before the next sweep is the same
+// computation as the reference's class-by-class loop.
+//
+// Thread layout (x fastest everywhere, so every warp touches consecutive
+// addresses of the (nx+2)(ny+2)(nz+2) class block):
+//  * column kernels (advctzc, diffz, wetdep): one thread per (i,j) column,
+//    marching k with a register window;
+//  * x-line kernels (advctx, diffx): one block per x line, the line staged in
+//    shared memory;
+//  * y-line kernels (advcty, diffy): one block per tile of TI adjacent y
+//    lines at one k, the tile staged in shared memory, rows of TI
+//    consecutive x addresses per load.
+// A block owns whole lines, so the in-place update cannot race with a
+// neighbour block's reads.
+#include <algorithm>
+#include <cstdio>
+
+#include "f3d_internal.h"
+
+namespace f3d {
+
+// ------------------------------------------------------------- setbcc
+// Sources/setbcc.f90:19-109.  One thread per ghost cell written; reads
+// only interior cells, so all writes are independent.
+template <class T>
+__global__ void k_setbcc(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vx,
+                         const T* vy, const T* vz, const T* vset, long long vstride,
+                         const T* vdep, long long dstride, const T* rkver, const T* dz) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  T* cc = c + (long long)blockIdx.y * cstride;
+  const T* vs = vset + (long long)blockIdx.y * vstride;
+  const T* vd = vdep + (long long)blockIdx.y * dstride;
+  const bool bot = (iz_loc == 1), top = (iz_loc + nz_loc - 1 == nz);
+  const long long nb = bot ? (long long)nx * ny : (long long)(nx + 2) * (ny + 2);
+  const long long nt = top ? (long long)nx * ny : (long long)(nx + 2) * (ny + 2);
+  const long long nxf = 2LL * ny * nz_loc, nyf = 2LL * nx * nz_loc;
+  const long long total = nb + nt + nxf + nyf + 8;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long u = t;
+    if (u < nb) {  // bottom plane (setbcc.f90:19-33)
+      if (bot) {
+        const int i = (int)(u % nx) + 1, j = (int)(u / nx) + 1;
+        if ((vz[d.M(i, j, 1)] + vs[d.M(i, j, 1)]) >= T(0))
+          cc[d.C(i, j, 0)] = T(0);
+        else
+          cc[d.C(i, j, 0)] = cc[d.C(i, j, 1)] * (T(1) + dz[0] * vd[d.P(i, j)] / rkver[d.M(i, j, 1)]);
+      } else {
+        const int i = (int)(u % (nx + 2)), j = (int)(u / (nx + 2));
+        cc[d.C(i, j, 0)] = T(0);
+      }
+      continue;
+    }
+    u -= nb;
+    if (u < nt) {  // top plane (setbcc.f90:37-49)
+      if (top) {
+        const int i = (int)(u % nx) + 1, j = (int)(u / nx) + 1;
+        if ((vz[d.M(i, j, nz)] + vs[d.M(i, j, nz)]) <= T(0))
+          cc[d.C(i, j, nz + 1)] = T(0);
+        else
+          cc[d.C(i, j, nz + 1)] = cc[d.C(i, j, nz)];
+      } else {
+        const int i = (int)(u % (nx + 2)), j = (int)(u / (nx + 2));
+        cc[d.C(i, j, nz + 1)] = T(0);
+      }
+      continue;
+    }
+    u -= nt;
+    if (u < nxf) {  // x faces (setbcc.f90:53-66)
+      const int side = (int)(u % 2);
+      const long long r = u / 2;
+      const int j = (int)(r % ny) + 1, k = (int)(r / ny) + iz_loc;
+      if (side == 0)
+        cc[d.C(0, j, k)] = (vx[d.M(1, j, k)] >= T(0)) ? T(0) : cc[d.C(1, j, k)];
+      else
+        cc[d.C(nx + 1, j, k)] = (vx[d.M(nx, j, k)] <= T(0)) ? T(0) : cc[d.C(nx, j, k)];
+      continue;
+    }
+    u -= nxf;
+    if (u < nyf) {  // y faces (setbcc.f90:70-83)
+      const int side = (int)(u % 2);
+      const long long r = u / 2;
+      const int i = (int)(r % nx) + 1, k = (int)(r / nx) + iz_loc;
+      if (side == 0)
+        cc[d.C(i, 0, k)] = (vy[d.M(i, 1, k)] >= T(0)) ? T(0) : cc[d.C(i, 1, k)];
+      else
+        cc[d.C(i, ny + 1, k)] = (vy[d.M(i, ny, k)] <= T(0)) ? T(0) : cc[d.C(i, ny, k)];
+      continue;
+    }
+    u -= nyf;
+    // corners (setbcc.f90:87-109)
+    const int q = (int)u;
+    const int ci = (q & 1) ? nx + 1 : 0, cj = (q & 2) ? ny + 1 : 0;
+    const int si = (q & 1) ? nx : 1, sj = (q & 2) ? ny : 1;
+    if (q < 4) {
+      cc[d.C(ci, cj, 0)] = bot ? cc[d.C(si, sj, 1)] : T(0);
+    } else {
+      cc[d.C(ci, cj, nz + 1)] = top ? cc[d.C(si, sj, nz)] : T(0);
+    }
+  }
+}
+
+template <class T>
+void launch_setbcc(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vx,
+                   const T* vy, const T* vz, const T* vset, long long vstride, const T* vdep,
+                   long long dstride, const T* rkver, const T* dz, int ncls, cudaStream_t s) {
+  const long long total = 2LL * (d.nx + 2) * (d.ny + 2) + 2LL * (d.nx + d.ny) * nz_loc + 8;
+  const int bs = 256;
+  const int nb = (int)std::min<long long>((total + bs - 1) / bs, 4096);
+  k_setbcc<T><<<dim3(nb, ncls), bs, 0, s>>>(c, cstride, d, nz_loc, iz_loc, vx, vy, vz, vset,
+                                              vstride, vdep, dstride, rkver, dz);
+  count_launch();
+}
+
+// ------------------------------------------------------------ advctzc
+// Sources/advctzc.f90:28-81.  work(k,1), work(k,2) of the reference are
+// evaluated from the ORIGINAL column, so a register window of originals
+// (c(k-1), c(k), c(k+1), c(k+2)) carries them as k advances.
+template <class T>
+struct ZTab {  // per-level constants of advctzc.f90:34-36 (IEEE, as on the host)
+  T dzz, dzk, dzk_1, dzm1;
+};
+
+template <class T>
+__device__ __forceinline__ void adv_z_work(T cm, T c0, T cp, T vk, T vk_1, const ZTab<T>& z, T dt,
+                                           T& w1, T& w2) {
+  const T vk_12 = T(0.5) * (vk + vk_1);
+  w1 = dt * (vk * c0 - vk_1 * cm) * z.dzz;
+  const T deltar = (cp - c0) * z.dzk;
+  const T deltal = (c0 - cm) * z.dzk_1;
+  const T sigma = T(0.5) * (sign1(deltar) + sign1(deltal)) * fmin2(absd(deltar), absd(deltal));
+  const T Crk = absd(vk_12) * dt * z.dzk_1;
+  w2 = dt * T(0.5) * z.dzm1 * (T(1) - Crk) * sigma * absd(vk_12) * z.dzz;
+}
+
+template <class T>
+__global__ void k_advctzc(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vz,
+                          const T* vset, long long vstride, const T* dz, T dt) {
+  extern __shared__ unsigned char smem_raw[];
+  ZTab<T>* tab = reinterpret_cast<ZTab<T>*>(smem_raw);
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (int k = threadIdx.x + 1; k <= nz; k += blockDim.x) {
+    tab[k].dzz = T(2) / (dz[k] + dz[k - 1]);
+    tab[k].dzk = T(1) / dz[k];
+    tab[k].dzk_1 = T(1) / dz[k - 1];
+    tab[k].dzm1 = dz[k - 1];
+  }
+  __syncthreads();
+  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (col >= (long long)nx * ny) return;
+  const int i = (int)(col % nx) + 1, j = (int)(col / nx) + 1;
+  T* cc = c + (long long)blockIdx.y * cstride;
+  const T* vs = vset + (long long)blockIdx.y * vstride;
+  const long long cb = d.C(i, j, 0), cs = (long long)(nx + 2) * (ny + 2);
+  const long long mb = d.M(i, j, 1), ms = (long long)nx * ny;
+  auto VK = [&](int k) { return vz[mb + (k - 1) * ms] + vs[mb + (k - 1) * ms]; };
+  auto CO = [&](int k) { return cc[cb + k * cs]; };
+  const T dznz = T(1) / dz[nz];
+  const int kb = iz_loc, ke = iz_loc + nz_loc - 1;
+  T c_m1 = CO(kb - 1), c_0 = CO(kb), c_p1 = CO(kb + 1);
+  T vk_0 = VK(kb), vk_m1 = VK(kb > 1 ? kb - 1 : 1);
+  T w1_k, w2_k, w2_km;
+  adv_z_work(c_m1, c_0, c_p1, vk_0, vk_m1, tab[kb], dt, w1_k, w2_k);
+  if (kb == 1) {
+    w2_km = w2_k;
+  } else {
+    T w1_dummy;
+    adv_z_work(CO(kb - 2), c_m1, c_0, vk_m1, VK(kb - 1 > 1 ? kb - 2 : 1), tab[kb - 1], dt, w1_dummy,
+               w2_km);
+  }
+  for (int k = kb; k <= ke; ++k) {
+    T w1_n, w2_n, c_p2 = T(0), vk_p1 = T(0);
+    if (k + 1 <= nz) {
+      c_p2 = CO(k + 2);
+      vk_p1 = VK(k + 1);
+      adv_z_work(c_0, c_p1, c_p2, vk_p1, vk_0, tab[k + 1], dt, w1_n, w2_n);
+    } else {
+      w1_n = dt * vk_0 * (c_p1 - c_0) * dznz;  // work(nz+1,1), advctzc.f90:58-64
+      w2_n = w2_k;                             // kmin = nz
+    }
+    T cn;
+    if (vk_0 > T(0))
+      cn = c_0 - w1_k - (w2_k - w2_km);
+    else
+      cn = c_0 - w1_n - (w2_n - w2_k);
+    cc[cb + k * cs] = cn;
+    w2_km = w2_k;
+    w2_k = w2_n;
+    w1_k = w1_n;
+    c_m1 = c_0;
+    c_0 = c_p1;
+    c_p1 = c_p2;
+    vk_m1 = vk_0;
+    vk_0 = vk_p1;
+  }
+  (void)c_m1;
+  (void)vk_m1;
+}
+
+template <class T>
+void launch_advctzc(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vz,
+                    const T* vset, long long vstride, const T* dz, T dt, int ncls,
+                    cudaStream_t s) {
+  const int bs = 128;
+  const long long cols = (long long)d.nx * d.ny;
+  const size_t sm = sizeof(ZTab<T>) * (d.nz + 1);
+  k_advctzc<T><<<dim3((unsigned)((cols + bs - 1) / bs), ncls), bs, sm, s>>>(
+      c, cstride, d, nz_loc, iz_loc, vz, vset, vstride, dz, dt);
+  count_launch();
+}
+
+// ------------------------------------------------------ advctx / advcty
+// Sources/advctx.f90:24-56 and Sources/advcty.f90:24-55 on one staged line:
+// cl[0..n+1] concentrations, vl(q) velocity at q (1..n).  Phase 1 fills
+// w1[1..n+1], w2[1..n]; phase 2 updates.
+template <class T>
+__device__ __forceinline__ void adv_line_work(const T* cl, int q, int n, T vq, T vq_1, T dx, T dt,
+                                              T auxv, T& w1, T& w2) {
+  const T vq_12 = T(0.5) * (vq + vq_1);
+  w1 = auxv * (vq * cl[q] - vq_1 * cl[q - 1]);
+  const T deltar = (cl[q + 1] - cl[q]) / dx;
+  const T deltal = (cl[q] - cl[q - 1]) / dx;
+  const T sigma = T(0.5) * (sign1(deltar) + sign1(deltal)) * fmin2(absd(deltar), absd(deltal));
+  const T Cri = auxv * absd(vq_12);
+  w2 = dt * T(0.5) * (T(1) - Cri) * sigma * absd(vq_12);
+  (void)n;
+}
+
+template <class T>
+__device__ __forceinline__ T adv_line_update(T cq, T vq, int q, int n, const T* w1, const T* w2) {
+  if (vq > T(0)) return cq - w1[q] - (w2[q] - w2[q > 1 ? q - 1 : 1]);
+  return cq - w1[q + 1] - (w2[q < n ? q + 1 : n] - w2[q]);
+}
+
+// One block per x line (j,k,class); threads stride over i.
+template <class T>
+__global__ void k_advctx(T* c, long long cstride, Dims d, int iz_loc, const T* vx, T dx, T dt) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nx = d.nx, ny = d.ny;
+  T* cl = reinterpret_cast<T*>(smem_raw);
+  T* w1 = cl + (nx + 2);
+  T* w2 = w1 + (nx + 2);
+  const int j = blockIdx.x % ny + 1, k = blockIdx.x / ny + iz_loc;
+  T* cc = c + (long long)blockIdx.y * cstride + d.C(0, j, k);
+  const T* vl = vx + d.M(1, j, k) - 1;  // vl[i] = vx(i,j,k)
+  for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) cl[q] = cc[q];
+  __syncthreads();
+  const T auxv = dt / dx;
+  for (int q = threadIdx.x + 1; q <= nx + 1; q += blockDim.x) {
+    if (q <= nx) {
+      adv_line_work(cl, q, nx, vl[q], vl[q > 1 ? q - 1 : 1], dx, dt, auxv, w1[q], w2[q]);
+    } else {
+      w1[nx + 1] = auxv * vl[nx] * (cl[nx + 1] - cl[nx]);  // advctx.f90:46
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x)
+    cc[q] = adv_line_update(cl[q], vl[q], q, nx, w1, w2);
+}
+
+// One block per tile of TI adjacent y lines (i0..i0+TI-1) at one k.
+template <class T>
+__global__ void k_advcty(T* c, long long cstride, Dims d, int iz_loc, const T* vy, T dy, T dt) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nx = d.nx, ny = d.ny, TI = blockDim.x;
+  T* cl = reinterpret_cast<T*>(smem_raw);  // [q][TI]
+  T* w1 = cl + (ny + 2) * TI;
+  T* w2 = w1 + (ny + 2) * TI;
+  const int ntile = (nx + TI - 1) / TI;
+  const int i0 = (blockIdx.x % ntile) * TI + 1, k = blockIdx.x / ntile + iz_loc;
+  const int tx = threadIdx.x, ty = threadIdx.y, TJ = blockDim.y;
+  const int i = i0 + tx;
+  const bool act = i <= nx;
+  T* cc = c + (long long)blockIdx.y * cstride;
+  const long long rowstride = nx + 2;
+  const long long base = d.C(act ? i : nx, 0, k);
+  for (int q = ty; q <= ny + 1; q += TJ) cl[q * TI + tx] = act ? cc[base + q * rowstride] : T(0);
+  __syncthreads();
+  const T auxv = dt / dy;
+  const long long vb = d.M(act ? i : nx, 1, k) - nx;  // vb + q*nx = vy(i,q,k)
+  if (act) {
+    // w arrays strided by TI: view line tx through a pointer offset.
+    for (int q = ty + 1; q <= ny + 1; q += TJ) {
+      if (q <= ny) {
+        const T vq = vy[vb + (long long)q * nx];
+        const T vq_1 = vy[vb + (long long)(q > 1 ? q - 1 : 1) * nx];
+        const T vq_12 = T(0.5) * (vq + vq_1);
+        const T cq = cl[q * TI + tx], cm = cl[(q - 1) * TI + tx], cp = cl[(q + 1) * TI + tx];
+        w1[q * TI + tx] = auxv * (vq * cq - vq_1 * cm);
+        const T deltar = (cp - cq) / dy;
+        const T deltal = (cq - cm) / dy;
+        const T sigma =
+            T(0.5) * (sign1(deltar) + sign1(deltal)) * fmin2(absd(deltar), absd(deltal));
+        const T Crj = auxv * absd(vq_12);
+        w2[q * TI + tx] = dt * T(0.5) * (T(1) - Crj) * sigma * absd(vq_12);
+      } else {
+        const T vn = vy[vb + (long long)ny * nx];
+        w1[(ny + 1) * TI + tx] = auxv * vn * (cl[(ny + 1) * TI + tx] - cl[ny * TI + tx]);  // advcty.f90:45
+      }
+    }
+  }
+  __syncthreads();
+  if (act) {
+    for (int q = ty + 1; q <= ny; q += TJ) {
+      const T vq = vy[vb + (long long)q * nx];
+      const T cq = cl[q * TI + tx];
+      T cn;
+      if (vq > T(0))
+        cn = cq - w1[q * TI + tx] - (w2[q * TI + tx] - w2[(q > 1 ? q - 1 : 1) * TI + tx]);
+      else
+        cn = cq - w1[(q + 1) * TI + tx] - (w2[(q < ny ? q + 1 : ny) * TI + tx] - w2[q * TI + tx]);
+      cc[base + q * rowstride] = cn;
+    }
+  }
+}
+
+static int pick_ti(int nline, size_t elem, int arrays) {
+  // Widest tile whose staging fits in 96 KB.
+  for (int ti = 32; ti >= 4; ti >>= 1)
+    if ((size_t)arrays * (nline + 2) * ti * elem <= 96 * 1024) return ti;
+  return 4;
+}
+
+static void set_smem(const void* fn, size_t bytes) {
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <class T>
+void launch_advctx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vx, T dx,
+                   T dt, int ncls, cudaStream_t s) {
+  const size_t sm = 3 * (size_t)(d.nx + 2) * sizeof(T);
+  set_smem((const void*)k_advctx<T>, sm);
+  const int bs = d.nx >= 256 ? 256 : 128;
+  k_advctx<T><<<dim3(d.ny * nz_loc, ncls), bs, sm, s>>>(c, cstride, d, iz_loc, vx, dx, dt);
+  count_launch();
+}
+
+template <class T>
+void launch_advcty(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vy, T dy,
+                   T dt, int ncls, cudaStream_t s) {
+  const int TI = pick_ti(d.ny, sizeof(T), 3);
+  const int TJ = 256 / TI;
+  const size_t sm = 3 * (size_t)(d.ny + 2) * TI * sizeof(T);
+  set_smem((const void*)k_advcty<T>, sm);
+  const int ntile = (d.nx + TI - 1) / TI;
+  k_advcty<T><<<dim3(ntile * nz_loc, ncls), dim3(TI, TJ), sm, s>>>(c, cstride, d, iz_loc, vy, dy, dt);
+  count_launch();
+}
+
+// -------------------------------------------------------------- diffz
+// Sources/diffz.f90:22-62, one thread per column.  The four kinds of face
+// flux (bottom/top non-averaged, interior averaged) are evaluated exactly as
+// written; an interior face shared by cells k and k+1 is the same
+// expression in both, so it is computed once and carried.
+template <class T>
+__global__ void k_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* dz, T dt,
+                        const T* rkver, const T* rho) {
+  extern __shared__ unsigned char smem_raw[];
+  T* l_dz = reinterpret_cast<T*>(smem_raw);  // 0..nz
+  T* l_dzdz = l_dz + (d.nz + 1);             // 1..nz
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (int k = threadIdx.x; k <= nz; k += blockDim.x) {
+    l_dz[k] = T(1) / dz[k];
+    if (k >= 1) l_dzdz[k] = T(2) / (dz[k] + dz[k - 1]);
+  }
+  __syncthreads();
+  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (col >= (long long)nx * ny) return;
+  const int i = (int)(col % nx) + 1, j = (int)(col / nx) + 1;
+  T* cc = c + (long long)blockIdx.y * cstride;
+  const long long cb = d.C(i, j, 0), cs = (long long)(nx + 2) * (ny + 2);
+  const long long mb = d.M(i, j, 1), ms = (long long)nx * ny;
+  auto C = [&](int k) { return cc[cb + k * cs]; };
+  auto R = [&](int k) { return rho[mb + (k - 1) * ms]; };
+  auto K = [&](int k) { return rkver[mb + (k - 1) * ms]; };
+  const int kb = iz_loc, ke = iz_loc + nz_loc - 1;
+  // Interior face flux between k and k+1 (diffz.f90:42-45):
+  //   0.5*(rho(k+1)K(k+1) + rho(k)K(k)) * (c(k+1)/rho(k+1) - c(k)/rho(k)) * l_dz(k)
+  auto face = [&](int k, T qk, T qk1, T rk, T rk1, T Kk, T Kk1) {
+    const T rks = T(0.5) * (rk1 * Kk1 + rk * Kk);
+    return rks * (qk1 - qk) * l_dz[k];
+  };
+  // Window of originals: c(k-1), c(k), c(k+1); rho, K at k-1, k, k+1.
+  T cm = C(kb - 1), c0 = C(kb), cp = C(kb + 1);
+  T rm = (kb > 1) ? R(kb - 1) : T(0), r0 = R(kb), rp = (kb < nz) ? R(kb + 1) : T(0);
+  T Km = (kb > 1) ? K(kb - 1) : T(0), K0 = K(kb), Kp = (kb < nz) ? K(kb + 1) : T(0);
+  T qm = (kb > 1) ? cm / rm : T(0), q0 = c0 / r0, qp = (kb < nz) ? cp / rp : T(0);
+  // gradb of the first interior cell needs the face (kb-1, kb).
+  T fprev = (kb >= 3) ? face(kb - 1, qm, q0, rm, r0, Km, K0) : T(0);
+  for (int k = kb; k <= ke; ++k) {
+    T work;
+    if (k == 1) {  // bottom (diffz.f90:32-39); kb == 1 here
+      const T rkst = K(2) * R(2);
+      const T rksb = K(1) * R(1);
+      const T gradt = rkst * ((cp / rp) - (c0 / r0)) * l_dz[1];
+      T gradb = rksb * ((c0 / r0) - (cm / r0)) * l_dz[0];
+      gradb = fmax2(T(0), gradb);
+      work = dt * (gradt - gradb) * l_dzdz[1];
+      fprev = face(1, q0, qp, r0, rp, K0, Kp);  // interior face (1,2) for k = 2
+    } else if (k == nz) {  // top (diffz.f90:51-58)
+      const T rkst = K0 * r0;
+      const T rksb = Km * rm;
+      T gradt = rkst * ((cp / r0) - (c0 / r0)) * l_dz[nz];
+      const T gradb = rksb * ((c0 / r0) - (cm / rm)) * l_dz[nz - 1];
+      gradt = fmin2(T(0), gradt);
+      work = dt * (gradt - gradb) * l_dz[nz];
+    } else {  // interior (diffz.f90:41-47)
+      if (k == 2 && kb == 2) fprev = face(1, qm, q0, rm, r0, Km, K0);
+      const T gradt = face(k, q0, qp, r0, rp, K0, Kp);
+      const T gradb = fprev;
+      work = dt * (gradt - gradb) * l_dzdz[k];
+      fprev = gradt;
+    }
+    cc[cb + k * cs] = c0 + work;
+    // advance the window (originals)
+    if (k < ke) {
+      cm = c0; c0 = cp; cp = C(k + 2);
+      rm = r0; r0 = rp; rp = (k + 2 <= nz) ? R(k + 2) : T(0);
+      Km = K0; K0 = Kp; Kp = (k + 2 <= nz) ? K(k + 2) : T(0);
+      qm = q0; q0 = qp; qp = (k + 2 <= nz) ? cp / rp : T(0);
+    }
+  }
+}
+
+template <class T>
+void launch_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* dz, T dt,
+                  const T* rkver, const T* rho, int ncls, cudaStream_t s) {
+  const int bs = 128;
+  const long long cols = (long long)d.nx * d.ny;
+  const size_t sm = 2 * sizeof(T) * (d.nz + 1);
+  k_diffz<T><<<dim3((unsigned)((cols + bs - 1) / bs), ncls), bs, sm, s>>>(c, cstride, d, nz_loc,
+                                                                         iz_loc, dz, dt, rkver, rho);
+  count_launch();
+}
+
+// ------------------------------------------------------- diffx / diffy
+// Sources/diffx.f90:20-55, Sources/diffy.f90:20-55.  lr(q) = 1/rho(q) and
+// pk(q) = rkh(q)*rho(q) are staged with the line.
+template <class T>
+__device__ __forceinline__ T diff_line_cell(int q, int n, const T* cl, const T* lr, const T* pk,
+                                            int st, T dtdx2) {
+  // st: stride between consecutive line positions in the staged arrays
+  auto Cq = [&](int a) { return cl[a * st]; };
+  auto Lq = [&](int a) { return lr[a * st]; };
+  auto Pq = [&](int a) { return pk[a * st]; };
+  T gradr, gradl;
+  if (q == 1) {
+    gradr = Pq(2) * (Cq(2) * Lq(2) - Cq(1) * Lq(1));
+    gradl = Pq(1) * (Cq(1) * Lq(1) - Cq(0) * Lq(1));
+    gradl = fmax2(T(0), gradl);
+  } else if (q == n) {
+    gradr = Pq(n) * (Cq(n + 1) * Lq(n) - Cq(n) * Lq(n));
+    gradl = Pq(n - 1) * (Cq(n) * Lq(n) - Cq(n - 1) * Lq(n - 1));
+    gradr = fmin2(T(0), gradr);
+  } else {
+    const T rksr = T(0.5) * (Pq(q + 1) + Pq(q));
+    const T rksl = T(0.5) * (Pq(q) + Pq(q - 1));
+    gradr = rksr * (Cq(q + 1) * Lq(q + 1) - Cq(q) * Lq(q));
+    gradl = rksl * (Cq(q) * Lq(q) - Cq(q - 1) * Lq(q - 1));
+  }
+  return Cq(q) + dtdx2 * (gradr - gradl);
+}
+
+template <class T>
+__global__ void k_diffx(T* c, long long cstride, Dims d, int iz_loc, T dx, T dt, const T* rkh,
+                        const T* rho) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nx = d.nx, ny = d.ny;
+  T* cl = reinterpret_cast<T*>(smem_raw);
+  T* lr = cl + (nx + 2);
+  T* pk = lr + (nx + 2);
+  const int j = blockIdx.x % ny + 1, k = blockIdx.x / ny + iz_loc;
+  T* cc = c + (long long)blockIdx.y * cstride + d.C(0, j, k);
+  const long long mb = d.M(1, j, k) - 1;
+  for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) {
+    cl[q] = cc[q];
+    if (q >= 1 && q <= nx) {
+      const T r = rho[mb + q];
+      lr[q] = T(1) / r;
+      pk[q] = rkh[mb + q] * r;
+    }
+  }
+  __syncthreads();
+  const T dtdx2 = dt / (dx * dx);
+  for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x)
+    cc[q] = diff_line_cell(q, nx, cl, lr, pk, 1, dtdx2);
+}
+
+template <class T>
+__global__ void k_diffy(T* c, long long cstride, Dims d, int iz_loc, T dy, T dt, const T* rkh,
+                        const T* rho) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nx = d.nx, ny = d.ny, TI = blockDim.x;
+  T* cl = reinterpret_cast<T*>(smem_raw);
+  T* lr = cl + (ny + 2) * TI;
+  T* pk = lr + (ny + 2) * TI;
+  const int ntile = (nx + TI - 1) / TI;
+  const int i0 = (blockIdx.x % ntile) * TI + 1, k = blockIdx.x / ntile + iz_loc;
+  const int tx = threadIdx.x, ty = threadIdx.y, TJ = blockDim.y;
+  const int i = i0 + tx;
+  const bool act = i <= nx;
+  T* cc = c + (long long)blockIdx.y * cstride;
+  const long long rowstride = nx + 2;
+  const long long base = d.C(act ? i : nx, 0, k);
+  const long long vb = d.M(act ? i : nx, 1, k) - nx;
+  for (int q = ty; q <= ny + 1; q += TJ) {
+    cl[q * TI + tx] = act ? cc[base + q * rowstride] : T(0);
+    if (q >= 1 && q <= ny) {
+      const T r = act ? rho[vb + (long long)q * nx] : T(1);
+      lr[q * TI + tx] = T(1) / r;
+      pk[q * TI + tx] = act ? rkh[vb + (long long)q * nx] * r : T(0);
+    }
+  }
+  __syncthreads();
+  if (!act) return;
+  const T dtdy2 = dt / (dy * dy);
+  for (int q = ty + 1; q <= ny; q += TJ)
+    cc[base + q * rowstride] = diff_line_cell(q, ny, cl + tx, lr + tx, pk + tx, TI, dtdy2);
+}
+
+template <class T>
+void launch_diffx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dx, T dt,
+                  const T* rkh, const T* rho, int ncls, cudaStream_t s) {
+  const size_t sm = 3 * (size_t)(d.nx + 2) * sizeof(T);
+  set_smem((const void*)k_diffx<T>, sm);
+  const int bs = d.nx >= 256 ? 256 : 128;
+  k_diffx<T><<<dim3(d.ny * nz_loc, ncls), bs, sm, s>>>(c, cstride, d, iz_loc, dx, dt, rkh, rho);
+  count_launch();
+}
+
+template <class T>
+void launch_diffy(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dy, T dt,
+                  const T* rkh, const T* rho, int ncls, cudaStream_t s) {
+  const int TI = pick_ti(d.ny, sizeof(T), 3);
+  const int TJ = 256 / TI;
+  const size_t sm = 3 * (size_t)(d.ny + 2) * TI * sizeof(T);
+  set_smem((const void*)k_diffy<T>, sm);
+  const int ntile = (d.nx + TI - 1) / TI;
+  k_diffy<T><<<dim3(ntile * nz_loc, ncls), dim3(TI, TJ), sm, s>>>(c, cstride, d, iz_loc, dy, dt,
+                                                                   rkh, rho);
+  count_launch();
+}
+
+// ------------------------------------------------------------- wetdep
+// Sources/wetdep.f90:28-50.  lambda and the deposit are binary64 in every
+// form (the wet deposit is a ground-deposit accumulation).
+template <class T>
+__global__ void k_wetdep(T* c, long long cstride, double* cwet, int ic0, Dims d, int nz_loc,
+                         int iz_loc, double dt, const double* diam, const double* zlayer,
+                         const double* dz, const double* zi, const double* prate) {
+  const int ic = ic0 + blockIdx.y;  // 0-based class
+  double diam_max = 100.0;
+  diam_max = diam_max * 1e-6;
+  if (diam[ic] > diam_max) return;
+  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (col >= (long long)d.nx * d.ny) return;
+  const int i = (int)(col % d.nx) + 1, j = (int)(col / d.nx) + 1;
+  const double a = 8.4e-5, b = 0.79;
+  const long long p = d.P(i, j);
+  const double lambda = fmin2(dt * a * pow(prate[p], b), 1.0);
+  T* cc = c + (long long)blockIdx.y * cstride;
+  double* cw = cwet + (long long)(ic + 1) * d.plane();
+  const double z = zi[p];
+  double acc = cw[p];
+  for (int k = iz_loc; k <= iz_loc + nz_loc - 1; ++k) {
+    if (zlayer[k - 1] <= z) {
+      const long long q = d.C(i, j, k);
+      const double ck = (double)cc[q];
+      acc = acc + dz[k] * lambda * ck;
+      cc[q] = (T)(ck * (1.0 - lambda));
+    }
+  }
+  cw[p] = acc;
+}
+
+template <class T>
+void launch_wetdep(T* c, long long cstride, double* cwet, int ic0, Dims d, int nz_loc, int iz_loc,
+                   double dt, const double* diam, const double* zlayer, const double* dz,
+                   const double* zi, const double* prate, int ncls, cudaStream_t s) {
+  if (ncls <= 0) return;
+  const int bs = 128;
+  const long long cols = (long long)d.nx * d.ny;
+  k_wetdep<T><<<dim3((unsigned)((cols + bs - 1) / bs), ncls), bs, 0, s>>>(
+      c, cstride, cwet, ic0, d, nz_loc, iz_loc, dt, diam, zlayer, dz, zi, prate);
+  count_launch();
+}
+
+// -------------------------------------------------------------- accum
+// Sources/accum.f90:17-25 (binary64).
+template <class T>
+__global__ void k_accum(const T* c, long long cstride, double* cdry, int ic0, Dims d, double dt,
+                        const double* vset, long long vstride, const double* vdep,
+                        long long dstride) {
+  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (col >= (long long)d.nx * d.ny) return;
+  const int i = (int)(col % d.nx) + 1, j = (int)(col / d.nx) + 1;
+  const int ic = ic0 + blockIdx.y;
+  const T* cc = c + (long long)blockIdx.y * cstride;
+  const double* vs = vset + (long long)blockIdx.y * vstride;
+  const double* vd = vdep + (long long)blockIdx.y * dstride;
+  double* cd = cdry + (long long)(ic + 1) * d.plane();
+  const long long p = d.P(i, j);
+  cd[p] = cd[p] - dt * (double)cc[d.C(i, j, 1)] * fmin2(0.0, vs[d.M(i, j, 1)] + vd[p]);
+}
+
+template <class T>
+void launch_accum(const T* c, long long cstride, double* cdry, int ic0, Dims d, int iz_loc,
+                  double dt, const double* vset, long long vstride, const double* vdep,
+                  long long dstride, int ncls, cudaStream_t s) {
+  if (iz_loc != 1 || ncls <= 0) return;
+  const int bs = 128;
+  const long long cols = (long long)d.nx * d.ny;
+  k_accum<T><<<dim3((unsigned)((cols + bs - 1) / bs), ncls), bs, 0, s>>>(
+      c, cstride, cdry, ic0, d, dt, vset, vstride, vdep, dstride);
+  count_launch();
+}
+
+// --------------------------------------------------------------- clip
+// Sources/sizloop.f90:77-78: c = MAX(0,c) over the whole halo array.
+template <class T>
+__global__ void k_clip(T* c, long long n) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    c[q] = fmax2(T(0), c[q]);
+}
+
+template <class T>
+void launch_clip(T* c, long long n, cudaStream_t s) {
+  const int bs = 256;
+  const int nb = (int)std::min<long long>((n + bs - 1) / bs, 152LL * 16);
+  k_clip<T><<<nb, bs, 0, s>>>(c, n);
+  count_launch();
+}
+
+// ------------------------------------------------------------- setsrc
+// Sources/setsrc.f90:20-35.  One thread per class walks the sources in
+// file order, so several sources in one cell add in the reference's order.
+template <class T>
+__global__ void k_setsrc(T* c, long long cstride, Dims d, int nc, int nsou, const int* isrc,
+                         const int* jsrc, const int* ksrc, const double* tmrat, const double* dz,
+                         const double* zlayer, const double* Hm1, double dX1, double dX2,
+                         double dt) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= nc) return;
+  T* cc = c + (long long)ic * cstride;
+  for (int is = 0; is < nsou; ++is) {
+    const int i = isrc[is], j = jsrc[is], k = ksrc[is];
+    if (k < 1 || k > d.nz) continue;
+    double dzeta;
+    if (k == 1)
+      dzeta = 0.5 * dz[k] + zlayer[k - 1];
+    else
+      dzeta = 0.5 * (dz[k - 1] + dz[k]);
+    const double vol0 = Hm1[d.P(i, j)] * dX1 * dX2 * dzeta;
+    const long long q = d.C(i, j, k);
+    cc[q] = (T)((double)cc[q] + dt * tmrat[is + (long long)nsou * ic] / vol0);
+  }
+}
+
+template <class T>
+void launch_setsrc(T* c, long long cstride, Dims d, int nc, int nsou, const int* isrc,
+                   const int* jsrc, const int* ksrc, const double* tmrat, const double* dz,
+                   const double* zlayer, const double* Hm1, double dX1, double dX2, double dt,
+                   cudaStream_t s) {
+  if (nsou <= 0) return;
+  k_setsrc<T><<<(nc + 63) / 64, 64, 0, s>>>(c, cstride, d, nc, nsou, isrc, jsrc, ksrc, tmrat, dz,
+                                             zlayer, Hm1, dX1, dX2, dt);
+  count_launch();
+}
+
+// ------------------------------------------------------- conversions
+__global__ void k_d2f(float* dst, const double* src, long long n) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    dst[q] = (float)src[q];
+}
+__global__ void k_f2d(double* dst, const float* src, long long n) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    dst[q] = (double)src[q];
+}
+void launch_d2f(float* dst, const double* src, long long n, cudaStream_t s) {
+  if (n <= 0) return;
+  const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  k_d2f<<<nb, 256, 0, s>>>(dst, src, n);
+  count_launch();
+}
+void launch_f2d(double* dst, const float* src, long long n, cudaStream_t s) {
+  if (n <= 0) return;
+  const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  k_f2d<<<nb, 256, 0, s>>>(dst, src, n);
+  count_launch();
+}
+
+// ---------------------------------------------------- instantiations
+#define F3D_INST(T)                                                                              \
+  template void launch_setbcc<T>(T*, long long, Dims, int, int, const T*, const T*, const T*,    \
+                                 const T*, long long, const T*, long long, const T*, const T*,   \
+                                 int, cudaStream_t);                                             \
+  template void launch_advctzc<T>(T*, long long, Dims, int, int, const T*, const T*, long long,  \
+                                  const T*, T, int, cudaStream_t);                               \
+  template void launch_advctx<T>(T*, long long, Dims, int, int, const T*, T, T, int,             \
+                                 cudaStream_t);                                                  \
+  template void launch_advcty<T>(T*, long long, Dims, int, int, const T*, T, T, int,             \
+                                 cudaStream_t);                                                  \
+  template void launch_diffz<T>(T*, long long, Dims, int, int, const T*, T, const T*, const T*,  \
+                                int, cudaStream_t);                                              \
+  template void launch_diffx<T>(T*, long long, Dims, int, int, T, T, const T*, const T*, int,    \
+                                cudaStream_t);                                                   \
+  template void launch_diffy<T>(T*, long long, Dims, int, int, T, T, const T*, const T*, int,    \
+                                cudaStream_t);                                                   \
+  template void launch_wetdep<T>(T*, long long, double*, int, Dims, int, int, double,            \
+                                 const double*, const double*, const double*, const double*,     \
+                                 const double*, int, cudaStream_t);                              \
+  template void launch_accum<T>(const T*, long long, double*, int, Dims, int, double,            \
+                                const double*, long long, const double*, long long, int,         \
+                                cudaStream_t);                                                   \
+  template void launch_clip<T>(T*, long long, cudaStream_t);                                     \
+  template void launch_setsrc<T>(T*, long long, Dims, int, int, const int*, const int*,          \
+                                 const int*, const double*, const double*, const double*,        \
+                                 const double*, double, double, double, cudaStream_t);
+
+F3D_INST(double)
+F3D_INST(float)
+
+}  // namespace f3d

@@ -1,0 +1,388 @@
+/*
+ * fall3d_gpu.h -- C ABI of the GB300 transport library for FALL3D 7.0.
+ *
+ * The library replaces the per-time-step transport of particle-class
+ * concentrations of FALL3D 7.0 (lmingari/Fall3D) and the coefficient
+ * chain that feeds it.  Two layers are exported:
+ *
+ *  1. Fine-grained entry points, one per reference subroutine, with the
+ *     reference argument lists passed by reference (what a Fortran
+ *     `interface ... bind(C)` without VALUE produces).  Array arguments
+ *     may all be host memory (copied to the GPU and back around the
+ *     kernel: the "compat" mode used when the Fortran driver owns the
+ *     Master arrays) or all device memory (used in place).  Mixing the
+ *     two in one call is rejected with F3D_ERR_ARG.
+ *
+ *  2. A coarse context API that keeps the whole state resident in HBM:
+ *     create a context for one scenario, feed it meteorology and sources,
+ *     step it, and read budgets and fields back only when needed.
+ *
+ * Layout is the reference's (Sources/Master.f90:92-136): Fortran column
+ * major, x fastest.  c is (0:nx+1, 0:ny+1, 0:nz+1, nc), met fields are
+ * (nx, ny, nz), vset is (nx, ny, nz, nc), vdep is (nx, ny, nc),
+ * cdry/cwet/cload are (nx, ny, 0:nc), dz is (0:nz).  Integers are 32-bit
+ * (Sources/KindType.f90:10), reals are IEEE binary64 (KindType.f90:11).
+ *
+ * Every entry point returns an int status: 0 is success.  The message of
+ * the last failure on the calling thread is available from
+ * f3d_last_error().  Nothing throws across this boundary and nothing traps
+ * on the device: non-finite values and device wait time-outs come back as
+ * status codes or counters.
+ */
+#ifndef FALL3D_GPU_H
+#define FALL3D_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Status codes                                                        */
+/* ------------------------------------------------------------------ */
+#define F3D_OK            0
+#define F3D_ERR_ARG       1  /* invalid argument, size or pointer kind        */
+#define F3D_ERR_CUDA      2  /* CUDA runtime error                             */
+#define F3D_ERR_NOCONV    3  /* vsettl / get_gama did not converge             */
+#define F3D_ERR_STATE     4  /* call out of order (e.g. step before meteo)     */
+#define F3D_ERR_OOM       5  /* device allocation failed                       */
+#define F3D_ERR_RANGE     6  /* source index outside the grid, time not in DBS */
+#define F3D_ERR_INTERNAL  7  /* device-side consistency check failed           */
+
+/* Model selectors, as decoded by Sources/readat.f90:227-314. */
+#define F3D_MODV_ARASTOOPOUR 1
+#define F3D_MODV_GANSER      2
+#define F3D_MODV_WILSON      3
+#define F3D_MODV_DELLINO     4
+#define F3D_MODKV_CONSTANT   0
+#define F3D_MODKV_SIMILARITY 1
+#define F3D_MODKV_SURFACE    2
+#define F3D_MODKH_CONSTANT   0
+#define F3D_MODKH_RAMS       1
+#define F3D_MODKH_CMAQ       2
+#define F3D_COORD_LONLAT     0
+#define F3D_COORD_UTM        1
+
+/* Precision forms of the coarse API. */
+#define F3D_PREC_FP64 64  /* plain form: every operation in binary64, in the
+                             reference's operation order                    */
+#define F3D_PREC_FP32 32  /* precision form: stencil arithmetic in binary32;
+                             budgets, accum, finddt and the coefficient chain
+                             stay binary64                                  */
+
+/* Returns the message of the last failing call on this thread (always
+ * NUL-terminated, truncated to len-1 bytes).  Returns the full length. */
+int f3d_last_error(char* buf, int len);
+
+/* Library version string and the device it runs on (cudaGetDevice). */
+const char* f3d_version(void);
+
+/* ------------------------------------------------------------------ */
+/* 1. Fine-grained entry points (reference argument lists)             */
+/* ------------------------------------------------------------------ */
+
+/* Sources/setbcc.f90:1 setbcc(c,nx,ny,nz,nz_loc,iz_loc,vx,vy,vz,vset,vdep,rkver,dz) */
+int f3d_setbcc(double* c, const int* nx, const int* ny, const int* nz,
+               const int* nz_loc, const int* iz_loc,
+               const double* vx, const double* vy, const double* vz,
+               const double* vset, const double* vdep, const double* rkver,
+               const double* dz);
+
+/* Sources/advctzc.f90:1 advctzc(c,nx,ny,nz,nz_loc,iz_loc,vz,vset,dz,dt,lmeth) */
+int f3d_advctzc(double* c, const int* nx, const int* ny, const int* nz,
+                const int* nz_loc, const int* iz_loc,
+                const double* vz, const double* vset, const double* dz,
+                const double* dt, const int* lmeth);
+
+/* Sources/advctx.f90:1 advctx(c,nx,ny,nz,nz_loc,iz_loc,vx,dx,dt,work,lmeth).
+ * work is accepted for signature compatibility and never touched. */
+int f3d_advctx(double* c, const int* nx, const int* ny, const int* nz,
+               const int* nz_loc, const int* iz_loc, const double* vx,
+               const double* dx, const double* dt, double* work,
+               const int* lmeth);
+
+/* Sources/advcty.f90:1 advcty(c,nx,ny,nz,nz_loc,iz_loc,vy,dy,dt,work,lmeth) */
+int f3d_advcty(double* c, const int* nx, const int* ny, const int* nz,
+               const int* nz_loc, const int* iz_loc, const double* vy,
+               const double* dy, const double* dt, double* work,
+               const int* lmeth);
+
+/* Sources/diffz.f90:1 diffz(c,nx,ny,nz,nz_loc,iz_loc,dz,dt,rkver,rho,work) */
+int f3d_diffz(double* c, const int* nx, const int* ny, const int* nz,
+              const int* nz_loc, const int* iz_loc, const double* dz,
+              const double* dt, const double* rkver, const double* rho,
+              double* work);
+
+/* Sources/diffx.f90:1 diffx(c,nx,ny,nz,nz_loc,iz_loc,dx,dt,rkhor,rho,work) */
+int f3d_diffx(double* c, const int* nx, const int* ny, const int* nz,
+              const int* nz_loc, const int* iz_loc, const double* dx,
+              const double* dt, const double* rkhor, const double* rho,
+              double* work);
+
+/* Sources/diffy.f90:1 diffy(c,nx,ny,nz,nz_loc,iz_loc,dy,dt,rkhor,rho,work) */
+int f3d_diffy(double* c, const int* nx, const int* ny, const int* nz,
+              const int* nz_loc, const int* iz_loc, const double* dy,
+              const double* dt, const double* rkhor, const double* rho,
+              double* work);
+
+/* Sources/wetdep.f90:1 wetdep(c,cwet,ic,nx,ny,nz,nz_loc,iz_loc,dt,diam,zlayer,dz,zi,prate).
+ * cwet points at cwet(1,1,0); ic is 1-based; diam holds all classes. */
+int f3d_wetdep(double* c, double* cwet, const int* ic, const int* nx,
+               const int* ny, const int* nz, const int* nz_loc,
+               const int* iz_loc, const double* dt, const double* diam,
+               const double* zlayer, const double* dz, const double* zi,
+               const double* prate);
+
+/* Sources/accum.f90:1 accum(c,cdry,ic,nx,ny,nz,nz_loc,iz_loc,vz,dt,vset,vdep).
+ * cdry points at cdry(1,1,0); vz is unused by the reference and here. */
+int f3d_accum(double* c, double* cdry, const int* ic, const int* nx,
+              const int* ny, const int* nz, const int* nz_loc,
+              const int* iz_loc, const double* vz, const double* dt,
+              const double* vset, const double* vdep);
+
+/* The clip of Sources/sizloop.f90:77-78: c = MAX(0,c) over the whole
+ * halo array of classes ic_loc..ic_loc+nc_loc-1 (c holds all nc). */
+int f3d_clip(double* c, const int* nx, const int* ny, const int* nz,
+             const int* nc, const int* ic_loc, const int* nc_loc);
+
+/* Sources/cmass2d.f90:1 cmass2d(c,vx,vy,vz,vset,nx,ny,nz,nc,ic_loc,nc_loc,
+ * iz_loc,nz_loc,dx,dy,dz,dt,outmass): outmass += outflow of this step.
+ * The device sum is exact-then-rounded (see the parity note in the
+ * library docs); the reference sums sequentially. */
+int f3d_cmass2d(const double* c, const double* vx, const double* vy,
+                const double* vz, const double* vset, const int* nx,
+                const int* ny, const int* nz, const int* nc,
+                const int* ic_loc, const int* nc_loc, const int* iz_loc,
+                const int* nz_loc, const double* dx, const double* dy,
+                const double* dz, const double* dt, double* outmass);
+
+/* Sources/cmass3d.f90:1 cmass3d(c,cload,cdry,cwet,nx,ny,nz,nc,dx,dy,dz,
+ * massvol,massdep,massdry,masswet) */
+int f3d_cmass3d(const double* c, const double* cload, const double* cdry,
+                const double* cwet, const int* nx, const int* ny,
+                const int* nz, const int* nc, const double* dx,
+                const double* dy, const double* dz, double* massvol,
+                double* massdep, double* massdry, double* masswet);
+
+/* Sources/endstep.f90:80 getc0 followed by cload = cdry + cwet
+ * (endstep.f90:35,60).  np = number of particle classes. */
+int f3d_getc0(double* cdry, double* cwet, double* cload, const int* nx,
+              const int* ny, const int* nc, const int* np);
+
+/* Sources/setsrc.f90:1 setsrc (module state made explicit): c(i,j,k,:) +=
+ * dt*tmrat(is,:)/vol0.  tmrat(nsou,nc) is already scaled by Hm1
+ * (Sources/source.f90:75-77).  Sources with ksrc outside 1..nz are skipped
+ * as in the reference; isrc/jsrc outside 1..nx/1..ny are F3D_ERR_RANGE. */
+int f3d_setsrc(double* c, const int* nx, const int* ny, const int* nz,
+               const int* nc, const int* nsou, const int* isrc,
+               const int* jsrc, const int* ksrc, const double* tmrat,
+               const double* dz, const double* zlayer, const double* Hm1,
+               const double* dX1, const double* dX2, const double* dt);
+
+/* Sources/finddt.f90:1 finddt (module state made explicit).  rkh1, vx and
+ * rho are the scaled fields (Sources/meteo.f90:108-112). */
+int f3d_finddt(const int* nx, const int* ny, const int* nz, const int* nc,
+               const double* dX1, const double* dX2, const double* dz,
+               const double* vx, const double* vy, const double* vz,
+               const double* vset, const double* rkh1, const double* rkhor,
+               const double* rkver, const double* safety_factor,
+               double* dt, double* dtc);
+
+/* Sources/kappa3.f90:1 kappa3 (module state made explicit).  vx, vy are
+ * unscaled; rkver/rkhor are in/out (cells kappa3 does not assign keep
+ * their input value, e.g. rkver(:,:,1) under SIMILARITY). */
+int f3d_kappa3(const int* nx, const int* ny, const int* nz,
+               const int* modkv, const int* modkh, const int* coord_sys,
+               const double* rkv0, const double* rkh0, const double* Csh,
+               const double* dX1, const double* dX2, const double* dx,
+               const double* dy, const double* dz, const double* zlayer,
+               const double* Hm1, const double* vx, const double* vy,
+               const double* vptemp, const double* ustar, const double* zi,
+               const double* rl, double* rkver, double* rkhor);
+
+/* Sources/setvset.f90:1 setvset with vsettl's SAVEd drag coefficient made
+ * explicit: *cd is read as the chain's entry value and written back with
+ * its exit value (it starts at 1.0 at program start, setvset.f90:89).
+ * tempe and rho are unscaled.  aggregate = (classname(np)=='aggregate'). */
+int f3d_setvset(const int* nx, const int* ny, const int* nz, const int* nc,
+                const int* np, const int* modv, const double* diam,
+                const double* rhop, const double* psi, const double* sphe,
+                const double* tempe, const double* rho, const int* aggregate,
+                const double* vset_factor, double* vset, double* cd);
+
+/* Sources/setvdrydep.f90:1 setvdrydep (module state made explicit). */
+int f3d_setvdrydep(const int* nx, const int* ny, const int* nc,
+                   const double* diam, const double* zlayer,
+                   const double* ldu, const double* rl, const double* znt,
+                   const double* ustar, const double* tempe,
+                   const double* rho, double* vdep);
+
+/* Sources/meteo.f90:108-123 + Sources/corvver.f90:21-34 +
+ * Sources/setdivu.f90:16-30: scale vx, rho, build rkh1, correct vz for
+ * terrain (LON-LAT only) and compute divu.  All arrays in/out. */
+int f3d_meteo_scale(const int* nx, const int* ny, const int* nz,
+                    const int* coord_sys, const double* dX1,
+                    const double* dX2, const double* dz, const double* Hm1,
+                    const double* topg, double* vx, double* vy, double* vz,
+                    double* rho, const double* rkhor, double* rkh1,
+                    double* divu);
+
+/* ------------------------------------------------------------------ */
+/* 2. Coarse context API (state resident on the GPU)                   */
+/* ------------------------------------------------------------------ */
+
+/* Static description of one scenario: the grid of Sources/reagrd.f90, the
+ * classes of Sources/reagrn.f90 and the model switches of readat.f90.
+ * Pointers are host memory and are copied at creation. */
+typedef struct f3d_grid {
+  int nx, ny, nz;        /* interior cells (each >= 3)                    */
+  int nc, np;            /* classes; particle classes are 1..np           */
+  int coord_sys;         /* F3D_COORD_*                                   */
+  int modkv, modkh, modv;/* F3D_MODKV_*, F3D_MODKH_*, F3D_MODV_*           */
+  int wetdep;            /* WET_DEPOSITION = YES                          */
+  int aggregate;         /* classname(np) == 'aggregate'                  */
+  int precision;         /* F3D_PREC_FP64 or F3D_PREC_FP32                 */
+  double dX1, dX2;       /* scaled cell sizes in m (reagrd.f90:157-158)    */
+  double dx, dy;         /* native spacing (deg or m), used by CMAQ        */
+  double rkh0, rkv0;     /* constant diffusivities (m2/s)                  */
+  double Csh;            /* RAMS constant (Sources/Numeric.f90:26)         */
+  double safety_factor;  /* CFL safety (Sources/inidat.f90:21)             */
+  double vset_factor;    /* aggregate settling factor (readat.f90:386)     */
+  const double* dz;      /* dz(0:nz)                                       */
+  const double* zlayer;  /* zlayer(nz)                                     */
+  const double* Hm1;     /* Hm1(nx,ny)                                     */
+  const double* topg;    /* topg(nx,ny)                                    */
+  const double* diam;    /* diam(nc) in m                                  */
+  const double* rhop;    /* rhop(nc)                                       */
+  const double* psi;     /* psi(nc) from setpsi                            */
+  const double* sphe;    /* sphe(nc)                                       */
+} f3d_grid;
+
+/* Time-dependent meteorology of one scenario: nt snapshots of the DBS
+ * variables, each valid on [times(it), times(it+1)) as selected by
+ * libMaster/get_dbs_value_plane.f90:107-114 (piecewise constant, no
+ * interpolation in time).  Fields are already on the model levels.
+ * Arrays are snapshot-slowest; host or device memory. */
+typedef struct f3d_met_series {
+  int nt;
+  const int* times;      /* nt snapshot times, seconds after DBS origin   */
+  double time_lag;       /* DBS origin to run origin (reagrd.f90:277-308) */
+  const double *u, *v, *w, *t, *tp, *rho;          /* nt*nx*ny*nz          */
+  const double *ust, *pblh, *rmol, *znt, *prate;   /* nt*nx*ny (PRATE mm/s) */
+  const double* ldu;     /* nx*ny land use, time independent              */
+} f3d_met_series;
+
+/* Source intervals as in the .src file (libMaster/get_source_*.f90): the
+ * interval [t1(i), t2(i)) holds nsou(i) sources; index arrays and rates are
+ * concatenated over intervals, rates (nsou_i, nc) column major, unscaled. */
+typedef struct f3d_src_series {
+  int nint;
+  const int *t1, *t2, *nsou;
+  const int *isrc, *jsrc, *ksrc;
+  const double* tmrat;
+} f3d_src_series;
+
+/* One line of the mass-budget log (Sources/writim.f90:18-52). */
+typedef struct f3d_log_record {
+  int iiter;
+  double time, dt, dtc;
+  double massvol, massdep, massdry, masswet, outmass, erumass;
+} f3d_log_record;
+
+typedef struct f3d_ctx f3d_ctx;
+
+int f3d_ctx_create(const f3d_grid* grid, f3d_ctx** out);
+int f3d_ctx_destroy(f3d_ctx* ctx);
+/* Device bytes held by a context of this grid (admission control). */
+int f3d_ctx_footprint(const f3d_grid* grid, long long* bytes);
+
+/* Sources/meteo.f90:19-149 on the device for one DBS snapshot: reamet's
+ * vz(:,:,1)=0 and PRATE*3600, kappa3, setvset (continuing the cd chain),
+ * setvdrydep, scaling, corvver, setdivu and finddt.  Fields are the raw
+ * DBS variables of the snapshot (host or device pointers). */
+int f3d_meteo(f3d_ctx* ctx, const double* u, const double* v,
+              const double* w, const double* t, const double* tp,
+              const double* rho, const double* ust, const double* pblh,
+              const double* rmol, const double* znt, const double* prate,
+              const double* ldu);
+
+/* Sources/source.f90:24-77: install the sources of one interval (rates
+ * unscaled, as read), compute flowrate and scale rates by Hm1. */
+int f3d_source(f3d_ctx* ctx, int nsou, const int* isrc, const int* jsrc,
+               const int* ksrc, const double* tmrat);
+
+/* Sources/Fall3d.f90:112-117: time += dt, iiter += 1,
+ * erumass += flowrate*dt, setsrc, sizloop (setbcc, advection, diffusion,
+ * wetdep, accum for every class, clip, cmass2d). */
+int f3d_step(f3d_ctx* ctx);
+
+/* Sources/endstep.f90:59-60 + writim.f90:18: getc0, cload = cdry + cwet and
+ * cmass3d on the device. */
+int f3d_budget(f3d_ctx* ctx, double* massvol, double* massdep,
+               double* massdry, double* masswet);
+
+/* Scalar state of the time loop. */
+int f3d_get_state(const f3d_ctx* ctx, int* iiter, double* time, double* dt,
+                  double* dtc, double* erumass, double* outmass,
+                  double* flowrate);
+int f3d_set_time(f3d_ctx* ctx, double time, int iiter);
+
+/* Copy state to host (any pointer may be NULL): c (binary64 even in the
+ * FP32 form), cdry, cwet (nx,ny,0:nc), vset (nx,ny,nz,nc), vdep. */
+int f3d_download(f3d_ctx* ctx, double* c, double* cdry, double* cwet,
+                 double* vset, double* vdep);
+/* Overwrite the concentration state (restart): c (binary64), cdry, cwet
+ * (NULL leaves a field unchanged), plus erumass, outmass and the cd state. */
+int f3d_upload_state(f3d_ctx* ctx, const double* c, const double* cdry,
+                     const double* cwet, double erumass, double outmass,
+                     double cd);
+/* Coefficient fields after the last f3d_meteo, for inspection: the scaled
+ * vx, vy, vz, rho, rkhor, rkh1, rkver (each nx*ny*nz; NULL skips). */
+int f3d_download_coeffs(f3d_ctx* ctx, double* vx, double* vy, double* vz,
+                        double* rho, double* rkhor, double* rkh1,
+                        double* rkver);
+/* vsettl iteration counts of the last f3d_meteo, nx*ny*nz*nc int32
+ * (0 for the closed-form Dellino model; the reference does not keep them). */
+int f3d_download_iters(f3d_ctx* ctx, int* iters);
+/* vsettl drag-coefficient chain state (setvset.f90:89). */
+int f3d_get_cd(const f3d_ctx* ctx, double* cd);
+
+/* Output quantities of Sources/printres_nc.f90 on the device:
+ * LOAD = cload(:,:,0)/Hm1 (:104-122), COL_MASS (:218-246),
+ * C_GRND (:391-410).  Each (nx,ny); NULL skips. */
+int f3d_outputs(f3d_ctx* ctx, double* load, double* col_mass,
+                double* c_grnd);
+
+/* Sources/Fall3d.f90:73-121: the time loop from beg_time to end_time
+ * (at most max_steps steps if max_steps > 0), reading meteorology and
+ * sources when their intervals end, logging the mass budget at the steps
+ * endstep.f90:51 selects.  Up to log_cap records are written to log. */
+int f3d_run(f3d_ctx* ctx, const f3d_met_series* met,
+            const f3d_src_series* src, double beg_time, double end_time,
+            int max_steps, f3d_log_record* log, int log_cap, int* nlog);
+
+/* Time loop state of f3d_run kept in the context so that f3d_run can be
+ * called repeatedly to continue (each call resumes where the last ended). */
+int f3d_run_reset(f3d_ctx* ctx);
+
+/* The CUDA stream all work of this context is enqueued on (cudaStream_t),
+ * for callers that time or order their own work against it. */
+int f3d_ctx_stream(f3d_ctx* ctx, void** stream);
+
+/* Per-kernel timing with CUDA events recorded on the context's stream
+ * around every launch of f3d_step while enabled.  f3d_profile_read returns,
+ * for up to cap kernel kinds, the name, launch count and total milliseconds
+ * since the last reset (it synchronises the stream). */
+int f3d_profile_enable(f3d_ctx* ctx, int enable);
+int f3d_profile_read(f3d_ctx* ctx, int cap, char* names, int name_len,
+                     long long* launches, double* total_ms, int* nkinds);
+
+/* Number of CUDA kernels this library launched since load (diagnostic). */
+long long f3d_kernel_launches(void);
+
+/* Synchronise the context's stream. */
+int f3d_sync(f3d_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FALL3D_GPU_H */
