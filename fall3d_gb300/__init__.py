@@ -27,6 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfall3d_gb300.so")
 
 PREC_FP64, PREC_FP32 = 64, 32
+OPT_FUSED, OPT_TILE = 1, 2
 
 
 class F3DError(RuntimeError):
@@ -100,6 +101,8 @@ def load(build_if_missing: bool = False):
         "f3d_sync": [VP],
         "f3d_last_error": [C.c_char_p, I],
         "f3d_ctx_stream": [VP, C.POINTER(VP)],
+        "f3d_set_option": [VP, I, I],
+        "f3d_get_option": [VP, I, IP],
         "f3d_profile_enable": [VP, I],
         "f3d_profile_read": [VP, I, C.c_char_p, I, C.POINTER(C.c_longlong), DP, IP],
     }
@@ -427,6 +430,14 @@ class Context:
 
     def run_reset(self):
         _check(self.lib.f3d_run_reset(self.h))
+
+    def set_option(self, key: int, value: int):
+        _check(self.lib.f3d_set_option(self.h, int(key), int(value)))
+
+    def get_option(self, key: int) -> int:
+        v = C.c_int()
+        _check(self.lib.f3d_get_option(self.h, int(key), C.byref(v)))
+        return v.value
 
     # -- timing ------------------------------------------------------------
     def stream_handle(self) -> int:

@@ -17,6 +17,7 @@
 
 #include "../../include/fall3d_gpu.h"
 #include "f3d_internal.h"
+#include "f3d_fused.h"
 
 namespace f3d {
 int ctx_error(int code, const char* msg);
@@ -47,6 +48,13 @@ struct f3d_ctx {
   float *vx32 = nullptr, *vy32 = nullptr, *vz32 = nullptr, *rho32 = nullptr, *rkhor32 = nullptr,
         *rkh132 = nullptr, *rkver32 = nullptr, *vset32 = nullptr, *vdep32 = nullptr,
         *dz32 = nullptr;
+  // fused FP32 step: second concentration buffer, 1/rho, K*rho products,
+  // per-column wet rate, per-class wet-deposition switch
+  float* c32b = nullptr;
+  float *lrho32 = nullptr, *pkx32 = nullptr, *pky32 = nullptr, *pkz32 = nullptr;
+  double* lambda2d = nullptr;
+  unsigned char* wet_class = nullptr;
+  int opt_fused = 1, opt_tile = 0;
   // sources
   int *isrc = nullptr, *jsrc = nullptr, *ksrc = nullptr;
   double* tmrat = nullptr;
@@ -134,8 +142,8 @@ long long footprint_bytes(const f3d_grid* g) {
   b += 4LL * s3 * nc;                          // vsettl iteration counts
   b += 8LL * 3 * pl * (nc + 1);                // cdry cwet cload
   if (g->precision == F3D_PREC_FP32) {
-    b += 4LL * halo * nc;
-    b += 4LL * (7 * s3 + s3 * nc + pl * nc + nz + 1);
+    b += 2 * 4LL * halo * nc;
+    b += 4LL * (11 * s3 + s3 * nc + pl * nc + nz + 1) + 8LL * pl + nc;
   } else {
     b += 8LL * halo * nc;
   }
@@ -303,6 +311,62 @@ void sizloop(f3d_ctx* x) {
 }
 
 
+// The precision form's step as one fused kernel (f3d_fused.cu), then the
+// clipped state's boundary outflow (cmass2d) in binary64.
+void sizloop_fused(f3d_ctx* x) {
+  const Dims d = x->d;
+  const int nc = x->g.nc;
+  const long long hb = d.halo(), s3 = d.cells(), pl = d.plane();
+  cudaStream_t s = x->stream;
+  FusedArgs a{};
+  a.c_in = x->c32;
+  a.c_out = x->c32b;
+  a.cstride = hb;
+  a.d = d;
+  a.ncls = nc;
+  a.xfirst = (x->iiter % 2 == 0) ? 1 : 0;
+  a.dt = (float)x->dt;
+  a.dt64 = x->dt;
+  a.vx = x->vx32;
+  a.vy = x->vy32;
+  a.vz = x->vz32;
+  a.vset = x->vset32;
+  a.vstride = s3;
+  a.vdep = x->vdep32;
+  a.dstride = pl;
+  a.rkver1 = x->rkver32;
+  a.lrho = x->lrho32;
+  a.pkx = x->pkx32;
+  a.pky = x->pky32;
+  a.pkz = x->pkz32;
+  a.dz = x->dz32;
+  a.auxvx = (float)(x->dt / x->g.dX1);
+  a.auxvy = (float)(x->dt / x->g.dX2);
+  a.inv_dx = (float)(1.0 / x->g.dX1);
+  a.inv_dy = (float)(1.0 / x->g.dX2);
+  a.dtdx2 = (float)(x->dt / (x->g.dX1 * x->g.dX1));
+  a.dtdy2 = (float)(x->dt / (x->g.dX2 * x->g.dX2));
+  a.wet_class = x->g.wetdep ? x->wet_class : nullptr;
+  a.lambda2d = x->lambda2d;
+  a.zi = x->zi;
+  a.zlayer = x->zlayer;
+  a.dz64 = x->dz;
+  a.cwet = x->cwet;
+  a.cdry = x->cdry;
+  a.vset64 = x->vset;
+  a.vdep64 = x->vdep;
+  {
+    ProfScope ps(x, "step_fused");
+    launch_step_fused(a, x->opt_tile, s);
+  }
+  std::swap(x->c32, x->c32b);
+  {
+    ProfScope ps(x, "cmass2d");
+    launch_cmass2d<float>(x->c32, x->vx, x->vy, x->vz, x->vset, d, 1, nc, 1, d.nz, x->g.dX1,
+                          x->g.dX2, x->dz, x->dt, x->red_scratch, small_outmass(x), s);
+  }
+}
+
 }  // namespace
 
 namespace f3d {
@@ -401,6 +465,13 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
     A(vset32, s3 * nc);
     A(vdep32, pl * nc);
     A(dz32, nz + 1);
+    A(c32b, hb * nc);
+    A(lrho32, s3);
+    A(pkx32, s3);
+    A(pky32, s3);
+    A(pkz32, s3);
+    A(lambda2d, pl);
+    A(wet_class, nc);
   } else {
     A(c64, hb * nc);
   }
@@ -439,6 +510,14 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
     if (!rc && cudaStreamSynchronize(x->stream) != cudaSuccess) rc = f3d::ctx_error(F3D_ERR_CUDA, "sync failed");
   }
   if (!rc && x->prec == F3D_PREC_FP32) {
+    // wetdep.f90:28-30 and sizloop.f90:65: particles of at most 100 um
+    std::vector<unsigned char> wc(nc, 0);
+    double diam_max = 100.0;
+    diam_max = diam_max * 1e-6;
+    for (size_t ic = 0; ic < nc; ++ic)
+      wc[ic] = (g->wetdep && (int)ic < g->np && !(g->diam[ic] > diam_max)) ? 1 : 0;
+    if (cudaMemcpyAsync(x->wet_class, wc.data(), nc, cudaMemcpyHostToDevice, x->stream) != cudaSuccess)
+      rc = f3d::ctx_error(F3D_ERR_CUDA, "upload failed");
     launch_d2f(x->dz32, x->dz, (long long)nz + 1, x->stream);
     if (cudaStreamSynchronize(x->stream) != cudaSuccess) rc = f3d::ctx_error(F3D_ERR_CUDA, "sync failed");
   }
@@ -507,6 +586,8 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
     launch_d2f(x->rkver32, x->rkver, (long long)s3, s);
     launch_d2f(x->vset32, x->vset, (long long)(s3 * g.nc), s);
     launch_d2f(x->vdep32, x->vdep, (long long)(pl * g.nc), s);
+    launch_fp32_coeffs((long long)s3, x->rho, x->rkh1, x->rkhor, x->rkver, x->lrho32, x->pkx32,
+                       x->pky32, x->pkz32, s);
   }
   CK(cudaGetLastError());
   struct {
@@ -522,6 +603,10 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
   dtcn = fmax2(dtcn, 1e-13);  // finddt.f90:58-66
   x->dtc = 1.0 / dtcn;
   x->dt = g.safety_factor * x->dtc;
+  if (x->prec == F3D_PREC_FP32 && g.wetdep) {
+    launch_wet_lambda((long long)pl, x->dt, x->prate, x->lambda2d, s);
+    CK(cudaGetLastError());
+  }
   x->have_met = 1;
   return F3D_OK;
 }
@@ -601,7 +686,9 @@ int f3d_step(f3d_ctx* x) {
     launch_setsrc<double>(x->c64, d.halo(), d, x->g.nc, x->nsou, x->isrc, x->jsrc, x->ksrc, x->tmrat,
                           x->dz, x->zlayer, x->Hm1, x->g.dX1, x->g.dX2, x->dt, x->stream);
   }
-  if (x->prec == F3D_PREC_FP32)
+  if (x->prec == F3D_PREC_FP32 && x->opt_fused)
+    sizloop_fused(x);
+  else if (x->prec == F3D_PREC_FP32)
     sizloop<float>(x);
   else
     sizloop<double>(x);
@@ -772,6 +859,30 @@ int f3d_outputs(f3d_ctx* x, double* load, double* col_mass, double* c_grnd) {
   if (c_grnd) CK(cudaMemcpyAsync(c_grnd, tmp + 2 * pl, pl * sizeof(double), cudaMemcpyDefault, s));
   CK(cudaFreeAsync(tmp, s));
   CK(cudaStreamSynchronize(s));
+  return F3D_OK;
+}
+
+int f3d_set_option(f3d_ctx* x, int key, int value) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  if (key == F3D_OPT_FUSED) {
+    x->opt_fused = value ? 1 : 0;
+  } else if (key == F3D_OPT_TILE) {
+    if (value < 0 || value > 2) return f3d::ctx_error(F3D_ERR_ARG, "tile shape must be 0..2");
+    x->opt_tile = value;
+  } else {
+    return f3d::ctx_error(F3D_ERR_ARG, "unknown option");
+  }
+  return F3D_OK;
+}
+
+int f3d_get_option(const f3d_ctx* x, int key, int* value) {
+  if (!x || !value) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  if (key == F3D_OPT_FUSED)
+    *value = x->opt_fused;
+  else if (key == F3D_OPT_TILE)
+    *value = x->opt_tile;
+  else
+    return f3d::ctx_error(F3D_ERR_ARG, "unknown option");
   return F3D_OK;
 }
 

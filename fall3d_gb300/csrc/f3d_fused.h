@@ -1,0 +1,47 @@
+// f3d_fused.h -- arguments of the precision form's fused step kernel.
+#pragma once
+
+#include "f3d_internal.h"
+
+namespace f3d {
+
+struct FusedArgs {
+  const float* c_in;  // class blocks of (nx+2)(ny+2)(nz+2), after setsrc
+  float* c_out;       // same layout; receives the step's result incl. ghosts
+  long long cstride;
+  Dims d;
+  int ncls;
+  int xfirst;  // iiter even: x before y (sizloop.f90:42-48)
+  float dt;
+  double dt64;
+  // binary32 coefficients (scaled fields of meteo.f90:108-112)
+  const float *vx, *vy, *vz;
+  const float* vset;  // class blocks of nx*ny*nz
+  long long vstride;
+  const float* vdep;  // class blocks of nx*ny
+  long long dstride;
+  const float* rkver1;  // rkver(:,:,1) (setbcc bottom)
+  const float* lrho;    // 1/rho
+  const float *pkx, *pky, *pkz;  // rkh1*rho, rkhor*rho, rkver*rho
+  const float* dz;      // dz(0:nz)
+  float auxvx, auxvy, inv_dx, inv_dy, dtdx2, dtdy2;
+  // binary64 deposits
+  const unsigned char* wet_class;  // per class: wet deposition applies (or NULL)
+  const double* lambda2d;          // min(dt*a*prate^b,1) per column
+  const double* zi;
+  const double* zlayer;
+  const double* dz64;
+  double* cwet;  // (nx,ny,0:nc)
+  double* cdry;
+  const double* vset64;  // class blocks, vstride apart
+  const double* vdep64;  // class blocks of nx*ny
+};
+
+// shape 0: 32x32 region / 256 threads; 1: 64x32 / 512; 2: 32x32 / 512.
+void launch_step_fused(const FusedArgs& a, int shape, cudaStream_t s);
+void launch_wet_lambda(long long n, double dt, const double* prate, double* lam, cudaStream_t s);
+void launch_fp32_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,
+                        const double* rkver, float* lrho, float* pkx, float* pky, float* pkz,
+                        cudaStream_t s);
+
+}  // namespace f3d

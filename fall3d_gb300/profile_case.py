@@ -1,0 +1,41 @@
+"""Runs a few steps of a named workload through the context API: the case
+that profiler captures of the step kernels run.
+
+    python -m fall3d_gb300.profile_case [--workload cfg1] [--steps 3]
+                                        [--precision 32] [--fused 1] [--tile 0]
+"""
+from __future__ import annotations
+
+import argparse
+
+import fall3d_gb300 as F
+from fall3d_gb300 import synth
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="cfg1")
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--precision", type=int, default=32)
+    ap.add_argument("--fused", type=int, default=1)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--classes", type=int, default=0, help="override the class count")
+    args = ap.parse_args()
+    over = {"max_snapshots": 2}
+    if args.classes:
+        over["nc"] = args.classes
+    s = synth.make_scenario(args.workload, seed=0, **over)
+    g = F.Context(s, args.precision)
+    if args.precision == 32:
+        g.set_option(F.OPT_FUSED, args.fused)
+        g.set_option(F.OPT_TILE, args.tile)
+    g.source(0)
+    g.meteo(0)
+    g.step(args.steps)
+    g.sync()
+    st = g.state()
+    print(f"{args.workload}: {st['iiter']} steps, dt {st['dt']:.3f} s, outmass {st['outmass']:.6e}")
+
+
+if __name__ == "__main__":
+    main()

@@ -364,6 +364,14 @@ int f3d_run(f3d_ctx* ctx, const f3d_met_series* met,
  * called repeatedly to continue (each call resumes where the last ended). */
 int f3d_run_reset(f3d_ctx* ctx);
 
+/* Options of a context (f3d_set_option / f3d_get_option). */
+#define F3D_OPT_FUSED 1  /* FP32 form: 1 = one fused kernel per step (default),
+                            0 = one kernel per reference routine          */
+#define F3D_OPT_TILE  2  /* fused kernel tile: 0 = 32x32 region/256 threads
+                            (default), 1 = 64x32/512, 2 = 32x32/512        */
+int f3d_set_option(f3d_ctx* ctx, int key, int value);
+int f3d_get_option(const f3d_ctx* ctx, int key, int* value);
+
 /* The CUDA stream all work of this context is enqueued on (cudaStream_t),
  * for callers that time or order their own work against it. */
 int f3d_ctx_stream(f3d_ctx* ctx, void** stream);
