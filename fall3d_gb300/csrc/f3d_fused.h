@@ -37,7 +37,8 @@ struct FusedArgs {
   const double* vdep64;  // class blocks of nx*ny
 };
 
-// shape 0: 32x32 region / 256 threads; 1: 64x32 / 512; 2: 32x32 / 512.
+// tile region (x by y) / threads: 0 = 32x32 / 256 (default), 1 = 32x64 / 512,
+// 2 = 32x32 / 512.
 void launch_step_fused(const FusedArgs& a, int shape, cudaStream_t s);
 void launch_wet_lambda(long long n, double dt, const double* prate, double* lam, cudaStream_t s);
 void launch_fp32_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,

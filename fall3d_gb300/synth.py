@@ -150,12 +150,15 @@ def make_classes(nc, phimin, phimax, rho_coarse=2500.0, rho_fine=1000.0,
 
 
 def setpsi(modv, sphe, diam):
-    """Sources/setpsi.f90:27-58 for the models the generator uses."""
+    """Shape factor psi of Sources/setpsi.f90:27-58: 1 (ARASTOOPOUR) or the
+    sphericity (GANSER).  For WILSON and DELLINO the reference derives psi from
+    get_gama's axis ratio; the synthetic scenarios use a fixed psi = 0.75
+    there (psi is an input of the transport path either way)."""
     if modv == MODV_ARASTOOPOUR:
         return np.ones_like(sphe)
     if modv == MODV_GANSER:
         return sphe.copy()
-    raise ValueError("setpsi: WILSON/DELLINO psi need get_gama; pass psi explicitly")
+    return np.full_like(sphe, 0.75)
 
 
 def suzuki_column(ns, H, A, lam, M0, fc):
