@@ -52,9 +52,12 @@ struct f3d_ctx {
   // per-column wet rate, per-class wet-deposition switch
   float* c32b = nullptr;
   float *lrho32 = nullptr, *pkx32 = nullptr, *pky32 = nullptr, *pkz32 = nullptr;
+  float* vk32 = nullptr;  // vz + vset per class
   double* lambda2d = nullptr;
   unsigned char* wet_class = nullptr;
   int opt_fused = 1, opt_tile = 0;
+  // the fused kernel applies: zlayer non-decreasing, 32-bit offsets in a class
+  int fused_ok = 1;
   // sources
   int *isrc = nullptr, *jsrc = nullptr, *ksrc = nullptr;
   double* tmrat = nullptr;
@@ -330,7 +333,7 @@ void sizloop_fused(f3d_ctx* x) {
   a.vx = x->vx32;
   a.vy = x->vy32;
   a.vz = x->vz32;
-  a.vset = x->vset32;
+  a.vk = x->vk32;
   a.vstride = s3;
   a.vdep = x->vdep32;
   a.dstride = pl;
@@ -412,6 +415,9 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
   x->g.diam = x->g.rhop = x->g.psi = x->g.sphe = nullptr;
   x->d = Dims{g->nx, g->ny, g->nz};
   x->prec = g->precision;
+  for (int k = 1; k < g->nz; ++k)
+    if (!(g->zlayer[k] >= g->zlayer[k - 1])) x->fused_ok = 0;
+  if (x->d.halo() >= (1LL << 31) || x->d.cells() >= (1LL << 31)) x->fused_ok = 0;
   if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete x;
     return f3d::ctx_error(F3D_ERR_CUDA, "cudaStreamCreate failed");
@@ -470,6 +476,7 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
     A(pkx32, s3);
     A(pky32, s3);
     A(pkz32, s3);
+    A(vk32, s3 * nc);
     A(lambda2d, pl);
     A(wet_class, nc);
   } else {
@@ -588,6 +595,7 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
     launch_d2f(x->vdep32, x->vdep, (long long)(pl * g.nc), s);
     launch_fp32_coeffs((long long)s3, x->rho, x->rkh1, x->rkhor, x->rkver, x->lrho32, x->pkx32,
                        x->pky32, x->pkz32, s);
+    launch_vk32((long long)s3, g.nc, x->vz32, x->vset32, x->vk32, s);
   }
   CK(cudaGetLastError());
   struct {
@@ -686,7 +694,7 @@ int f3d_step(f3d_ctx* x) {
     launch_setsrc<double>(x->c64, d.halo(), d, x->g.nc, x->nsou, x->isrc, x->jsrc, x->ksrc, x->tmrat,
                           x->dz, x->zlayer, x->Hm1, x->g.dX1, x->g.dX2, x->dt, x->stream);
   }
-  if (x->prec == F3D_PREC_FP32 && x->opt_fused)
+  if (x->prec == F3D_PREC_FP32 && x->opt_fused && x->fused_ok)
     sizloop_fused(x);
   else if (x->prec == F3D_PREC_FP32)
     sizloop<float>(x);

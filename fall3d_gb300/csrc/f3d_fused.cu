@@ -2,31 +2,43 @@
 //
 // One CTA owns an output tile of one class and marches up the column, so
 // each concentration is read from and written to HBM once per step.  The
-// sweeps of Sources/sizloop.f90:35-71 are pipelined per horizontal plane k:
+// sweeps of Sources/sizloop.f90:35-71 are pipelined per horizontal plane:
+// iteration t runs
 //
-//   A  setbcc + advctzc   per column in registers (window of the original
-//                         column c(k-1..k+2) and work(k), work(k+1))
-//   B  advctx / advcty    x: warp shuffles along a row; y: shared memory
-//   C  diffz (plane k-1)  per column in registers (needs plane k of B)
-//   D  diffx / diffy      x: warp shuffles; y: shared memory
-//   E  wetdep, accum, clip, store (per cell)
+//   A  setbcc + advctzc   plane t, per column in registers (window of the
+//                         original column c(t-1..t+2) and work(t), work(t+1))
+//   B  advctx / advcty    plane t; x: warp shuffles along a row; y: shared
+//                         memory
+//   C  diffz              plane k = t-1 (needs plane t of B)
+//   D  diffx / diffy      plane k; x: warp shuffles; y: shared memory
+//   E  wetdep, accum, clip, store (plane k)
 //
-// Thread layout: the tile region H is 32 columns (one warp lane each) by HY
+// Thread layout: the tile region is 32 columns (one warp lane each) by HY
 // rows; warp w owns rows w, w+NW, w+2NW, ...  Every thread keeps the state of
-// its RPW columns in registers for the whole march; x neighbours are lanes of
-// the same warp, y neighbours go through one shared-memory plane.  The x/y
-// sweeps need +-2 cells (advection) then +-1 (diffusion), so the output tile
-// is (32-6) x (HY-6).  The ghost cells of setbcc are formed from the original
-// column (setbcc.f90:53-83) by the thread that owns the ghost position and
-// stay unchanged through the sweeps (the reference's stale ghosts).  Input
-// and output are distinct buffers (halos are read by neighbouring CTAs).
+// its RPW columns in registers for the whole march.  The x/y sweeps need +-2
+// cells (advection) then +-1 (diffusion), so the output tile is
+// (32-6) x (HY-6).  The ghost cells of setbcc are formed from the original
+// column (setbcc.f90:53-83) and stay unchanged through the sweeps (the
+// reference's stale ghosts).  Input and output are distinct buffers (halos
+// are read by neighbouring CTAs).
 //
-// Arithmetic is binary32 with the reference's formulas; divisions by dx, dy
-// and rho become multiplications by precomputed reciprocals.  The unit is
-// compiled with --fmad=false: each cell's result is then independent of the
-// tile shape.  The wet deposit and the dry-deposition accumulation stay
-// binary64.
+// Tiles whose region lies inside the domain (no ghost cell, no boundary
+// face within reach of an output cell) run a body without any boundary
+// logic; so do the planes 3..nz-2 (no top/bottom special case).  Halo cells
+// of the region compute with the interior formulas; their values are wrong
+// but never reach an output cell.
+//
+// Memory pipeline: the inputs of iteration t+1 are copied global -> shared
+// with cp.async while iteration t computes, into a double-buffered staging
+// area; each thread copies the positions it owns (coalesced rows of 32).
+//
+// Arithmetic is binary32 with the reference's formulas and operation order;
+// divisions by dx, dy and rho are multiplications by precomputed
+// reciprocals.  The unit is compiled with --fmad=false, so each cell's result
+// is independent of the tile shape.  The wet deposit and the dry-deposition
+// accumulation stay binary64.
 #include <algorithm>
+#include <type_traits>
 
 #include "f3d_fused.h"
 
@@ -40,13 +52,22 @@ struct ZT32 {
   float dzz, dzk, dzk_1, dzm1, l_dz, l_dzdz;
 };
 
+// 0.5*(SIGN(1,dr)+SIGN(1,dl))*MIN(|dr|,|dl|) (advctx.f90:40): +-min when
+// the signs agree, +0 when they differ.  Exact for every non-NaN dr, dl
+// (the reference's formula gives a NaN only for infinite slopes of opposite
+// sign).
+__device__ __forceinline__ float minmod(float dr, float dl) {
+  const float m = fminf(fabsf(dr), fabsf(dl));
+  const unsigned sr = __float_as_uint(dr) & 0x80000000u;
+  const unsigned diff = (__float_as_uint(dr) ^ __float_as_uint(dl)) & 0x80000000u;
+  return diff ? 0.0f : __uint_as_float(__float_as_uint(m) | sr);
+}
+
 __device__ __forceinline__ void zwork(float cm, float c0, float cp, float vk, float vk_1,
                                       const ZT32& z, float dt, float& w1, float& w2) {
   const float vk_12 = 0.5f * (vk + vk_1);
   w1 = dt * (vk * c0 - vk_1 * cm) * z.dzz;
-  const float deltar = (cp - c0) * z.dzk;
-  const float deltal = (c0 - cm) * z.dzk_1;
-  const float sigma = 0.5f * (sign1(deltar) + sign1(deltal)) * fmin2(fabsf(deltar), fabsf(deltal));
+  const float sigma = minmod((cp - c0) * z.dzk, (c0 - cm) * z.dzk_1);
   const float Crk = fabsf(vk_12) * dt * z.dzk_1;
   w2 = dt * 0.5f * z.dzm1 * (1.0f - Crk) * sigma * fabsf(vk_12) * z.dzz;
 }
@@ -56,56 +77,80 @@ __device__ __forceinline__ void line_work(float cm, float c0, float cp, float vq
                                           float auxv, float invd, float dt, float& w1, float& w2) {
   const float vq_12 = 0.5f * (vq + vq_1);
   w1 = auxv * (vq * c0 - vq_1 * cm);
-  const float deltar = (cp - c0) * invd;
-  const float deltal = (c0 - cm) * invd;
-  const float sigma = 0.5f * (sign1(deltar) + sign1(deltal)) * fmin2(fabsf(deltar), fabsf(deltal));
+  const float sigma = minmod((cp - c0) * invd, (c0 - cm) * invd);
   const float Cri = auxv * fabsf(vq_12);
   w2 = dt * 0.5f * (1.0f - Cri) * sigma * fabsf(vq_12);
 }
 
-// The update of advctx.f90:48-54.
+// The update of advctx.f90:48-54 (and advctzc.f90:66-72).
 __device__ __forceinline__ float line_update(float c0, float vq, float w1, float w1p, float w2,
                                              float w2m, float w2p) {
-  if (vq > 0.0f) return c0 - w1 - (w2 - w2m);
-  return c0 - w1p - (w2p - w2);
+  const bool up = vq > 0.0f;
+  const float a = up ? w1 : w1p;
+  const float b = up ? (w2 - w2m) : (w2p - w2);
+  return c0 - a - b;
 }
 
 // diffx/diffy cell of Sources/diffx.f90:20-55 with l = 1/rho, P = rkh*rho.
+// MAX(0,g) / MIN(0,g) of the reference keep 0 for a NaN g.
+__device__ __forceinline__ float diff_mid(float cm, float c0, float cp, float lm, float l0, float lp,
+                                          float Pm, float P0, float Pp, float dtdx2) {
+  const float gradr = 0.5f * (Pp + P0) * (cp * lp - c0 * l0);
+  const float gradl = 0.5f * (P0 + Pm) * (c0 * l0 - cm * lm);
+  return c0 + dtdx2 * (gradr - gradl);
+}
 __device__ __forceinline__ float diff_cell(bool first, bool last, float cm, float c0, float cp,
                                            float lm, float l0, float lp, float Pm, float P0,
                                            float Pp, float dtdx2) {
   float gradr, gradl;
   if (first) {
     gradr = Pp * (cp * lp - c0 * l0);
-    gradl = fmax2(0.0f, P0 * (c0 * l0 - cm * l0));
+    const float g = P0 * (c0 * l0 - cm * l0);
+    gradl = g > 0.0f ? g : 0.0f;
   } else if (last) {
-    gradr = fmin2(0.0f, P0 * (cp * l0 - c0 * l0));
+    const float g = P0 * (cp * l0 - c0 * l0);
+    gradr = g < 0.0f ? g : 0.0f;
     gradl = Pm * (c0 * l0 - cm * lm);
   } else {
-    const float rksr = 0.5f * (Pp + P0);
-    const float rksl = 0.5f * (P0 + Pm);
-    gradr = rksr * (cp * lp - c0 * l0);
-    gradl = rksl * (c0 * l0 - cm * lm);
+    return diff_mid(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, dtdx2);
   }
   return c0 + dtdx2 * (gradr - gradl);
 }
 
-// Position kinds inside the tile region.
-enum : int { K_OUT = 0, K_IN = 1, K_GX = 2, K_GY = 3 };
+__device__ __forceinline__ float clip0(float x) { return x > 0.0f ? x : 0.0f; }  // MAX(0,x)
+
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 4 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__device__ __forceinline__ float shup(float v) { return __shfl_up_sync(FULL, v, 1); }
+__device__ __forceinline__ float shdn(float v) { return __shfl_down_sync(FULL, v, 1); }
+
+// Staged fields of iteration t (plane index in parentheses).
+enum : int { F_C = 0, F_VK, F_VX, F_VY, F_L, F_PZ, F_L1, F_PX, F_PY, NF };
+//            c(t+2) vz+vset(t+1) vx(t) vy(t) 1/rho(t) K*rho_z(t) 1/rho(t-1) K*rho_x(t-1) K*rho_y(t-1)
+
+using False_ = std::integral_constant<bool, false>;
+using True_ = std::integral_constant<bool, true>;
 
 template <int HY, int NW>
 __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fused(const FusedArgs a) {
-  constexpr int HX = 32, NT = 32 * NW, RPW = HY / NW, TX = HX - 6, TY = HY - 6;
+  constexpr int HX = 32, NT = 32 * NW, RPW = HY / NW, TX = HX - 6, TY = HY - 6, NP = HX * HY;
   static_assert(HY % NW == 0, "rows must divide among warps");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* P0s = reinterpret_cast<float*>(smem_raw);  // y-sweep plane (advection)
-  float* W1s = P0s + HX * HY;
-  float* W2s = W1s + HX * HY;
-  float* P1s = W2s + HX * HY;                      // y-sweep plane (diffusion)
-  double* wacc = reinterpret_cast<double*>(P1s + HX * HY);  // wet state per output cell
+  // a guard row on either side keeps the +-1 row reads of halo rows in bounds
+  float* stage = reinterpret_cast<float*>(smem_raw) + HX;  // [2][NF][NP]
+  float* P0s = stage + 2 * NF * NP;                          // y-sweep planes
+  float* W1s = P0s + NP;
+  float* W2s = W1s + NP;
+  float* P1s = W2s + NP;
+  double* wacc = reinterpret_cast<double*>(P1s + NP + HX);  // wet state per output cell
   double* wlam = wacc + TX * TY;
-  double* wzi = wlam + TX * TY;
-  ZT32* tab = reinterpret_cast<ZT32*>(wzi + TX * TY);
+  int* wkz = reinterpret_cast<int*>(wlam + TX * TY);  // highest k with zlayer(k) <= zi
+  ZT32* tab = reinterpret_cast<ZT32*>(wkz + TX * TY);
 
   const Dims d = a.d;
   const int nx = d.nx, ny = d.ny, nz = d.nz;
@@ -117,6 +162,10 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
   const int oi1 = min(nx, i0 + TX - 1), oj1 = min(ny, j0 + TY - 1);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gi = gx0 + lane;
+  const bool xin = gi >= 1 && gi <= nx;  // interior x line position
+  const int pl = nx * ny;                 // met plane (32-bit offsets: checked on the host)
+  const int cs = (nx + 2) * (ny + 2);     // c plane
+  const bool edge = !(gx0 >= 1 && gx0 + HX - 1 <= nx && gy0 >= 1 && gy0 + HY - 1 <= ny);
 
   for (int k = threadIdx.x; k <= nz; k += NT) {
     ZT32 z;
@@ -131,49 +180,90 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
     tab[k] = z;
   }
   const bool wet = a.wet_class && a.wet_class[cls];
-  const long long pl = d.plane();
   for (int o = threadIdx.x; o < TX * TY; o += NT) {
     const int oi = i0 + o % TX, oj = j0 + o / TX;
     wacc[o] = 0.0;
     wlam[o] = 0.0;
-    wzi[o] = -1e300;
+    wkz[o] = 0;
     if (!wet || oi > oi1 || oj > oj1) continue;
-    const long long p2 = (long long)(oi - 1) + (long long)nx * (oj - 1);
+    const int p2 = (oi - 1) + nx * (oj - 1);
     wlam[o] = a.lambda2d[p2];
-    wzi[o] = a.zi[p2];
     wacc[o] = a.cwet[(long long)(cls + 1) * pl + p2];
+    // zlayer is non-decreasing (checked on the host), so the layers below
+    // the mixing height are a prefix of the column (wetdep.f90:37)
+    const double zi = a.zi[p2];
+    int kz = 0;
+    while (kz < nz && a.zlayer[kz] <= zi) ++kz;
+    wkz[o] = kz;
   }
-  __syncthreads();
 
-  const long long cs = (long long)(nx + 2) * (ny + 2);
   const float* __restrict__ cin = a.c_in + (long long)cls * a.cstride;
   float* __restrict__ cout = a.c_out + (long long)cls * a.cstride;
-  const float* __restrict__ vs = a.vset + (long long)cls * a.vstride;
+  const float* __restrict__ vkc = a.vk + (long long)cls * a.vstride;
   const float dt = a.dt;
   const float dznz = 1.0f / a.dz[nz];
-  const bool xin = gi >= 1 && gi <= nx;  // interior x line position
+  const float auxvx = a.auxvx, auxvy = a.auxvy;
+  const int cb0 = gi + (nx + 2) * (gy0 + warp);  // c(gi, gj, 0) of row r = 0
+  const int mb0 = (gi - 1) + nx * (gy0 + warp - 1);
 
   // ------------------------------------------------ per-position state
-  int kind[RPW];
+  unsigned kin = 0, kgx = 0, kgy = 0;  // position kinds as bit masks over r
   float o_0[RPW], o_p1[RPW], vk0[RPW], w1k[RPW], w2km[RPW], w2k[RPW], gtop[RPW];
-  float ra[RPW], rb[RPW], rc[RPW], fprev[RPW], gprev[RPW];
+  float ra[RPW], rb[RPW], rc[RPW], fprev[RPW], gprev[RPW], pb[RPW];
 #pragma unroll
   for (int r = 0; r < RPW; ++r) {
-    const int hy = warp + NW * r;
-    const int gj = gy0 + hy;
+    const int gj = gy0 + warp + NW * r;
     const bool yin = gj >= 1 && gj <= ny;
-    int kd = K_OUT;
-    if (xin && yin) kd = K_IN;
-    else if ((gi == 0 || gi == nx + 1) && yin) kd = K_GX;
-    else if ((gj == 0 || gj == ny + 1) && xin) kd = K_GY;
-    kind[r] = kd;
+    if (xin && yin) kin |= 1u << r;
+    else if ((gi == 0 || gi == nx + 1) && yin) kgx |= 1u << r;
+    else if ((gj == 0 || gj == ny + 1) && xin) kgy |= 1u << r;
     o_0[r] = o_p1[r] = vk0[r] = w1k[r] = w2km[r] = w2k[r] = gtop[r] = 0.0f;
-    ra[r] = rb[r] = rc[r] = fprev[r] = gprev[r] = 0.0f;
-    if (kd != K_IN) continue;
-    const long long cb = (long long)gi + (long long)(nx + 2) * gj;
-    const long long mb = (long long)(gi - 1) + (long long)nx * (gj - 1);
+    ra[r] = rb[r] = rc[r] = fprev[r] = gprev[r] = pb[r] = 0.0f;
+  }
+
+  // issue the staged inputs of iteration t into buffer t&1; positions outside
+  // the domain copy nothing (zero fill) from a clamped, valid address
+  auto prefetch = [&](auto edge_c, const int t) {
+    constexpr bool EDGE = decltype(edge_c)::value;
+    float* sb = stage + (t & 1) * (NF * NP);
+    const bool okc = t + 2 <= nz, okk = t + 1 <= nz, okm = t <= nz, okl = t >= 2;
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      const int p = (warp + NW * r) * HX + lane;
+      const bool in = !EDGE || (kin >> r & 1u);
+      const int co = in ? cb0 + NW * r * (nx + 2) : 0;
+      const int mo = in ? mb0 + NW * r * nx : 0;
+      if (okc) cp_async4(sb + F_C * NP + p, cin + co + (t + 2) * cs, in);
+      if (okk) cp_async4(sb + F_VK * NP + p, vkc + mo + t * pl, in);
+      if (okm) {
+        const int m = mo + (t - 1) * pl;
+        cp_async4(sb + F_VX * NP + p, a.vx + m, in);
+        cp_async4(sb + F_VY * NP + p, a.vy + m, in);
+        cp_async4(sb + F_L * NP + p, a.lrho + m, in);
+        cp_async4(sb + F_PZ * NP + p, a.pkz + m, in);
+      }
+      if (okl) {
+        const int m = mo + (t - 2) * pl;
+        cp_async4(sb + F_L1 * NP + p, a.lrho + m, in);
+        cp_async4(sb + F_PX * NP + p, a.pkx + m, in);
+        cp_async4(sb + F_PY * NP + p, a.pky + m, in);
+      }
+    }
+    cp_async_commit();
+  };
+  if (edge)
+    prefetch(True_{}, 1);
+  else
+    prefetch(False_{}, 1);
+
+  __syncthreads();  // tables and wet state
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    if (!(kin >> r & 1u)) continue;
+    const int gj = gy0 + warp + NW * r;
+    const int cb = cb0 + NW * r * (nx + 2), mb = mb0 + NW * r * nx;
     const float c1 = cin[cb + cs], c2 = cin[cb + 2 * cs];
-    const float vk1 = __ldg(a.vz + mb) + __ldg(vs + mb);
+    const float vk1 = __ldg(vkc + mb);
     float gb;  // setbcc bottom (setbcc.f90:19-33)
     if (vk1 >= 0.0f)
       gb = 0.0f;
@@ -186,63 +276,72 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
     w2km[r] = w2k[r];
     rc[r] = gb;  // diffz window: c(0) is the bottom ghost
     if (gi >= i0 && gi <= oi1 && gj >= j0 && gj <= oj1) {
-      cout[cb] = fmax2(0.0f, gb);  // clipped ghost (sizloop.f90:77)
-      if (gi == 1 && gj == 1) cout[d.C(0, 0, 0)] = fmax2(0.0f, c1);  // setbcc.f90:87-91
-      if (gi == nx && gj == 1) cout[d.C(nx + 1, 0, 0)] = fmax2(0.0f, c1);
-      if (gi == 1 && gj == ny) cout[d.C(0, ny + 1, 0)] = fmax2(0.0f, c1);
-      if (gi == nx && gj == ny) cout[d.C(nx + 1, ny + 1, 0)] = fmax2(0.0f, c1);
+      cout[cb] = clip0(gb);  // clipped ghost (sizloop.f90:77)
+      if (gi == 1 && gj == 1) cout[d.C(0, 0, 0)] = clip0(c1);  // setbcc.f90:87-91
+      if (gi == nx && gj == 1) cout[d.C(nx + 1, 0, 0)] = clip0(c1);
+      if (gi == 1 && gj == ny) cout[d.C(0, ny + 1, 0)] = clip0(c1);
+      if (gi == nx && gj == ny) cout[d.C(nx + 1, ny + 1, 0)] = clip0(c1);
     }
   }
 
-  const float auxvx = a.auxvx, auxvy = a.auxvy;
-  for (int t = 1; t <= nz + 1; ++t) {
-    const long long vpl = (long long)(t - 1) * pl;  // met plane t
+  // ------------------------------------------------ one iteration of the march
+  auto plane = [&](auto edge_c, auto steady_c, const int t) {
+    constexpr bool EDGE = decltype(edge_c)::value;
+    constexpr bool STEADY = decltype(steady_c)::value;  // 3 <= t <= nz-2
+    cp_async_wait_all();  // own staged inputs of iteration t are in shared memory
+    const float* sb = stage + (t & 1) * (NF * NP);
     float s2[RPW];
-    if (t <= nz) {
+    if (STEADY || t <= nz) {
       float s1[RPW];
+      const ZT32 zn = tab[(STEADY || t + 1 <= nz) ? t + 1 : nz];
       // ---------------- A: setbcc ghosts + advctzc for plane t
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
-        const int gj = gy0 + warp + NW * r;
-        s1[r] = 0.0f;
-        if (kind[r] == K_GX) {  // x-face ghost from the original column (setbcc.f90:53-66)
-          const int ia = gi == 0 ? 1 : nx;
-          const float cadj = cin[(long long)ia + (long long)(nx + 2) * (gj + (long long)(ny + 2) * t)];
-          const float v = __ldg(a.vx + vpl + (long long)(ia - 1) + (long long)nx * (gj - 1));
-          s1[r] = (gi == 0) ? (v >= 0.0f ? 0.0f : cadj) : (v <= 0.0f ? 0.0f : cadj);
-        } else if (kind[r] == K_GY) {  // y-face ghost (setbcc.f90:70-83)
-          const int ja = gj == 0 ? 1 : ny;
-          const float cadj = cin[(long long)gi + (long long)(nx + 2) * (ja + (long long)(ny + 2) * t)];
-          const float v = __ldg(a.vy + vpl + (long long)(gi - 1) + (long long)nx * (ja - 1));
-          s1[r] = (gj == 0) ? (v >= 0.0f ? 0.0f : cadj) : (v <= 0.0f ? 0.0f : cadj);
-        } else if (kind[r] == K_IN) {
-          const long long cb = (long long)gi + (long long)(nx + 2) * gj;
-          const long long mb = (long long)(gi - 1) + (long long)nx * (gj - 1);
+        const int hy = warp + NW * r;
+        const int p = hy * HX + lane;
+        float ghost = 0.0f;
+        if constexpr (EDGE) {
+          const int gj = gy0 + hy;
+          // x-face ghosts take c(1|nx, j, t) and vx from the neighbour lane
+          // (setbcc.f90:53-66)
+          const float cn_up = shup(o_0[r]), cn_dn = shdn(o_0[r]);
+          const float vxo = sb[F_VX * NP + p];
+          const float vx_up = shup(vxo), vx_dn = shdn(vxo);
+          ghost = (gi == 0) ? (vx_dn >= 0.0f ? 0.0f : cn_dn) : (vx_up <= 0.0f ? 0.0f : cn_up);
+          if (gj == 0 || gj == ny + 1) {  // y-face ghosts (setbcc.f90:70-83)
+            ghost = 0.0f;
+            if (xin) {
+              const int ja = gj == 0 ? 1 : ny;
+              const float cadj = cin[gi + (nx + 2) * ja + t * cs];
+              const float v = __ldg(a.vy + (t - 1) * pl + (gi - 1) + nx * (ja - 1));
+              ghost = (gj == 0) ? (v >= 0.0f ? 0.0f : cadj) : (v <= 0.0f ? 0.0f : cadj);
+            }
+          }
+        }
+        {  // the column update, on every position (zero inputs outside the domain)
           float w1n, w2n, o_p2 = 0.0f, vkp = 0.0f;
-          if (t + 1 <= nz) {
-            vkp = __ldg(a.vz + mb + (long long)t * pl) + __ldg(vs + mb + (long long)t * pl);
-            if (t + 2 <= nz) {
-              o_p2 = cin[cb + (long long)(t + 2) * cs];
+          if (STEADY || t + 1 <= nz) {
+            vkp = sb[F_VK * NP + p];
+            if (STEADY || t + 2 <= nz) {
+              o_p2 = sb[F_C * NP + p];
             } else {  // the top ghost (setbcc.f90:37-49), vkp = vk(nz)
               o_p2 = (vkp <= 0.0f) ? 0.0f : o_p1[r];
               gtop[r] = o_p2;
-              if (gi >= i0 && gi <= oi1 && gj >= j0 && gj <= oj1) {
-                cout[cb + (long long)(nz + 1) * cs] = fmax2(0.0f, o_p2);
-                if (gi == 1 && gj == 1) cout[d.C(0, 0, nz + 1)] = fmax2(0.0f, o_p1[r]);
-                if (gi == nx && gj == 1) cout[d.C(nx + 1, 0, nz + 1)] = fmax2(0.0f, o_p1[r]);
-                if (gi == 1 && gj == ny) cout[d.C(0, ny + 1, nz + 1)] = fmax2(0.0f, o_p1[r]);
-                if (gi == nx && gj == ny) cout[d.C(nx + 1, ny + 1, nz + 1)] = fmax2(0.0f, o_p1[r]);
+              const int gj = gy0 + hy;
+              if (gi >= i0 && gi <= oi1 && gj >= j0 && gj <= oj1) {  // an interior position
+                cout[cb0 + NW * r * (nx + 2) + (nz + 1) * cs] = clip0(o_p2);
+                if (gi == 1 && gj == 1) cout[d.C(0, 0, nz + 1)] = clip0(o_p1[r]);
+                if (gi == nx && gj == 1) cout[d.C(nx + 1, 0, nz + 1)] = clip0(o_p1[r]);
+                if (gi == 1 && gj == ny) cout[d.C(0, ny + 1, nz + 1)] = clip0(o_p1[r]);
+                if (gi == nx && gj == ny) cout[d.C(nx + 1, ny + 1, nz + 1)] = clip0(o_p1[r]);
               }
             }
-            zwork(o_0[r], o_p1[r], o_p2, vkp, vk0[r], tab[t + 1], dt, w1n, w2n);
+            zwork(o_0[r], o_p1[r], o_p2, vkp, vk0[r], zn, dt, w1n, w2n);
           } else {  // t == nz: work(nz+1,1) (advctzc.f90:58-64)
             w1n = dt * vk0[r] * (gtop[r] - o_0[r]) * dznz;
             w2n = w2k[r];
           }
-          if (vk0[r] > 0.0f)
-            s1[r] = o_0[r] - w1k[r] - (w2k[r] - w2km[r]);
-          else
-            s1[r] = o_0[r] - w1n - (w2n - w2k[r]);
+          s1[r] = (vk0[r] > 0.0f) ? o_0[r] - w1k[r] - (w2k[r] - w2km[r]) : o_0[r] - w1n - (w2n - w2k[r]);
           w2km[r] = w2k[r];
           w2k[r] = w2n;
           w1k[r] = w1n;
@@ -250,66 +349,77 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
           o_p1[r] = o_p2;
           vk0[r] = vkp;
         }
+        if constexpr (EDGE) {
+          if ((kgx | kgy) >> r & 1u) s1[r] = ghost;
+        }
       }
       // ---------------- B: advctx (shuffles) and advcty (shared memory)
       auto adv_x = [&](const float* in, float* out) {
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
-          const int gj = gy0 + warp + NW * r;
-          const bool row = gj >= 1 && gj <= ny;
+          const int p = (warp + NW * r) * HX + lane;
           const float c0 = in[r];
-          const float v = (row && xin) ? __ldg(a.vx + vpl + (long long)(gi - 1) + (long long)nx * (gj - 1)) : 0.0f;
-          const float cm = __shfl_up_sync(FULL, c0, 1), cp = __shfl_down_sync(FULL, c0, 1);
-          const float vm_raw = __shfl_up_sync(FULL, v, 1);
-          const float vm = gi > 1 ? vm_raw : v;  // v(max(1,q-1))
-          float w1 = 0.0f, w2 = 0.0f;
-          if (xin) line_work(cm, c0, cp, v, vm, auxvx, a.inv_dx, dt, w1, w2);
-          else if (gi == nx + 1) w1 = auxvx * vm_raw * (c0 - cm);  // work(nx+1,1) (advctx.f90:46)
-          const float w1p = __shfl_down_sync(FULL, w1, 1);
-          const float w2m_raw = __shfl_up_sync(FULL, w2, 1), w2p_raw = __shfl_down_sync(FULL, w2, 1);
-          const float w2m = gi > 1 ? w2m_raw : w2;
-          const float w2p = gi < nx ? w2p_raw : w2;
-          out[r] = (row && xin) ? line_update(c0, v, w1, w1p, w2, w2m, w2p) : c0;
+          const float v = sb[F_VX * NP + p];  // 0 outside the domain
+          const float cm = shup(c0), cp = shdn(c0);
+          const float vm_raw = shup(v);
+          float w1, w2;
+          if constexpr (EDGE) {
+            const float vm = gi == 1 ? v : vm_raw;  // v(max(1,q-1))
+            line_work(cm, c0, cp, v, vm, auxvx, a.inv_dx, dt, w1, w2);
+            if (gi == nx + 1) w1 = auxvx * vm_raw * (c0 - cm);  // work(nx+1,1) (advctx.f90:46)
+          } else {
+            line_work(cm, c0, cp, v, vm_raw, auxvx, a.inv_dx, dt, w1, w2);
+          }
+          const float w1p = shdn(w1);
+          const float w2m_raw = shup(w2), w2p_raw = shdn(w2);
+          if constexpr (EDGE) {
+            const float w2m = gi == 1 ? w2 : w2m_raw;
+            const float w2p = gi == nx ? w2 : w2p_raw;
+            const float u = line_update(c0, v, w1, w1p, w2, w2m, w2p);
+            out[r] = (kin >> r & 1u) ? u : c0;
+          } else {
+            out[r] = line_update(c0, v, w1, w1p, w2, w2m_raw, w2p_raw);
+          }
         }
       };
       auto adv_y = [&](const float* in, float* out) {
 #pragma unroll
         for (int r = 0; r < RPW; ++r) P0s[(warp + NW * r) * HX + lane] = in[r];
         __syncthreads();
+        // every thread is past iteration t-1: its staging buffer may be refilled
+        prefetch(edge_c, t + 1);
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
           const int hy = warp + NW * r;
-          const int gj = gy0 + hy;
-          float w1 = 0.0f, w2 = 0.0f;
-          if (xin && gj >= 1 && gj <= ny + 1) {
-            const float c0 = P0s[hy * HX + lane];
-            const float cm = P0s[max(hy - 1, 0) * HX + lane];
-            const long long mcol = vpl + (long long)(gi - 1);
-            if (gj <= ny) {
-              const float cp = P0s[min(hy + 1, HY - 1) * HX + lane];
-              const float v = __ldg(a.vy + mcol + (long long)nx * (gj - 1));
-              const float vm = __ldg(a.vy + mcol + (long long)nx * (gj > 1 ? gj - 2 : 0));
-              line_work(cm, c0, cp, v, vm, auxvy, a.inv_dy, dt, w1, w2);
-            } else {  // work(ny+1,1) (advcty.f90:45)
-              w1 = auxvy * __ldg(a.vy + mcol + (long long)nx * (ny - 1)) * (c0 - cm);
-            }
+          const int p = hy * HX + lane;
+          float w1, w2;
+          const float c0 = P0s[p], cm = P0s[p - HX], cp = P0s[p + HX];
+          const float v = sb[F_VY * NP + p], vm_raw = sb[F_VY * NP + p - HX];  // vy(i, j-1)
+          if constexpr (EDGE) {  // row conditions are uniform across the warp
+            const int gj = gy0 + hy;
+            line_work(cm, c0, cp, v, gj == 1 ? v : vm_raw, auxvy, a.inv_dy, dt, w1, w2);
+            if (gj == ny + 1) w1 = auxvy * vm_raw * (c0 - cm);  // work(ny+1,1) (advcty.f90:45)
+          } else {
+            line_work(cm, c0, cp, v, vm_raw, auxvy, a.inv_dy, dt, w1, w2);
           }
-          W1s[hy * HX + lane] = w1;
-          W2s[hy * HX + lane] = w2;
+          W1s[p] = w1;
+          W2s[p] = w2;
         }
         __syncthreads();
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
           const int hy = warp + NW * r;
-          const int gj = gy0 + hy;
-          out[r] = in[r];
-          if (xin && gj >= 1 && gj <= ny) {
-            const float v = __ldg(a.vy + vpl + (long long)(gi - 1) + (long long)nx * (gj - 1));
-            const int hm = max(hy - 1, 0), hp = min(hy + 1, HY - 1);
-            const float w2 = W2s[hy * HX + lane];
-            const float w2m = gj > 1 ? W2s[hm * HX + lane] : w2;
-            const float w2p = gj < ny ? W2s[hp * HX + lane] : w2;
-            out[r] = line_update(in[r], v, W1s[hy * HX + lane], W1s[hp * HX + lane], w2, w2m, w2p);
+          const int p = hy * HX + lane;
+          const float v = sb[F_VY * NP + p];
+          const float w2 = W2s[p], w2m_raw = W2s[p - HX], w2p_raw = W2s[p + HX];
+          if constexpr (EDGE) {
+            const int gj = gy0 + hy;
+            const float w2m = gj == 1 ? w2 : w2m_raw;
+            const float w2p = gj == ny ? w2 : w2p_raw;
+            const float u = line_update(in[r], v, W1s[p], W1s[p + HX], w2, w2m, w2p);
+            out[r] = (kin >> r & 1u) ? u : in[r];
+          } else {
+            out[r] = line_update(in[r], v, W1s[p], W1s[p + HX], w2, w2m_raw, w2p_raw);
           }
         }
       };
@@ -324,93 +434,101 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
     } else {
 #pragma unroll
       for (int r = 0; r < RPW; ++r) s2[r] = 0.0f;
+      __syncthreads();  // the y-sweep plane of the previous iteration is read by all warps
     }
-    if (t < 2) {
+    if (!STEADY && t < 2) {
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
-        if (kind[r] == K_IN) {
-          ra[r] = rb[r];
-          rb[r] = rc[r];
-          rc[r] = s2[r];
-        } else {
-          gprev[r] = s2[r];  // ghost (or unused) value of plane t
-        }
+        const int p = (warp + NW * r) * HX + lane;
+        if (EDGE) gprev[r] = s2[r];  // ghost value of plane t
+        ra[r] = rb[r];
+        rb[r] = rc[r];
+        rc[r] = s2[r];
+        pb[r] = sb[F_PZ * NP + p];  // rkver*rho at plane 1
       }
-      continue;
+      return;
     }
     // ---------------- C: diffz for plane k = t-1 (diffz.f90:22-62)
     const int k = t - 1;
-    const long long kpl = (long long)(k - 1) * pl;
     float s3[RPW];
+    const ZT32 zk = tab[k];
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
-      if (kind[r] != K_IN) {
-        s3[r] = gprev[r];  // ghost value of plane k (unchanged by the sweeps)
-        gprev[r] = s2[r];
-        continue;
-      }
-      const int gj = gy0 + warp + NW * r;
+      const int p = (warp + NW * r) * HX + lane;
+      // window c(k-1), c(k), c(k+1); past the last plane c(nz+1) is the top
+      // ghost (diffz.f90:54)
       ra[r] = rb[r];
       rb[r] = rc[r];
-      rc[r] = (t <= nz) ? s2[r] : gtop[r];  // c(nz+1): the top ghost (diffz.f90:54)
-      const long long m = kpl + (long long)(gi - 1) + (long long)nx * (gj - 1);
-      const float lb = __ldg(a.lrho + m), pb = __ldg(a.pkz + m);
+      rc[r] = (STEADY || t <= nz) ? s2[r] : gtop[r];
+      // 1/rho at k and k+1, K*rho at k (carried) and k+1
+      const float lb = sb[F_L1 * NP + p];
       float work;
-      if (k == 1) {
-        const float lc = __ldg(a.lrho + m + pl), pc = __ldg(a.pkz + m + pl);
-        const float qt = rc[r] * lc - rb[r] * lb;
-        const float gradt = pc * qt * tab[1].l_dz;
-        const float gradb = fmax2(0.0f, pb * (rb[r] * lb - ra[r] * lb) * tab[0].l_dz);
-        work = dt * (gradt - gradb) * tab[1].l_dzdz;
-        fprev[r] = 0.5f * (pc + pb) * qt * tab[1].l_dz;
-      } else if (k == nz) {
-        const float la = __ldg(a.lrho + m - pl), pa = __ldg(a.pkz + m - pl);
-        const float gradt = fmin2(0.0f, pb * (rc[r] * lb - rb[r] * lb) * tab[nz].l_dz);
-        const float gradb = pa * (rb[r] * lb - ra[r] * la) * tab[nz - 1].l_dz;
-        work = dt * (gradt - gradb) * tab[nz].l_dz;
-      } else {
-        const float lc = __ldg(a.lrho + m + pl), pc = __ldg(a.pkz + m + pl);
-        const ZT32 zk = tab[k];
-        const float gradt = 0.5f * (pc + pb) * (rc[r] * lc - rb[r] * lb) * zk.l_dz;
+      if (STEADY || (k > 1 && k < nz)) {
+        const float lc = sb[F_L * NP + p], pc = sb[F_PZ * NP + p];
+        const float gradt = 0.5f * (pc + pb[r]) * (rc[r] * lc - rb[r] * lb) * zk.l_dz;
         work = dt * (gradt - fprev[r]) * zk.l_dzdz;
         fprev[r] = gradt;
+        pb[r] = pc;
+      } else if (k == 1) {
+        const float lc = sb[F_L * NP + p], pc = sb[F_PZ * NP + p];
+        const float qt = rc[r] * lc - rb[r] * lb;
+        const float gradt = pc * qt * tab[1].l_dz;
+        const float g = pb[r] * (rb[r] * lb - ra[r] * lb) * tab[0].l_dz;
+        const float gradb = g > 0.0f ? g : 0.0f;  // MAX(0,g): 0 for NaN
+        work = dt * (gradt - gradb) * tab[1].l_dzdz;
+        fprev[r] = 0.5f * (pc + pb[r]) * qt * tab[1].l_dz;
+        pb[r] = pc;
+      } else {  // k == nz
+        const int m = ((kin >> r & 1u) ? mb0 + NW * r * nx : 0) + (nz - 2) * pl;
+        const float la = __ldg(a.lrho + m), pa = __ldg(a.pkz + m);
+        const float g = pb[r] * (rc[r] * lb - rb[r] * lb) * tab[nz].l_dz;
+        const float gradt = g < 0.0f ? g : 0.0f;
+        const float gradb = pa * (rb[r] * lb - ra[r] * la) * tab[nz - 1].l_dz;
+        work = dt * (gradt - gradb) * tab[nz].l_dz;
       }
       s3[r] = rb[r] + work;
+      if constexpr (EDGE) {
+        if (!(kin >> r & 1u)) s3[r] = gprev[r];  // ghost value of plane k (unchanged by the sweeps)
+        gprev[r] = s2[r];
+      }
     }
     // ---------------- D: diffx (shuffles) and diffy (shared memory)
     auto dif_x = [&](const float* in, float* out) {
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
-        const int gj = gy0 + warp + NW * r;
-        const bool row = gj >= 1 && gj <= ny;
-        const long long m = kpl + (long long)(gi - 1) + (long long)nx * (gj - 1);
-        const float l0 = (row && xin) ? __ldg(a.lrho + m) : 0.0f;
-        const float P0 = (row && xin) ? __ldg(a.pkx + m) : 0.0f;
+        const int p = (warp + NW * r) * HX + lane;
+        const float l0 = sb[F_L1 * NP + p], P0 = sb[F_PX * NP + p];
         const float c0 = in[r];
-        const float cm = __shfl_up_sync(FULL, c0, 1), cp = __shfl_down_sync(FULL, c0, 1);
-        const float lm = __shfl_up_sync(FULL, l0, 1), lp = __shfl_down_sync(FULL, l0, 1);
-        const float Pm = __shfl_up_sync(FULL, P0, 1), Pp = __shfl_down_sync(FULL, P0, 1);
-        out[r] = (row && xin) ? diff_cell(gi == 1, gi == nx, cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2)
-                              : c0;
+        const float cm = shup(c0), cp = shdn(c0);
+        const float lm = shup(l0), lp = shdn(l0);
+        const float Pm = shup(P0), Pp = shdn(P0);
+        if constexpr (EDGE) {
+          float u = diff_mid(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2);
+          if (gi == 1 || gi == nx) u = diff_cell(gi == 1, gi == nx, cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2);
+          out[r] = (kin >> r & 1u) ? u : c0;
+        } else {
+          out[r] = diff_mid(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2);
+        }
       }
     };
     auto dif_y = [&](const float* in, float* out) {
 #pragma unroll
       for (int r = 0; r < RPW; ++r) P1s[(warp + NW * r) * HX + lane] = in[r];
       __syncthreads();
+      const float* L = sb + F_L1 * NP;
+      const float* PY = sb + F_PY * NP;
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
         const int hy = warp + NW * r;
-        const int gj = gy0 + hy;
-        out[r] = in[r];
-        if (xin && gj >= 1 && gj <= ny) {
-          const long long m = kpl + (long long)(gi - 1) + (long long)nx * (gj - 1);
-          const float l0 = __ldg(a.lrho + m), P0 = __ldg(a.pky + m);
-          const bool first = gj == 1, last = gj == ny;
-          const float lm = first ? 0.0f : __ldg(a.lrho + m - nx), Pm = first ? 0.0f : __ldg(a.pky + m - nx);
-          const float lp = last ? 0.0f : __ldg(a.lrho + m + nx), Pp = last ? 0.0f : __ldg(a.pky + m + nx);
-          const float cm = P1s[max(hy - 1, 0) * HX + lane], cp = P1s[min(hy + 1, HY - 1) * HX + lane];
-          out[r] = diff_cell(first, last, cm, in[r], cp, lm, l0, lp, Pm, P0, Pp, a.dtdy2);
+        const int p = hy * HX + lane;
+        const int hm = p - HX, hp = p + HX;
+        if constexpr (EDGE) {
+          const int gj = gy0 + hy;
+          const float u = diff_cell(gj == 1, gj == ny, P1s[hm], in[r], P1s[hp], L[hm], L[p], L[hp], PY[hm],
+                                    PY[p], PY[hp], a.dtdy2);
+          out[r] = (kin >> r & 1u) ? u : in[r];
+        } else {
+          out[r] = diff_mid(P1s[hm], in[r], P1s[hp], L[hm], L[p], L[hp], PY[hm], PY[p], PY[hp], a.dtdy2);
         }
       }
     };
@@ -423,49 +541,71 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
       dif_x(s3a, s4);
     }
     // ---------------- E: wetdep, accum, clip, store (plane k)
-    const double zl = a.zlayer[k - 1], dzk64 = a.dz64[k];
+    const double dzk64 = a.dz64[k];
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
-      const int gj = gy0 + warp + NW * r;
-      const bool rows_out = gj >= j0 && gj <= oj1;
-      if (kind[r] == K_GX && rows_out && ((gi == 0 && i0 == 1) || (gi == nx + 1 && oi1 == nx))) {
-        cout[(long long)gi + (long long)(nx + 2) * (gj + (long long)(ny + 2) * k)] = fmax2(0.0f, s3[r]);
-        continue;
+      const int hy = warp + NW * r;
+      const int gj = gy0 + hy;
+      const int cidx = cb0 + NW * r * (nx + 2) + k * cs;
+      bool out_cell;
+      if constexpr (EDGE) {
+        const bool rows_out = gj >= j0 && gj <= oj1;
+        const bool cols_out = gi >= i0 && gi <= oi1;
+        if ((kgx >> r & 1u) && rows_out && ((gi == 0 && i0 == 1) || (gi == nx + 1 && oi1 == nx))) {
+          cout[cidx] = clip0(s3[r]);
+          continue;
+        }
+        if ((kgy >> r & 1u) && cols_out && ((gj == 0 && j0 == 1) || (gj == ny + 1 && oj1 == ny))) {
+          cout[cidx] = clip0(s3[r]);
+          continue;
+        }
+        out_cell = (kin >> r & 1u) && rows_out && cols_out;
+      } else {
+        out_cell = lane >= 3 && lane < 3 + TX && hy >= 3 && hy < 3 + TY;
       }
-      const bool cols_out = gi >= i0 && gi <= oi1;
-      if (kind[r] == K_GY && cols_out && ((gj == 0 && j0 == 1) || (gj == ny + 1 && oj1 == ny))) {
-        cout[(long long)gi + (long long)(nx + 2) * (gj + (long long)(ny + 2) * k)] = fmax2(0.0f, s3[r]);
-        continue;
-      }
-      if (kind[r] != K_IN || !rows_out || !cols_out) continue;
+      if (!out_cell) continue;
       float cnew = s4[r];
-      const int o = (gi - i0) + TX * (gj - j0);
-      if (wet && zl <= wzi[o]) {  // wetdep (wetdep.f90:37-49)
-        wacc[o] = wacc[o] + dzk64 * wlam[o] * (double)cnew;
-        cnew = (float)((double)cnew * (1.0 - wlam[o]));
+      if (wet) {
+        const int o = (gi - i0) + TX * (gj - j0);
+        if (k <= wkz[o]) {  // wetdep (wetdep.f90:37-49)
+          wacc[o] = wacc[o] + dzk64 * wlam[o] * (double)cnew;
+          cnew = (float)((double)cnew * (1.0 - wlam[o]));
+        }
       }
-      const long long p2 = (long long)(gi - 1) + (long long)nx * (gj - 1);
-      if (k == 1) {  // accum (accum.f90:17-25), binary64
-        double* cd = a.cdry + (long long)(cls + 1) * pl + p2;
-        const double vsd = a.vset64[(long long)cls * a.vstride + p2] + a.vdep64[(long long)cls * pl + p2];
+      if (!STEADY && k == 1) {  // accum (accum.f90:17-25), binary64
+        const int mb = mb0 + NW * r * nx;
+        double* cd = a.cdry + (long long)(cls + 1) * pl + mb;
+        const double vsd = a.vset64[(long long)cls * a.vstride + mb] + a.vdep64[(long long)cls * pl + mb];
         *cd = *cd - a.dt64 * (double)cnew * fmin2(0.0, vsd);
       }
-      cout[(long long)gi + (long long)(nx + 2) * (gj + (long long)(ny + 2) * k)] = fmax2(0.0f, cnew);
+      cout[cidx] = clip0(cnew);
     }
-  }
+  };
+
+  auto march = [&](auto edge_c) {
+    for (int t = 1; t <= 2; ++t) plane(edge_c, False_{}, t);
+    for (int t = 3; t <= nz - 2; ++t) plane(edge_c, True_{}, t);
+    for (int t = max(3, nz - 1); t <= nz + 1; ++t) plane(edge_c, False_{}, t);
+  };
+  if (edge)
+    march(True_{});
+  else
+    march(False_{});
+
   if (wet) {
     __syncthreads();
     for (int o = threadIdx.x; o < TX * TY; o += NT) {
       const int oi = i0 + o % TX, oj = j0 + o / TX;
       if (oi > oi1 || oj > oj1) continue;
-      a.cwet[(long long)(cls + 1) * pl + (long long)(oi - 1) + (long long)nx * (oj - 1)] = wacc[o];
+      a.cwet[(long long)(cls + 1) * pl + (oi - 1) + nx * (oj - 1)] = wacc[o];
     }
   }
 }
 
 template <int HY>
 size_t fused_smem(int nz) {
-  return sizeof(float) * 4 * 32 * HY + 3 * sizeof(double) * 26 * (HY - 6) + sizeof(ZT32) * (size_t)(nz + 1);
+  return sizeof(float) * ((2 * NF + 4) * 32 * HY + 2 * 32) +
+         (2 * sizeof(double) + sizeof(int)) * 26 * (HY - 6) + sizeof(ZT32) * (size_t)(nz + 1);
 }
 
 template <int HY, int NW>
@@ -493,6 +633,21 @@ void launch_step_fused(const FusedArgs& a, int shape, cudaStream_t s) {
       launch_fused_t<32, 8>(a, s);
       break;
   }
+}
+
+// vz + vset per class in binary32 (the vertical velocity of advctzc.f90:23).
+__global__ void k_vk32(long long n, int nc, const float* vz, const float* vset, float* vk) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float v = vz[q];
+    for (int c = 0; c < nc; ++c) vk[c * n + q] = v + vset[c * n + q];
+  }
+}
+
+void launch_vk32(long long n, int nc, const float* vz, const float* vset, float* vk, cudaStream_t s) {
+  const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  k_vk32<<<nb, 256, 0, s>>>(n, nc, vz, vset, vk);
+  count_launch();
 }
 
 // wet-deposition rate per column for the fused kernel: lambda =

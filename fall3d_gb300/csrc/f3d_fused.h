@@ -16,7 +16,7 @@ struct FusedArgs {
   double dt64;
   // binary32 coefficients (scaled fields of meteo.f90:108-112)
   const float *vx, *vy, *vz;
-  const float* vset;  // class blocks of nx*ny*nz
+  const float* vk;  // vz + vset, class blocks of nx*ny*nz
   long long vstride;
   const float* vdep;  // class blocks of nx*ny
   long long dstride;
@@ -40,6 +40,7 @@ struct FusedArgs {
 // tile region (x by y) / threads: 0 = 32x32 / 256 (default), 1 = 32x64 / 512,
 // 2 = 32x32 / 512.
 void launch_step_fused(const FusedArgs& a, int shape, cudaStream_t s);
+void launch_vk32(long long n, int nc, const float* vz, const float* vset, float* vk, cudaStream_t s);
 void launch_wet_lambda(long long n, double dt, const double* prate, double* lam, cudaStream_t s);
 void launch_fp32_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,
                         const double* rkver, float* lrho, float* pkx, float* pky, float* pkz,

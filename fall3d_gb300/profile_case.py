@@ -3,6 +3,10 @@ that profiler captures of the step kernels run.
 
     python -m fall3d_gb300.profile_case [--workload cfg1] [--steps 3]
                                         [--precision 32] [--fused 1] [--tile 0]
+                                        [--time]
+
+With --time, the steps after the first are timed per kernel with CUDA
+events and printed as milliseconds per launch.
 """
 from __future__ import annotations
 
@@ -20,6 +24,7 @@ def main():
     ap.add_argument("--fused", type=int, default=1)
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--classes", type=int, default=0, help="override the class count")
+    ap.add_argument("--time", action="store_true", help="print per-kernel times")
     args = ap.parse_args()
     over = {"max_snapshots": 2}
     if args.classes:
@@ -31,7 +36,15 @@ def main():
         g.set_option(F.OPT_TILE, args.tile)
     g.source(0)
     g.meteo(0)
-    g.step(args.steps)
+    if args.time:
+        g.step(1)
+        g.profile(True)
+        g.step(args.steps - 1)
+        g.sync()
+        for name, (n, ms) in sorted(g.profile_read().items(), key=lambda kv: -kv[1][1]):
+            print(f"  {name:12s} {n:4d} launches {ms / max(n, 1):9.4f} ms/launch")
+    else:
+        g.step(args.steps)
     g.sync()
     st = g.state()
     print(f"{args.workload}: {st['iiter']} steps, dt {st['dt']:.3f} s, outmass {st['outmass']:.6e}")

@@ -366,7 +366,9 @@ int f3d_run_reset(f3d_ctx* ctx);
 
 /* Options of a context (f3d_set_option / f3d_get_option). */
 #define F3D_OPT_FUSED 1  /* FP32 form: 1 = one fused kernel per step (default),
-                            0 = one kernel per reference routine          */
+                            0 = one kernel per reference routine.  Grids
+                            with a decreasing zlayer or >= 2^31 cells per
+                            class always use the per-routine kernels.     */
 #define F3D_OPT_TILE  2  /* fused kernel tile region x by y / threads:
                             0 = 32x32/256 (default), 1 = 32x64/512,
                             2 = 32x32/512; results do not depend on it   */
