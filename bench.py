@@ -58,7 +58,7 @@ def _scenario(max_snapshots=4):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -74,7 +74,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -111,13 +111,13 @@ class ClockSampler:
 
 
 # Algorithmic bytes per cell-class of each kernel (element size S).  The
-# fused step reads c and the class's vertical velocity vz+vset (combined once
-# per meteo interval) and writes c once per cell-class, and reads the six
-# class-independent fields (vx, vy, 1/rho and the three K*rho products) once
-# per cell: 3S + 6S/nc.  The per-routine kernels read every operand once and
-# write every output once, met fields per class.
+# whole step (and so the fused step kernel) has the fixed contract figure
+# 2S (read and write c) + S (vset) + 7S/nc (the class-shared fields vx, vy,
+# vz, rho, rkhor, rkh1, rkver, amortised over the classes) = 3S + 7S/nc,
+# whatever the kernel actually moves.  The per-routine kernels read every
+# operand once and write every output once, met fields per class.
 def kernel_bytes_per_cell_class(S, nc):
-    return {"step_fused": 3 * S + 6 * S / nc, "advctzc": 4 * S, "advctx": 3 * S, "advcty": 3 * S,
+    return {"step_fused": 3 * S + 7 * S / nc, "advctzc": 4 * S, "advctx": 3 * S, "advcty": 3 * S,
             "diffz": 4 * S, "diffx": 4 * S, "diffy": 4 * S, "clip": 2 * S}
 
 
@@ -317,7 +317,7 @@ def run_ours(args, rank, world, local_rank):
                 "frac": achieved / peak, "traffic": traffic, "kernel": dom_name,
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
                 "peak_source": f"{peak_kind} hbm_gbs"}
-    step_bytes = 12 + 24 / nc  # binary32 algorithmic bytes per cell-class-step
+    step_bytes = 12 + 28 / nc  # binary32 algorithmic bytes per cell-class-step
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -351,7 +351,7 @@ def run_ours(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")

@@ -20,10 +20,16 @@
  *    x86 produces a negative one, so the policy is written out explicitly.
  *  - libm: pow/exp/log/log10/acos/tan/atan/sin of the host C library.
  *
- * Parity status: UNPINNED by the reference's own tests.  The reference ships
- * no tests, golden vectors or fixtures, and it cannot be compiled in this
- * environment (Fortran, no Fortran compiler).  The oracle is instead pinned
- * by known-answer tests and the golden vectors in tests/golden/.
+ * Parity status: pinned against outputs of the reference itself.  The
+ * reference ships no tests, golden vectors or fixtures, and there is no
+ * Fortran compiler here; oracle/ref_translate.py translates the reference's
+ * own hot-path Fortran mechanically into C and builds it (oracle/_ref/),
+ * tests/golden/make_golden.py runs that build on six scenarios (every
+ * turbulence and settling model, UTM and lon-lat, wet deposition, two
+ * meteo updates, 60 steps of cfg0) and stores the fields, budgets and
+ * iteration counts, and tests/test_golden_cpu.py checks this oracle against
+ * them bit for bit.  Known-answer tests (tests/test_oracle_cpu.py) add
+ * analytic checks.
  */
 #include <cmath>
 #include <cstdint>
