@@ -378,6 +378,76 @@ int f3d_cmass2d(const double* c, const double* vx, const double* vy, const doubl
   return F3D_OK;
 }
 
+// ------------------------------------------------------------------------
+// cmass2d without allocation.  The block partials of the reduction and the
+// device copy of outmass live in one file-scope device array instead of a
+// cudaMalloc'd buffer.  Nothing in it has to start at zero: every block
+// writes its partial before the finishing kernel reads it, and outmass is
+// copied in before the launch.  The array is shared by every call on the
+// device, so calls must not overlap (one host thread at a time per device).
+static __device__ __align__(256) unsigned char f3d_noalloc_scratch[F3D_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::atomic<void*> g_noalloc_ptr[kMaxDevices];
+
+// Address of the scratch array on the current device: looked up once per
+// device (the first call on a device does this set-up), then cached.
+int noalloc_scratch(void** out) {
+  int dev = -1;
+  F3D_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return set_error(F3D_ERR_ARG, "device ordinal %d out of range", dev);
+  void* p = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    F3D_CUDA(cudaGetSymbolAddress(&p, f3d_noalloc_scratch));
+    g_noalloc_ptr[dev].store(p, std::memory_order_release);
+  }
+  *out = p;
+  return F3D_OK;
+}
+
+int require_device(const void* p, const char* name) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(F3D_ERR_ARG, "%s: not a CUDA pointer", name);
+  }
+  if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+    return set_error(F3D_ERR_ARG, "%s must be device (or managed) memory", name);
+  return F3D_OK;
+}
+}  // namespace
+
+int f3d_cmass2d_noalloc(const double* c, const double* vx, const double* vy, const double* vz,
+                        const double* vset, const int* nx, const int* ny, const int* nz,
+                        const int* nc, const int* ic_loc, const int* nc_loc, const int* iz_loc,
+                        const int* nz_loc, const double* dx, const double* dy, const double* dz,
+                        const double* dt, double* outmass) {
+  if (int r = check_dims(*nx, *ny, *nz)) return r;
+  if (int r = check_zrange(*nz, *nz_loc, *iz_loc)) return r;
+  if (*ic_loc < 1 || *nc_loc < 0 || *ic_loc + *nc_loc - 1 > *nc)
+    return set_error(F3D_ERR_ARG, "class range outside 1..nc");
+  const void* arrs[] = {c, vx, vy, vz, vset, dz};
+  const char* names[] = {"c", "vx", "vy", "vz", "vset", "dz"};
+  for (int q = 0; q < 6; ++q)
+    if (int r = require_device(arrs[q], names[q])) return r;
+  const Dims d = dims(*nx, *ny, *nz);
+  const long long nterms = 2LL * *nc_loc * (*ny + *nx) * *nz_loc + (long long)*nc_loc * d.plane();
+  const size_t part = reduce_scratch_bytes(nterms, 1);
+  if (part + sizeof(double) > (size_t)F3D_NOALLOC_SCRATCH_BYTES)
+    return set_error(F3D_ERR_RANGE, "f3d_cmass2d_noalloc needs %zu scratch bytes, more than the %d available",
+                     part + sizeof(double), F3D_NOALLOC_SCRATCH_BYTES);
+  void* scratch = nullptr;
+  if (int r = noalloc_scratch(&scratch)) return r;
+  double* dout = reinterpret_cast<double*>(reinterpret_cast<char*>(scratch) + part);
+  F3D_CUDA(cudaMemcpy(dout, outmass, sizeof(double), cudaMemcpyDefault));
+  launch_cmass2d<double>(c, vx, vy, vz, vset, d, *ic_loc, *nc_loc, *iz_loc, *nz_loc, *dx, *dy, dz, *dt,
+                         scratch, dout, 0);
+  F3D_CUDA(cudaGetLastError());
+  F3D_CUDA(cudaMemcpy(outmass, dout, sizeof(double), cudaMemcpyDefault));
+  return F3D_OK;
+}
+
 int f3d_cmass3d(const double* c, const double* cload, const double* cdry, const double* cwet,
                 const int* nx, const int* ny, const int* nz, const int* nc, const double* dx,
                 const double* dy, const double* dz, double* massvol, double* massdep,

@@ -155,6 +155,39 @@ int f3d_cmass2d(const double* c, const double* vx, const double* vy,
                 const int* nz_loc, const double* dx, const double* dy,
                 const double* dz, const double* dt, double* outmass);
 
+/* f3d_cmass2d without any allocation.  No counterpart in the reference.
+ *
+ * f3d_cmass2d takes a cudaMalloc'd scratch buffer for the partial sums of
+ * its reduction on every call (and device copies of host arrays).  Some
+ * callers cannot allocate there: a program whose device memory is fully
+ * committed to resident scenarios (so a new cudaMalloc can fail), and one
+ * that keeps other streams busy and cannot accept the device-wide
+ * synchronisation that cudaFree implies.  This variant uses a fixed device
+ * array of F3D_NOALLOC_SCRATCH_BYTES bytes compiled into the library.
+ *
+ *  - every array argument must be device (or managed) memory; host arrays
+ *    are rejected with F3D_ERR_ARG.  outmass may be host or device memory
+ *    and is accumulated as in f3d_cmass2d (outmass = outmass + outflow).
+ *  - the scratch this call needs is at most 1024 block partials of 16
+ *    bytes plus padding and an 8-byte accumulator (16.7 KB) for any grid; a
+ *    call needing more than F3D_NOALLOC_SCRATCH_BYTES returns F3D_ERR_RANGE.
+ *  - nothing in the scratch has to start at zero: each call writes every
+ *    partial before reading it and copies outmass in first.
+ *  - the first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress with that device current) and caches it; make
+ *    that first call before any stream capture begins.
+ *  - the array is shared by all calls in the process on one device: calls
+ *    that overlap in time (from several host threads) race on it and give
+ *    wrong sums.  Serialise them.
+ *  - the call returns when the result is in outmass (legacy default stream). */
+#define F3D_NOALLOC_SCRATCH_BYTES 32768
+int f3d_cmass2d_noalloc(const double* c, const double* vx, const double* vy,
+                        const double* vz, const double* vset, const int* nx,
+                        const int* ny, const int* nz, const int* nc,
+                        const int* ic_loc, const int* nc_loc, const int* iz_loc,
+                        const int* nz_loc, const double* dx, const double* dy,
+                        const double* dz, const double* dt, double* outmass);
+
 /* Sources/cmass3d.f90:1 cmass3d(c,cload,cdry,cwet,nx,ny,nz,nc,dx,dy,dz,
  * massvol,massdep,massdry,masswet) */
 int f3d_cmass3d(const double* c, const double* cload, const double* cdry,
