@@ -27,7 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfall3d_gb300.so")
 
 PREC_FP64, PREC_FP32 = 64, 32
-OPT_FUSED, OPT_TILE = 1, 2
+OPT_FUSED, OPT_TILE, OPT_GRAPH = 1, 2, 3
 
 
 class F3DError(RuntimeError):
@@ -105,6 +105,19 @@ def load(build_if_missing: bool = False):
         "f3d_get_option": [VP, I, IP],
         "f3d_profile_enable": [VP, I],
         "f3d_profile_read": [VP, I, C.c_char_p, I, C.POINTER(C.c_longlong), DP, IP],
+        "f3d_batch_create": [I, C.POINTER(VP)],
+        "f3d_batch_destroy": [VP],
+        "f3d_batch_add": [VP, VP, VP, VP, D, D, I, VP, I, IP],
+        "f3d_batch_step": [VP, IP],
+        "f3d_batch_poll": [VP, I, IP, IP, IP],
+        "f3d_batch_release": [VP, I],
+        "f3d_batch_sync": [VP],
+        "f3d_batch_set_option": [VP, I, I],
+        "f3d_batch_get_option": [VP, I, IP],
+        "f3d_batch_autotune": [VP, I, IP, C.POINTER(C.c_float)],
+        "f3d_batch_stats": [VP, C.POINTER(C.c_longlong), DP, IP],
+        "f3d_batch_stream": [VP, C.POINTER(VP)],
+        "f3d_cmass2d_noalloc": [VP, VP, VP, VP, VP, IP, IP, IP, IP, IP, IP, IP, IP, DP, DP, VP, DP, DP],
     }
     for name, args in fine.items():
         f = getattr(lib, name)
@@ -467,3 +480,96 @@ class Context:
 
 def version() -> str:
     return load().f3d_version().decode()
+
+
+class Batch:
+    """The batched precision form (f3d_batch_*): the time loops of many
+    precision-form contexts advanced together, one persistent launch (one
+    CUDA graph replay) per batch step."""
+
+    DONE, RUNNING, FAILED = 2, 1, 3
+
+    def __init__(self, max_scenarios: int):
+        self.lib = load()
+        h = VP()
+        _check(self.lib.f3d_batch_create(int(max_scenarios), C.byref(h)))
+        self.h = h
+        self._keep = {}  # slot -> (ctx, met, src, log records): alive while in the batch
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.f3d_batch_destroy(self.h)
+            self.h = VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, ctx: "Context", beg_time=None, end_time=None, max_steps=0, log_cap=4096, met=None,
+            src=None) -> int:
+        met = met or _abi.make_met(ctx.s.met)
+        src = src or _abi.make_src(ctx.s.src)
+        recs = (_abi.F3DLogRecord * log_cap)()
+        slot = C.c_int()
+        _check(self.lib.f3d_batch_add(self.h, ctx.h, C.addressof(met.struct), C.addressof(src.struct),
+                                      ctx.s.beg_time if beg_time is None else float(beg_time),
+                                      ctx.s.end_time if end_time is None else float(end_time),
+                                      int(max_steps), C.addressof(recs), int(log_cap), C.byref(slot)))
+        self._keep[slot.value] = (ctx, met, src, recs)
+        return slot.value
+
+    def step(self) -> int:
+        n = C.c_int()
+        _check(self.lib.f3d_batch_step(self.h, C.byref(n)))
+        return n.value
+
+    def run(self) -> None:
+        """Steps until no scenario is running."""
+        while self.step() > 0:
+            pass
+
+    def poll(self, slot: int):
+        """(state, steps, log records so far)."""
+        st, steps, nlog = C.c_int(), C.c_int(), C.c_int()
+        _check(self.lib.f3d_batch_poll(self.h, int(slot), C.byref(st), C.byref(steps), C.byref(nlog)))
+        return st.value, steps.value, nlog.value
+
+    def log(self, slot: int):
+        _, _, nlog = self.poll(slot)
+        return _abi.log_array(self._keep[slot][3], nlog)
+
+    def release(self, slot: int):
+        _check(self.lib.f3d_batch_release(self.h, int(slot)))
+        self._keep.pop(slot, None)
+
+    def sync(self):
+        _check(self.lib.f3d_batch_sync(self.h))
+
+    def set_option(self, key: int, value: int):
+        _check(self.lib.f3d_batch_set_option(self.h, int(key), int(value)))
+
+    def get_option(self, key: int) -> int:
+        v = C.c_int()
+        _check(self.lib.f3d_batch_get_option(self.h, int(key), C.byref(v)))
+        return v.value
+
+    def autotune(self, reps: int = 3):
+        """Picks the fastest tile shape on the running scenarios; returns
+        (best shape, [ms per shape])."""
+        best = C.c_int()
+        ms = (C.c_float * 3)()
+        _check(self.lib.f3d_batch_autotune(self.h, int(reps), C.byref(best), ms))
+        return best.value, [float(v) for v in ms]
+
+    def stats(self):
+        """(batch steps, cell-class-steps, running scenarios)."""
+        bs, cc, n = C.c_longlong(), C.c_double(), C.c_int()
+        _check(self.lib.f3d_batch_stats(self.h, C.byref(bs), C.byref(cc), C.byref(n)))
+        return bs.value, cc.value, n.value
+
+    def stream_handle(self) -> int:
+        p = VP()
+        _check(self.lib.f3d_batch_stream(self.h, C.byref(p)))
+        return int(p.value or 0)

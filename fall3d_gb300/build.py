@@ -30,6 +30,7 @@ UNITS = {
     "f3d_fused.cu": ["--fmad=false"],
     "f3d_api.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
     "f3d_ctx.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
+    "f3d_batch.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
 }
 
 

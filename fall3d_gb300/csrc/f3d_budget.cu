@@ -85,72 +85,114 @@ size_t reduce_scratch_bytes(long long nterms, int nsums) {
 // Terms of Sources/cmass2d.f90:42-102: x faces (ic, j, k, left/right),
 // y faces (ic, i, k, down/up), top (ic, i, j).
 template <class T>
+__device__ __forceinline__ double cmass2d_term(long long t, const T* c, const double* vx,
+                                               const double* vy, const double* vz, const double* vset,
+                                               const Dims& d, int ic_loc, int iz_loc, int nz_loc,
+                                               double dx, double dy, const double* dz, double dt,
+                                               long long n1, long long n2) {
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const long long hb = d.halo(), s3 = d.cells();
+  double term;
+  if (t < n1) {
+    const int side = (int)(t & 1);
+    long long r = t >> 1;
+    const int k = (int)(r % nz_loc) + iz_loc;
+    r /= nz_loc;
+    const int j = (int)(r % ny) + 1;
+    const int ic = (int)(r / ny) + ic_loc;
+    double faty = 1.0;
+    if (j == 1 || j == ny) faty = 0.5;
+    const double area = faty * dy * 0.5 * (dz[k] + dz[k - 1]);
+    const T* cc = c + (long long)(ic - 1) * hb;
+    if (side == 0) {
+      const double velo = vx[d.M(1, j, k)], conc = (double)cc[d.C(0, j, k)];
+      term = -(dt * area * velo * conc);
+    } else {
+      const double velo = vx[d.M(nx, j, k)], conc = (double)cc[d.C(nx + 1, j, k)];
+      term = dt * area * velo * conc;
+    }
+  } else if (t < n1 + n2) {
+    const long long u = t - n1;
+    const int side = (int)(u & 1);
+    long long r = u >> 1;
+    const int k = (int)(r % nz_loc) + iz_loc;
+    r /= nz_loc;
+    const int i = (int)(r % nx) + 1;
+    const int ic = (int)(r / nx) + ic_loc;
+    double fatx = 1.0;
+    if (i == 1 || i == nx) fatx = 0.5;
+    const double area = fatx * dx * 0.5 * (dz[k] + dz[k - 1]);
+    const T* cc = c + (long long)(ic - 1) * hb;
+    if (side == 0) {
+      const double velo = vy[d.M(i, 1, k)], conc = (double)cc[d.C(i, 0, k)];
+      term = -(dt * area * velo * conc);
+    } else {
+      const double velo = vy[d.M(i, ny, k)], conc = (double)cc[d.C(i, ny + 1, k)];
+      term = dt * area * velo * conc;
+    }
+  } else {
+    long long r = t - n1 - n2;
+    const int i = (int)(r % nx) + 1;
+    r /= nx;
+    const int j = (int)(r % ny) + 1;
+    const int ic = (int)(r / ny) + ic_loc;
+    double faty = 1.0;
+    if (j == 1 || j == ny) faty = 0.5;
+    double fatx = 1.0;
+    if (i == 1 || i == nx) fatx = 0.5;
+    const double area = fatx * faty * dx * dy;
+    const double velo = vz[d.M(i, j, nz)] + vset[(long long)(ic - 1) * s3 + d.M(i, j, nz)];
+    const double conc = (double)c[(long long)(ic - 1) * hb + d.C(i, j, nz + 1)];
+    term = dt * area * velo * conc;
+  }
+  return term;
+}
+
+template <class T>
 __global__ void k_cmass2d(const T* c, const double* vx, const double* vy, const double* vz,
                           const double* vset, Dims d, int ic_loc, int nc_loc, int iz_loc,
                           int nz_loc, double dx, double dy, const double* dz, double dt,
                           long long n1, long long n2, long long n3, DD* partial) {
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
-  const long long hb = d.halo(), s3 = d.cells();
   DD acc[1] = {dd_zero()};
   const long long ntot = n1 + n2 + n3;
   for (long long t = blockIdx.x * (long long)RB + threadIdx.x; t < ntot;
-       t += (long long)gridDim.x * RB) {
-    double term;
-    if (t < n1) {
-      const int side = (int)(t & 1);
-      long long r = t >> 1;
-      const int k = (int)(r % nz_loc) + iz_loc;
-      r /= nz_loc;
-      const int j = (int)(r % ny) + 1;
-      const int ic = (int)(r / ny) + ic_loc;
-      double faty = 1.0;
-      if (j == 1 || j == ny) faty = 0.5;
-      const double area = faty * dy * 0.5 * (dz[k] + dz[k - 1]);
-      const T* cc = c + (long long)(ic - 1) * hb;
-      if (side == 0) {
-        const double velo = vx[d.M(1, j, k)], conc = (double)cc[d.C(0, j, k)];
-        term = -(dt * area * velo * conc);
-      } else {
-        const double velo = vx[d.M(nx, j, k)], conc = (double)cc[d.C(nx + 1, j, k)];
-        term = dt * area * velo * conc;
-      }
-    } else if (t < n1 + n2) {
-      const long long u = t - n1;
-      const int side = (int)(u & 1);
-      long long r = u >> 1;
-      const int k = (int)(r % nz_loc) + iz_loc;
-      r /= nz_loc;
-      const int i = (int)(r % nx) + 1;
-      const int ic = (int)(r / nx) + ic_loc;
-      double fatx = 1.0;
-      if (i == 1 || i == nx) fatx = 0.5;
-      const double area = fatx * dx * 0.5 * (dz[k] + dz[k - 1]);
-      const T* cc = c + (long long)(ic - 1) * hb;
-      if (side == 0) {
-        const double velo = vy[d.M(i, 1, k)], conc = (double)cc[d.C(i, 0, k)];
-        term = -(dt * area * velo * conc);
-      } else {
-        const double velo = vy[d.M(i, ny, k)], conc = (double)cc[d.C(i, ny + 1, k)];
-        term = dt * area * velo * conc;
-      }
-    } else {
-      long long r = t - n1 - n2;
-      const int i = (int)(r % nx) + 1;
-      r /= nx;
-      const int j = (int)(r % ny) + 1;
-      const int ic = (int)(r / ny) + ic_loc;
-      double faty = 1.0;
-      if (j == 1 || j == ny) faty = 0.5;
-      double fatx = 1.0;
-      if (i == 1 || i == nx) fatx = 0.5;
-      const double area = fatx * faty * dx * dy;
-      const double velo = vz[d.M(i, j, nz)] + vset[(long long)(ic - 1) * s3 + d.M(i, j, nz)];
-      const double conc = (double)c[(long long)(ic - 1) * hb + d.C(i, j, nz + 1)];
-      term = dt * area * velo * conc;
-    }
-    acc[0] = dd_add_d(acc[0], term);
-  }
+       t += (long long)gridDim.x * RB)
+    acc[0] = dd_add_d(acc[0], cmass2d_term<T>(t, c, vx, vy, vz, vset, d, ic_loc, iz_loc, nz_loc, dx, dy,
+                                              dz, dt, n1, n2));
   block_store_dd<1>(acc, partial);
+}
+
+// Batched form: scenario blockIdx.y, its outflow summed over gridDim.x
+// blocks; the step's result is in the buffer the fused kernel wrote
+// (bstep even: c_b, odd: c_a).
+__global__ void k_cmass2d_batch(const BatchAux* tab, const int* bstep, DD* partial) {
+  const BatchAux& b = tab[blockIdx.y];
+  const float* c = (bstep[blockIdx.y] & 1) ? b.c_a : b.c_b;
+  DD acc[1] = {dd_zero()};
+  const long long ntot = b.n1 + b.n2 + b.n3;
+  for (long long t = blockIdx.x * (long long)RB + threadIdx.x; t < ntot;
+       t += (long long)gridDim.x * RB)
+    acc[0] = dd_add_d(acc[0], cmass2d_term<float>(t, c, b.vx, b.vy, b.vz, b.vset, b.d, 1, 1, b.d.nz, b.dX1,
+                                                  b.dX2, b.dz, b.dt, b.n1, b.n2));
+  block_store_dd<1>(acc, partial + (long long)blockIdx.y * gridDim.x);
+}
+
+// outmass = outmass + sum (cmass2d.f90:104), one block per scenario
+__global__ void k_cmass2d_batch_finish(const BatchAux* tab, const DD* partial, int nblk) {
+  const DD* p = partial + (long long)blockIdx.x * nblk;
+  DD v[1] = {dd_zero()};
+  for (int b = threadIdx.x; b < nblk; b += RB) v[0] = dd_add(v[0], p[b]);
+  __shared__ DD sh[RB / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int off = 16; off > 0; off >>= 1) v[0] = dd_add(v[0], dd_shfl_down(v[0], off));
+  if (lane == 0) sh[wid] = v[0];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DD a = sh[0];
+    for (int w = 1; w < RB / 32; ++w) a = dd_add(a, sh[w]);
+    double* out = tab[blockIdx.x].outmass;
+    *out = *out + a.hi;
+  }
 }
 
 template <class T>
@@ -329,6 +371,17 @@ void launch_outputs(const T* c, const double* cload, Dims d, int np, const doubl
   k_outputs<T><<<(unsigned)((pl + 127) / 128), 128, 0, s>>>(c, cload, d, np, dz, Hm1, load, col_mass,
                                                            c_grnd);
   count_launch();
+}
+
+size_t cmass2d_batch_scratch_bytes(int nscen) { return sizeof(DD) * (size_t)nscen * 64 + 256; }
+
+void launch_cmass2d_batch(const BatchAux* tab, const int* bstep, int nscen, void* scratch,
+                          cudaStream_t s) {
+  if (nscen <= 0) return;
+  DD* partial = reinterpret_cast<DD*>(scratch);
+  k_cmass2d_batch<<<dim3(64, nscen), RB, 0, s>>>(tab, bstep, partial);
+  k_cmass2d_batch_finish<<<nscen, RB, 0, s>>>(tab, partial, 64);
+  count_launch(2);
 }
 
 template void launch_cmass2d<double>(const double*, const double*, const double*, const double*,

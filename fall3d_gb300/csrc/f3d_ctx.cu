@@ -15,75 +15,13 @@
 #include <string>
 #include <vector>
 
-#include "../../include/fall3d_gpu.h"
-#include "f3d_internal.h"
-#include "f3d_fused.h"
+#include "f3d_ctx_impl.h"
 
 namespace f3d {
 int ctx_error(int code, const char* msg);
 }
 using namespace f3d;
 
-struct f3d_ctx {
-  f3d_grid g{};
-  Dims d{};
-  int prec = 64;
-  cudaStream_t stream = nullptr;
-  std::vector<void*> allocs;
-  // static
-  double *dz = nullptr, *zlayer = nullptr, *Hm1 = nullptr, *topg = nullptr;
-  double *diam = nullptr, *rhop = nullptr, *psi = nullptr, *sphe = nullptr;
-  // met and coefficients (binary64)
-  double *vx = nullptr, *vy = nullptr, *vz = nullptr, *tempe = nullptr, *vptemp = nullptr;
-  double *rho = nullptr, *rkhor = nullptr, *rkh1 = nullptr, *rkver = nullptr, *divu = nullptr;
-  double *vset = nullptr, *vdep = nullptr;
-  double *ustar = nullptr, *zi = nullptr, *rl = nullptr, *znt = nullptr, *prate = nullptr,
-         *ldu = nullptr;
-  int* iters = nullptr;
-  // state
-  double* c64 = nullptr;
-  float* c32 = nullptr;
-  double *cdry = nullptr, *cwet = nullptr, *cload = nullptr;
-  // FP32 copies
-  float *vx32 = nullptr, *vy32 = nullptr, *vz32 = nullptr, *rho32 = nullptr, *rkhor32 = nullptr,
-        *rkh132 = nullptr, *rkver32 = nullptr, *vset32 = nullptr, *vdep32 = nullptr,
-        *dz32 = nullptr;
-  // fused FP32 step: second concentration buffer, 1/rho, K*rho products,
-  // per-column wet rate, per-class wet-deposition switch
-  float* c32b = nullptr;
-  float *lrho32 = nullptr, *pkx32 = nullptr, *pky32 = nullptr, *pkz32 = nullptr;
-  float* vk32 = nullptr;  // vz + vset per class
-  double* lambda2d = nullptr;
-  unsigned char* wet_class = nullptr;
-  int opt_fused = 1, opt_tile = 0;
-  // the fused kernel applies: zlayer non-decreasing, 32-bit offsets in a class
-  int fused_ok = 1;
-  // sources
-  int *isrc = nullptr, *jsrc = nullptr, *ksrc = nullptr;
-  double* tmrat = nullptr;
-  int src_cap = 0, nsou = 0;
-  // scratch
-  void* red_scratch = nullptr;
-  void* vset_scratch = nullptr;
-  double* small = nullptr;  // [0] outmass, [1..4] budget, [8] cd, [16] dtcn bits, [24] status
-  // host scalars of the time loop
-  double time = 0.0, dt = 1.0, dtc = 0.0, erumass = 0.0, flowrate = 0.0;
-  int iiter = 0, have_met = 0;
-  // f3d_run loop state (Fall3d.f90:73-78)
-  int run_started = 0, meteotime = 1, sourcetime = 1;
-  double meteo_time = 0.0, source_time = 0.0;
-  // per-kernel event profiler (f3d_profile_*)
-  int prof = 0;
-  struct ProfRec {
-    int kind;
-    cudaEvent_t a, b;
-  };
-  std::vector<ProfRec> prof_pending;
-  std::vector<cudaEvent_t> prof_pool;
-  std::vector<std::string> prof_names;
-  std::vector<long long> prof_count;
-  std::vector<double> prof_ms;
-};
 
 namespace {
 
@@ -319,14 +257,32 @@ void sizloop(f3d_ctx* x) {
 void sizloop_fused(f3d_ctx* x) {
   const Dims d = x->d;
   const int nc = x->g.nc;
-  const long long hb = d.halo(), s3 = d.cells(), pl = d.plane();
   cudaStream_t s = x->stream;
+  const FusedArgs a = f3d::ctx_fused_args(x);
+  {
+    ProfScope ps(x, "step_fused");
+    launch_step_fused(a, x->opt_tile, s);
+  }
+  std::swap(x->c32, x->c32b);
+  {
+    ProfScope ps(x, "cmass2d");
+    launch_cmass2d<float>(x->c32, x->vx, x->vy, x->vz, x->vset, d, 1, nc, 1, d.nz, x->g.dX1,
+                          x->g.dX2, x->dz, x->dt, x->red_scratch, small_outmass(x), s);
+  }
+}
+
+}  // namespace
+
+namespace f3d {
+FusedArgs ctx_fused_args(f3d_ctx* x) {
+  const Dims d = x->d;
+  const long long hb = d.halo(), s3 = d.cells(), pl = d.plane();
   FusedArgs a{};
   a.c_in = x->c32;
   a.c_out = x->c32b;
   a.cstride = hb;
   a.d = d;
-  a.ncls = nc;
+  a.ncls = x->g.nc;
   a.xfirst = (x->iiter % 2 == 0) ? 1 : 0;
   a.dt = (float)x->dt;
   a.dt64 = x->dt;
@@ -358,19 +314,9 @@ void sizloop_fused(f3d_ctx* x) {
   a.cdry = x->cdry;
   a.vset64 = x->vset;
   a.vdep64 = x->vdep;
-  {
-    ProfScope ps(x, "step_fused");
-    launch_step_fused(a, x->opt_tile, s);
-  }
-  std::swap(x->c32, x->c32b);
-  {
-    ProfScope ps(x, "cmass2d");
-    launch_cmass2d<float>(x->c32, x->vx, x->vy, x->vz, x->vset, d, 1, nc, 1, d.nz, x->g.dX1,
-                          x->g.dX2, x->dz, x->dt, x->red_scratch, small_outmass(x), s);
-  }
+  return a;
 }
-
-}  // namespace
+}  // namespace f3d
 
 namespace f3d {
 int ctx_error(int code, const char* msg);
@@ -678,10 +624,7 @@ int f3d_source(f3d_ctx* x, int nsou, const int* isrc, const int* jsrc, const int
 int f3d_step(f3d_ctx* x) {
   if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
   if (!x->have_met) return f3d::ctx_error(F3D_ERR_STATE, "f3d_step before f3d_meteo");
-  // Fall3d.f90:112-114
-  x->time = x->time + x->dt;
-  x->iiter = x->iiter + 1;
-  x->erumass = x->erumass + x->flowrate * x->dt;
+  f3d::ctx_advance(x);
   const Dims d = x->d;
   // setsrc.f90:20-35
   if (x->prof) prof_drain(x);  // bounded event backlog: resolve the previous step
@@ -932,14 +875,105 @@ int f3d_run_reset(f3d_ctx* x) {
   return F3D_OK;
 }
 
-// Sources/Fall3d.f90:73-121 with the interval selection of
+}  // extern "C"
+
+namespace f3d {
+// Sources/Fall3d.f90:83-101 with the interval selection of
 // libMaster/get_dbs_value_plane.f90:100-114 and get_source_nsrc.f90:41-59.
+int ctx_run_prepare(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, double end_time) {
+  const size_t s3 = (size_t)x->d.cells(), pl = (size_t)x->d.plane();
+  const int nc = x->g.nc;
+  if (x->source_time <= x->time) {
+    if (x->sourcetime) {
+      const int ts = (int)x->time;
+      int found = -1;
+      size_t off = 0, off_found = 0, roff = 0, roff_found = 0;
+      for (int it = 0; it < src->nint; ++it) {
+        if (found < 0 && ts >= src->t1[it] && ts < src->t2[it]) {
+          found = it;
+          off_found = off;
+          roff_found = roff;
+        }
+        off += (size_t)src->nsou[it];
+        roff += (size_t)src->nsou[it] * nc;
+      }
+      if (found < 0) {
+        char m[128];
+        snprintf(m, sizeof m, "get_source_nsrc: no source interval at time %d", ts);
+        return f3d::ctx_error(F3D_ERR_RANGE, m);
+      }
+      const int rc = f3d_source(x, src->nsou[found], src->isrc + off_found, src->jsrc + off_found,
+                                src->ksrc + off_found, src->tmrat + roff_found);
+      if (rc) return rc;
+      x->source_time = (double)src->t2[found];
+    }
+    if (x->source_time >= end_time) x->sourcetime = 0;
+  }
+  if (x->meteo_time <= x->time) {
+    if (x->meteotime) {
+      const int ts = (int)(met->time_lag + x->time);
+      const int nt = met->nt;
+      if (ts < met->times[0] || ts > met->times[nt - 1]) {
+        char m[128];
+        snprintf(m, sizeof m, "get_dbs_value_plane: time %d outside the DBS interval", ts);
+        return f3d::ctx_error(F3D_ERR_RANGE, m);
+      }
+      int itime = nt - 1, endsec = met->times[nt - 1];
+      for (int it = 0; it < nt - 1; ++it)
+        if (ts >= met->times[it] && ts < met->times[it + 1]) {
+          itime = it;
+          endsec = met->times[it + 1];
+        }
+      const size_t o3 = (size_t)itime * s3, o2 = (size_t)itime * pl;
+      const int rc = f3d_meteo(x, met->u + o3, met->v + o3, met->w + o3, met->t + o3, met->tp + o3,
+                               met->rho + o3, met->ust + o2, met->pblh + o2, met->rmol + o2,
+                               met->znt + o2, met->prate ? met->prate + o2 : nullptr, met->ldu);
+      if (rc) return rc;
+      x->meteo_time = (double)endsec - met->time_lag;
+    }
+    if (x->meteo_time >= end_time) x->meteotime = 0;
+  }
+  return F3D_OK;
+}
+
+void ctx_advance(f3d_ctx* x) {  // Fall3d.f90:112-114
+  x->time = x->time + x->dt;
+  x->iiter = x->iiter + 1;
+  x->erumass = x->erumass + x->flowrate * x->dt;
+}
+
+int ctx_log(f3d_ctx* x, f3d_log_record* log, int log_cap, int* nlog) {
+  // endstep.f90:51: mass budget every 10 minutes of simulated time
+  if (x->iiter == 1 || std::fmod(x->time, 600.0) <= x->dt) {
+    if (log && nlog && *nlog < log_cap) {
+      double b[4];
+      int r2 = f3d_budget(x, &b[0], &b[1], &b[2], &b[3]);
+      if (r2) return r2;
+      f3d_log_record& r = log[(*nlog)++];
+      r.iiter = x->iiter;
+      r.time = x->time;
+      r.dt = x->dt;
+      r.dtc = x->dtc;
+      r.massvol = b[0];
+      r.massdep = b[1];
+      r.massdry = b[2];
+      r.masswet = b[3];
+      r2 = f3d_get_state(x, nullptr, nullptr, nullptr, nullptr, nullptr, &r.outmass, nullptr);
+      if (r2) return r2;
+      r.erumass = x->erumass;
+    }
+  }
+  return F3D_OK;
+}
+}  // namespace f3d
+
+extern "C" {
+
+// Sources/Fall3d.f90:73-121.
 int f3d_run(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, double beg_time,
             double end_time, int max_steps, f3d_log_record* log, int log_cap, int* nlog) {
   if (!x || !met || !src) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
   if (met->nt < 1) return f3d::ctx_error(F3D_ERR_ARG, "no meteorological snapshot");
-  const size_t s3 = (size_t)x->d.cells(), pl = (size_t)x->d.plane();
-  const int nc = x->g.nc;
   if (nlog) *nlog = 0;
   bool go_on = true;  // the reference's do-while runs at least one step
   if (!x->run_started) {
@@ -955,79 +989,11 @@ int f3d_run(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, do
   }
   int steps = 0;
   while (go_on) {
-    if (x->source_time <= x->time) {
-      if (x->sourcetime) {
-        const int ts = (int)x->time;
-        int found = -1;
-        size_t off = 0, off_found = 0, roff = 0, roff_found = 0;
-        for (int it = 0; it < src->nint; ++it) {
-          if (found < 0 && ts >= src->t1[it] && ts < src->t2[it]) {
-            found = it;
-            off_found = off;
-            roff_found = roff;
-          }
-          off += (size_t)src->nsou[it];
-          roff += (size_t)src->nsou[it] * nc;
-        }
-        if (found < 0) {
-          char m[128];
-          snprintf(m, sizeof m, "get_source_nsrc: no source interval at time %d", ts);
-          return f3d::ctx_error(F3D_ERR_RANGE, m);
-        }
-        const int rc = f3d_source(x, src->nsou[found], src->isrc + off_found, src->jsrc + off_found,
-                                  src->ksrc + off_found, src->tmrat + roff_found);
-        if (rc) return rc;
-        x->source_time = (double)src->t2[found];
-      }
-      if (x->source_time >= end_time) x->sourcetime = 0;
-    }
-    if (x->meteo_time <= x->time) {
-      if (x->meteotime) {
-        const int ts = (int)(met->time_lag + x->time);
-        const int nt = met->nt;
-        if (ts < met->times[0] || ts > met->times[nt - 1]) {
-          char m[128];
-          snprintf(m, sizeof m, "get_dbs_value_plane: time %d outside the DBS interval", ts);
-          return f3d::ctx_error(F3D_ERR_RANGE, m);
-        }
-        int itime = nt - 1, endsec = met->times[nt - 1];
-        for (int it = 0; it < nt - 1; ++it)
-          if (ts >= met->times[it] && ts < met->times[it + 1]) {
-            itime = it;
-            endsec = met->times[it + 1];
-          }
-        const size_t o3 = (size_t)itime * s3, o2 = (size_t)itime * pl;
-        const int rc = f3d_meteo(x, met->u + o3, met->v + o3, met->w + o3, met->t + o3, met->tp + o3,
-                                 met->rho + o3, met->ust + o2, met->pblh + o2, met->rmol + o2,
-                                 met->znt + o2, met->prate ? met->prate + o2 : nullptr, met->ldu);
-        if (rc) return rc;
-        x->meteo_time = (double)endsec - met->time_lag;
-      }
-      if (x->meteo_time >= end_time) x->meteotime = 0;
-    }
+    if (int rc = f3d::ctx_run_prepare(x, met, src, end_time)) return rc;
     const int rc = f3d_step(x);
     if (rc) return rc;
     ++steps;
-    // endstep.f90:51: mass budget every 10 minutes of simulated time
-    if (x->iiter == 1 || std::fmod(x->time, 600.0) <= x->dt) {
-      if (log && nlog && *nlog < log_cap) {
-        double b[4];
-        int r2 = f3d_budget(x, &b[0], &b[1], &b[2], &b[3]);
-        if (r2) return r2;
-        f3d_log_record& r = log[(*nlog)++];
-        r.iiter = x->iiter;
-        r.time = x->time;
-        r.dt = x->dt;
-        r.dtc = x->dtc;
-        r.massvol = b[0];
-        r.massdep = b[1];
-        r.massdry = b[2];
-        r.masswet = b[3];
-        r2 = f3d_get_state(x, nullptr, nullptr, nullptr, nullptr, nullptr, &r.outmass, nullptr);
-        if (r2) return r2;
-        r.erumass = x->erumass;
-      }
-    }
+    if (int r2 = f3d::ctx_log(x, log, log_cap, nlog)) return r2;
     if (x->time >= end_time) go_on = false;
     if (max_steps > 0 && steps >= max_steps) go_on = false;
   }

@@ -1,0 +1,85 @@
+// f3d_ctx_impl.h -- the context object behind the coarse C ABI (shared by
+// the single-scenario API in f3d_ctx.cu and the batched form in f3d_batch.cu).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../../include/fall3d_gpu.h"
+#include "f3d_internal.h"
+#include "f3d_fused.h"
+
+struct f3d_ctx {
+  f3d_grid g{};
+  Dims d{};
+  int prec = 64;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  // static
+  double *dz = nullptr, *zlayer = nullptr, *Hm1 = nullptr, *topg = nullptr;
+  double *diam = nullptr, *rhop = nullptr, *psi = nullptr, *sphe = nullptr;
+  // met and coefficients (binary64)
+  double *vx = nullptr, *vy = nullptr, *vz = nullptr, *tempe = nullptr, *vptemp = nullptr;
+  double *rho = nullptr, *rkhor = nullptr, *rkh1 = nullptr, *rkver = nullptr, *divu = nullptr;
+  double *vset = nullptr, *vdep = nullptr;
+  double *ustar = nullptr, *zi = nullptr, *rl = nullptr, *znt = nullptr, *prate = nullptr,
+         *ldu = nullptr;
+  int* iters = nullptr;
+  // state
+  double* c64 = nullptr;
+  float* c32 = nullptr;
+  double *cdry = nullptr, *cwet = nullptr, *cload = nullptr;
+  // FP32 copies
+  float *vx32 = nullptr, *vy32 = nullptr, *vz32 = nullptr, *rho32 = nullptr, *rkhor32 = nullptr,
+        *rkh132 = nullptr, *rkver32 = nullptr, *vset32 = nullptr, *vdep32 = nullptr,
+        *dz32 = nullptr;
+  // fused FP32 step: second concentration buffer, 1/rho, K*rho products,
+  // per-column wet rate, per-class wet-deposition switch
+  float* c32b = nullptr;
+  float *lrho32 = nullptr, *pkx32 = nullptr, *pky32 = nullptr, *pkz32 = nullptr;
+  float* vk32 = nullptr;  // vz + vset per class
+  double* lambda2d = nullptr;
+  unsigned char* wet_class = nullptr;
+  int opt_fused = 1, opt_tile = 0;
+  // the fused kernel applies: zlayer non-decreasing, 32-bit offsets in a class
+  int fused_ok = 1;
+  // sources
+  int *isrc = nullptr, *jsrc = nullptr, *ksrc = nullptr;
+  double* tmrat = nullptr;
+  int src_cap = 0, nsou = 0;
+  // scratch
+  void* red_scratch = nullptr;
+  void* vset_scratch = nullptr;
+  double* small = nullptr;  // [0] outmass, [1..4] budget, [8] cd, [16] dtcn bits, [24] status
+  // host scalars of the time loop
+  double time = 0.0, dt = 1.0, dtc = 0.0, erumass = 0.0, flowrate = 0.0;
+  int iiter = 0, have_met = 0;
+  // f3d_run loop state (Fall3d.f90:73-78)
+  int run_started = 0, meteotime = 1, sourcetime = 1;
+  double meteo_time = 0.0, source_time = 0.0;
+  // per-kernel event profiler (f3d_profile_*)
+  int prof = 0;
+  struct ProfRec {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<ProfRec> prof_pending;
+  std::vector<cudaEvent_t> prof_pool;
+  std::vector<std::string> prof_names;
+  std::vector<long long> prof_count;
+  std::vector<double> prof_ms;
+};
+
+namespace f3d {
+int ctx_error(int code, const char* msg);
+// Pieces of the time loop (Fall3d.f90:79-121) shared with the batched form.
+// Source and meteo updates due at x->time (Fall3d.f90:83-101).
+int ctx_run_prepare(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, double end_time);
+// time = time + dt, iiter = iiter + 1, erumass (Fall3d.f90:112-114)
+void ctx_advance(f3d_ctx* x);
+// the mass-budget log of endstep.f90:51 when due
+int ctx_log(f3d_ctx* x, f3d_log_record* log, int log_cap, int* nlog);
+// arguments of the fused precision-form step for the context's state
+FusedArgs ctx_fused_args(f3d_ctx* x);
+inline double* ctx_outmass(f3d_ctx* x) { return x->small; }
+}  // namespace f3d

@@ -136,11 +136,15 @@ enum : int { F_C = 0, F_VK, F_VX, F_VY, F_L, F_PZ, F_L1, F_PX, F_PY, NF };
 using False_ = std::integral_constant<bool, false>;
 using True_ = std::integral_constant<bool, true>;
 
+// One tile of one class: the whole march.  c_in / c_out are the class
+// blocks' base (all classes); commit = 0 skips the deposit writes (cdry, cwet)
+// so that the autotuner can time the kernel on a live state.
 template <int HY, int NW>
-__global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fused(const FusedArgs a) {
+__device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in, float* c_out,
+                                           const int xfirst, const int commit, const int cls,
+                                           const int tile, unsigned char* smem_raw) {
   constexpr int HX = 32, NT = 32 * NW, RPW = HY / NW, TX = HX - 6, TY = HY - 6, NP = HX * HY;
   static_assert(HY % NW == 0, "rows must divide among warps");
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   // a guard row on either side keeps the +-1 row reads of halo rows in bounds
   float* stage = reinterpret_cast<float*>(smem_raw) + HX;  // [2][NF][NP]
   float* P0s = stage + 2 * NF * NP;                          // y-sweep planes
@@ -154,8 +158,6 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
 
   const Dims d = a.d;
   const int nx = d.nx, ny = d.ny, nz = d.nz;
-  const int cls = blockIdx.x % a.ncls;
-  const int tile = blockIdx.x / a.ncls;
   const int tiles_x = (nx + TX - 1) / TX;
   const int i0 = 1 + (tile % tiles_x) * TX, j0 = 1 + (tile / tiles_x) * TY;
   const int gx0 = i0 - 3, gy0 = j0 - 3;
@@ -197,8 +199,8 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
     wkz[o] = kz;
   }
 
-  const float* __restrict__ cin = a.c_in + (long long)cls * a.cstride;
-  float* __restrict__ cout = a.c_out + (long long)cls * a.cstride;
+  const float* __restrict__ cin = c_in + (long long)cls * a.cstride;
+  float* __restrict__ cout = c_out + (long long)cls * a.cstride;
   const float* __restrict__ vkc = a.vk + (long long)cls * a.vstride;
   const float dt = a.dt;
   const float dznz = 1.0f / a.dz[nz];
@@ -424,7 +426,7 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
         }
       };
       float sa[RPW];
-      if (a.xfirst) {  // sizloop.f90:42-48
+      if (xfirst) {  // sizloop.f90:42-48
         adv_x(s1, sa);
         adv_y(sa, s2);
       } else {
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
       }
     };
     float s3a[RPW], s4[RPW];
-    if (a.xfirst) {  // sizloop.f90:55-61
+    if (xfirst) {  // sizloop.f90:55-61
       dif_x(s3, s3a);
       dif_y(s3a, s4);
     } else {
@@ -572,7 +574,7 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
           cnew = (float)((double)cnew * (1.0 - wlam[o]));
         }
       }
-      if (!STEADY && k == 1) {  // accum (accum.f90:17-25), binary64
+      if (!STEADY && k == 1 && commit) {  // accum (accum.f90:17-25), binary64
         const int mb = mb0 + NW * r * nx;
         double* cd = a.cdry + (long long)(cls + 1) * pl + mb;
         const double vsd = a.vset64[(long long)cls * a.vstride + mb] + a.vdep64[(long long)cls * pl + mb];
@@ -592,7 +594,7 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
   else
     march(False_{});
 
-  if (wet) {
+  if (wet && commit) {
     __syncthreads();
     for (int o = threadIdx.x; o < TX * TY; o += NT) {
       const int oi = i0 + o % TX, oj = j0 + o / TX;
@@ -602,10 +604,81 @@ __global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fuse
   }
 }
 
+template <int HY, int NW>
+__global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2)) k_step_fused(const FusedArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  fused_tile<HY, NW>(a, a.c_in, a.c_out, a.xfirst, 1, (int)(blockIdx.x % a.ncls), (int)(blockIdx.x / a.ncls),
+                     smem_raw);
+}
+
+// ------------------------------------------------------------ batched form
+// The step of every scenario of a batch in one persistent launch: the work
+// items are (scenario, tile, class), numbered scenario by scenario
+// (item_off[s] .. item_off[s+1]-1, class fastest); each CTA takes the next
+// item from a counter until none is left.  A scenario's arguments live in
+// constant memory; its buffers alternate with the number of batch steps it
+// has taken (bstep[s] even: c_in -> c_out, odd: c_out -> c_in), and the x/y
+// order follows iiter = iiter0[s] + bstep[s] + 1 (sizloop.f90:42-48).
+__constant__ FusedArgs c_batch[F3D_BATCH_MAX];
+static_assert(sizeof(FusedArgs) * F3D_BATCH_MAX <= 48 * 1024, "batch argument table exceeds constant memory");
+
+template <int HY, int NW>
+__global__ void __launch_bounds__(32 * NW, (32 * NW >= 512 ? 1 : 2))
+    k_step_fused_batch(const int* __restrict__ item_off, int nscen, int* counter,
+                       const int* __restrict__ bstep, const int* __restrict__ iiter0, int commit) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  const int total = item_off[nscen];
+  for (;;) {
+    __syncthreads();  // the previous item is done with shared memory
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= total) break;
+    int lo = 0, hi = nscen;  // item_off[lo] <= item < item_off[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (item_off[mid] <= item) lo = mid;
+      else hi = mid;
+    }
+    const FusedArgs& a = c_batch[lo];
+    const int local = item - item_off[lo];
+    const int bs = bstep[lo];
+    const float* cin = (bs & 1) ? a.c_out : a.c_in;
+    float* cout = (bs & 1) ? const_cast<float*>(a.c_in) : a.c_out;
+    const int iiter = iiter0[lo] + bs + 1;
+    fused_tile<HY, NW>(a, cin, cout, (iiter % 2 == 0) ? 1 : 0, commit, local % a.ncls, local / a.ncls, smem_raw);
+  }
+}
+
 template <int HY>
 size_t fused_smem(int nz) {
   return sizeof(float) * ((2 * NF + 4) * 32 * HY + 2 * 32) +
          (2 * sizeof(double) + sizeof(int)) * 26 * (HY - 6) + sizeof(ZT32) * (size_t)(nz + 1);
+}
+
+// persistent grid: as many CTAs as fit on the device at once
+template <int HY, int NW>
+int fused_batch_grid_t(int max_nz) {
+  const size_t sm = fused_smem<HY>(max_nz);
+  if (cudaFuncSetAttribute(k_step_fused_batch<HY, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+      cudaSuccess)
+    return -1;
+  int per_sm = 0, nsm = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_fused_batch<HY, NW>, 32 * NW, sm) !=
+          cudaSuccess)
+    return -1;
+  return per_sm < 1 ? -1 : per_sm * nsm;
+}
+
+template <int HY, int NW>
+void launch_fused_batch_t(int grid, const int* item_off, int nscen, int* counter, const int* bstep,
+                          const int* iiter0, int commit, int max_nz, cudaStream_t s) {
+  k_step_fused_batch<HY, NW><<<grid, 32 * NW, fused_smem<HY>(max_nz), s>>>(item_off, nscen, counter, bstep,
+                                                                            iiter0, commit);
+  count_launch();
 }
 
 template <int HY, int NW>
@@ -620,6 +693,45 @@ void launch_fused_t(const FusedArgs& a, cudaStream_t s) {
 }
 
 }  // namespace
+
+int fused_tiles(int nx, int ny, int shape) {
+  const int TY = (shape == 1 ? 64 : 32) - 6;
+  return ((nx + 25) / 26) * ((ny + TY - 1) / TY);
+}
+
+int upload_batch_args(const FusedArgs* h, int n, cudaStream_t s) {
+  if (n > F3D_BATCH_MAX) return 1;
+  return cudaMemcpyToSymbolAsync(c_batch, h, sizeof(FusedArgs) * (size_t)n, 0, cudaMemcpyHostToDevice, s) ==
+                 cudaSuccess
+             ? 0
+             : 1;
+}
+
+int fused_batch_grid(int shape, int max_nz) {
+  switch (shape) {
+    case 1:
+      return fused_batch_grid_t<64, 16>(max_nz);
+    case 2:
+      return fused_batch_grid_t<32, 16>(max_nz);
+    default:
+      return fused_batch_grid_t<32, 8>(max_nz);
+  }
+}
+
+void launch_step_fused_batch(int shape, int grid, const int* item_off, int nscen, int* counter,
+                             const int* bstep, const int* iiter0, int commit, int max_nz, cudaStream_t s) {
+  switch (shape) {
+    case 1:
+      launch_fused_batch_t<64, 16>(grid, item_off, nscen, counter, bstep, iiter0, commit, max_nz, s);
+      break;
+    case 2:
+      launch_fused_batch_t<32, 16>(grid, item_off, nscen, counter, bstep, iiter0, commit, max_nz, s);
+      break;
+    default:
+      launch_fused_batch_t<32, 8>(grid, item_off, nscen, counter, bstep, iiter0, commit, max_nz, s);
+      break;
+  }
+}
 
 void launch_step_fused(const FusedArgs& a, int shape, cudaStream_t s) {
   switch (shape) {

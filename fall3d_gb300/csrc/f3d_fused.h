@@ -40,6 +40,18 @@ struct FusedArgs {
 // tile region (x by y) / threads: 0 = 32x32 / 256 (default), 1 = 32x64 / 512,
 // 2 = 32x32 / 512.
 void launch_step_fused(const FusedArgs& a, int shape, cudaStream_t s);
+// tiles of one class of an nx x ny grid for a tile shape
+int fused_tiles(int nx, int ny, int shape);
+
+// Batched form: the arguments of up to F3D_BATCH_MAX scenarios in constant
+// memory (c_in / c_out are the scenario's two buffers), then one persistent
+// launch over the work items of all of them.
+#define F3D_BATCH_MAX 160
+int upload_batch_args(const FusedArgs* h, int n, cudaStream_t s);
+// sets the kernel's shared-memory limit and returns its persistent grid (-1 on error)
+int fused_batch_grid(int shape, int max_nz);
+void launch_step_fused_batch(int shape, int grid, const int* item_off, int nscen, int* counter,
+                             const int* bstep, const int* iiter0, int commit, int max_nz, cudaStream_t s);
 void launch_vk32(long long n, int nc, const float* vz, const float* vset, float* vk, cudaStream_t s);
 void launch_wet_lambda(long long n, double dt, const double* prate, double* lam, cudaStream_t s);
 void launch_fp32_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,

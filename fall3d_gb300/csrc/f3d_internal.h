@@ -56,6 +56,34 @@ void launch_setsrc(T* c, long long cstride, Dims d, int nc, int nsou, const int*
                    const double* zlayer, const double* Hm1, double dX1, double dX2, double dt,
                    cudaStream_t s);
 
+// Batched form: per scenario of a batch, the arguments of setsrc and cmass2d
+// (global memory, one entry per scenario in batch order).  c_a / c_b are
+// the scenario's two binary32 state buffers: after an even number of batch
+// steps the state is in c_a, after an odd number in c_b.
+struct BatchAux {
+  float* c_a;
+  float* c_b;
+  long long cstride;
+  Dims d;
+  int nc;
+  double dt;
+  // setsrc.f90:20-35
+  int nsou;
+  const int *isrc, *jsrc, *ksrc;
+  const double* tmrat;
+  const double *dz, *zlayer, *Hm1;
+  double dX1, dX2;
+  // cmass2d.f90:42-104 (binary64 velocities, device outmass)
+  const double *vx, *vy, *vz, *vset;
+  double* outmass;
+  long long n1, n2, n3;
+};
+void launch_setsrc_batch(const BatchAux* tab, const int* bstep, int nscen, int max_nc, cudaStream_t s);
+size_t cmass2d_batch_scratch_bytes(int nscen);
+void launch_cmass2d_batch(const BatchAux* tab, const int* bstep, int nscen, void* scratch,
+                          cudaStream_t s);
+void launch_batch_advance(int* bstep, int nscen, cudaStream_t s);
+
 // Budget reductions.  `scratch` holds at least reduce_scratch_bytes(...)
 // bytes; results are written as binary64 to device memory `out`.
 size_t reduce_scratch_bytes(long long nterms, int nsums);

@@ -674,6 +674,45 @@ void launch_setsrc(T* c, long long cstride, Dims d, int nc, int nsou, const int*
   count_launch();
 }
 
+// Batched form: scenario blockIdx.y, one thread per class; the state before
+// the step is in c_a after an even number of batch steps, else in c_b.
+__global__ void k_setsrc_batch(const BatchAux* tab, const int* bstep) {
+  const BatchAux& b = tab[blockIdx.y];
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= b.nc || b.nsou <= 0) return;
+  const Dims d = b.d;
+  float* cc = ((bstep[blockIdx.y] & 1) ? b.c_b : b.c_a) + (long long)ic * b.cstride;
+  for (int is = 0; is < b.nsou; ++is) {
+    const int i = b.isrc[is], j = b.jsrc[is], k = b.ksrc[is];
+    if (k < 1 || k > d.nz) continue;
+    double dzeta;
+    if (k == 1)
+      dzeta = 0.5 * b.dz[k] + b.zlayer[k - 1];
+    else
+      dzeta = 0.5 * (b.dz[k - 1] + b.dz[k]);
+    const double vol0 = b.Hm1[d.P(i, j)] * b.dX1 * b.dX2 * dzeta;
+    const long long q = d.C(i, j, k);
+    cc[q] = (float)((double)cc[q] + b.dt * b.tmrat[is + (long long)b.nsou * ic] / vol0);
+  }
+}
+
+void launch_setsrc_batch(const BatchAux* tab, const int* bstep, int nscen, int max_nc, cudaStream_t s) {
+  if (nscen <= 0) return;
+  k_setsrc_batch<<<dim3((max_nc + 63) / 64, nscen), 64, 0, s>>>(tab, bstep);
+  count_launch();
+}
+
+__global__ void k_batch_advance(int* bstep, int n) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) bstep[q] = bstep[q] + 1;
+}
+
+void launch_batch_advance(int* bstep, int nscen, cudaStream_t s) {
+  if (nscen <= 0) return;
+  k_batch_advance<<<(nscen + 127) / 128, 128, 0, s>>>(bstep, nscen);
+  count_launch();
+}
+
 // ------------------------------------------------------- conversions
 __global__ void k_d2f(float* dst, const double* src, long long n) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;

@@ -405,6 +405,8 @@ int f3d_run_reset(f3d_ctx* ctx);
 #define F3D_OPT_TILE  2  /* fused kernel tile region x by y / threads:
                             0 = 32x32/256 (default), 1 = 32x64/512,
                             2 = 32x32/512; results do not depend on it   */
+#define F3D_OPT_GRAPH 3  /* batches: 1 = replay one CUDA graph per batch step
+                            (default), 0 = launch the kernels one by one   */
 int f3d_set_option(f3d_ctx* ctx, int key, int value);
 int f3d_get_option(const f3d_ctx* ctx, int key, int* value);
 
@@ -425,6 +427,47 @@ long long f3d_kernel_launches(void);
 
 /* Synchronise the context's stream. */
 int f3d_sync(f3d_ctx* ctx);
+
+/* ------------------------------------------------------------------------
+ * Batched precision form (no counterpart in the reference, whose unit of
+ * work is one scenario per run).  A batch advances the time loops of up to
+ * max_scenarios precision-form contexts together: each scenario runs its
+ * own Fall3d.f90:79-121 loop (source and meteo updates when due, its own dt,
+ * its own x/y alternation), and one batch step performs the transport step
+ * of every running scenario in a single persistent launch, replayed as one
+ * CUDA graph.  A scenario's results are those of f3d_run on the same
+ * context.  Contexts stay owned by the caller and must not be used
+ * elsewhere while they are in a batch.
+ */
+typedef struct f3d_batch f3d_batch;
+int f3d_batch_create(int max_scenarios, f3d_batch** out);
+int f3d_batch_destroy(f3d_batch* b);
+/* Joins a context (FP32 form) to the batch: its time loop starts at
+ * beg_time and ends at end_time (or after max_steps > 0 steps), with the
+ * met and source series of f3d_run; log (log_cap records) receives the
+ * mass-budget records of endstep.f90:51.  *slot identifies it. */
+int f3d_batch_add(f3d_batch* b, f3d_ctx* ctx, const f3d_met_series* met,
+                  const f3d_src_series* src, double beg_time, double end_time,
+                  int max_steps, f3d_log_record* log, int log_cap, int* slot);
+/* One step of every running scenario; *n_running = scenarios still running. */
+int f3d_batch_step(f3d_batch* b, int* n_running);
+/* state: 0 free, 1 running, 2 done, 3 failed (the return code and
+ * f3d_last_error give the failure). */
+int f3d_batch_poll(f3d_batch* b, int slot, int* state, int* steps, int* nlog);
+/* Frees a slot (stops the scenario if still running). */
+int f3d_batch_release(f3d_batch* b, int slot);
+int f3d_batch_sync(f3d_batch* b);
+/* F3D_OPT_TILE (tile shape of the step kernel) and F3D_OPT_GRAPH. */
+int f3d_batch_set_option(f3d_batch* b, int key, int value);
+int f3d_batch_get_option(const f3d_batch* b, int key, int* value);
+/* Times the step kernel of the running scenarios for each tile shape (reps
+ * launches each, without changing any result), keeps the fastest and
+ * returns it and the per-shape milliseconds (ms[3]).  Call it after the
+ * first batch step. */
+int f3d_batch_autotune(f3d_batch* b, int reps, int* best, float* ms);
+int f3d_batch_stats(const f3d_batch* b, long long* batch_steps,
+                    double* cell_class_steps, int* n_running);
+int f3d_batch_stream(const f3d_batch* b, void** stream);
 
 #ifdef __cplusplus
 }
