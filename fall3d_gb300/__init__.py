@@ -118,6 +118,15 @@ def load(build_if_missing: bool = False):
         "f3d_batch_stats": [VP, C.POINTER(C.c_longlong), DP, IP],
         "f3d_batch_stream": [VP, C.POINTER(VP)],
         "f3d_cmass2d_noalloc": [VP, VP, VP, VP, VP, IP, IP, IP, IP, IP, IP, IP, IP, DP, DP, VP, DP, DP],
+        "f3d_server_create": [C.c_longlong, I, C.POINTER(VP)],
+        "f3d_server_destroy": [VP],
+        "f3d_server_submit": [VP, VP, VP, VP, D, D, I, IP],
+        "f3d_server_progress": [VP, I, IP, IP],
+        "f3d_server_poll": [VP, I, IP, DP, DP, DP, C.POINTER(C.c_longlong)],
+        "f3d_server_result": [VP, I, VP, VP, VP, VP, I, IP],
+        "f3d_server_forget": [VP, I],
+        "f3d_server_stats": [VP, C.POINTER(C.c_longlong), DP, C.POINTER(C.c_longlong), IP, IP],
+        "f3d_server_batch": [VP, C.POINTER(VP)],
     }
     for name, args in fine.items():
         f = getattr(lib, name)
@@ -573,3 +582,81 @@ class Batch:
         p = VP()
         _check(self.lib.f3d_batch_stream(self.h, C.byref(p)))
         return int(p.value or 0)
+
+
+class Server:
+    """The serving form (f3d_server_*): continuous batching of forecast
+    requests under an HBM admission cap."""
+
+    QUEUED, RUNNING, DONE, FAILED = 0, 1, 2, 3
+
+    def __init__(self, hbm_cap_bytes: int, max_running: int = 128):
+        self.lib = load()
+        h = VP()
+        _check(self.lib.f3d_server_create(int(hbm_cap_bytes), int(max_running), C.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.f3d_server_destroy(self.h)
+            self.h = VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, scen, log_cap: int = 1024) -> int:
+        grid = _abi.make_grid(scen.grid, PREC_FP32)
+        met = _abi.make_met(scen.met)
+        src = _abi.make_src(scen.src)
+        rid = C.c_int()
+        _check(self.lib.f3d_server_submit(self.h, C.addressof(grid.struct), C.addressof(met.struct),
+                                          C.addressof(src.struct), float(scen.beg_time),
+                                          float(scen.end_time), int(log_cap), C.byref(rid)))
+        self._keep[rid.value] = (grid, met, src, scen.grid["nx"], scen.grid["ny"])
+        return rid.value
+
+    def progress(self, max_steps: int = 1):
+        """(running, queued) after admitting and up to max_steps batch steps."""
+        r, q = C.c_int(), C.c_int()
+        _check(self.lib.f3d_server_progress(self.h, int(max_steps), C.byref(r), C.byref(q)))
+        return r.value, q.value
+
+    def poll(self, rid: int):
+        """dict(state, t_submit, t_admit, t_done, steps); a failed request
+        raises F3DError."""
+        st, steps = C.c_int(), C.c_longlong()
+        ts, ta, td = C.c_double(), C.c_double(), C.c_double()
+        rc = self.lib.f3d_server_poll(self.h, int(rid), C.byref(st), C.byref(ts), C.byref(ta), C.byref(td),
+                                      C.byref(steps))
+        if rc and st.value != self.FAILED:
+            _check(rc)
+        return dict(state=st.value, t_submit=ts.value, t_admit=ta.value, t_done=td.value,
+                    steps=steps.value, error=last_error() if rc else "")
+
+    def result(self, rid: int, log_cap: int = 1024):
+        """LOAD, COL_MASS, C_GRND (ny, nx) and the mass-budget log; frees the
+        request's host arrays of the submission."""
+        _, _, _, nx, ny = self._keep[rid]
+        load, col, grnd = (np.zeros((ny, nx)) for _ in range(3))
+        recs = (_abi.F3DLogRecord * log_cap)()
+        n = C.c_int()
+        _check(self.lib.f3d_server_result(self.h, int(rid), _addr(load), _addr(col), _addr(grnd),
+                                          C.addressof(recs), int(log_cap), C.byref(n)))
+        return dict(load=load, col_mass=col, c_grnd=grnd, log=_abi.log_array(recs, min(n.value, log_cap)))
+
+    def forget(self, rid: int):
+        _check(self.lib.f3d_server_forget(self.h, int(rid)))
+        self._keep.pop(rid, None)
+
+    def stats(self):
+        used, bs = C.c_longlong(), C.c_longlong()
+        ccs = C.c_double()
+        r, q = C.c_int(), C.c_int()
+        _check(self.lib.f3d_server_stats(self.h, C.byref(used), C.byref(ccs), C.byref(bs), C.byref(r),
+                                         C.byref(q)))
+        return dict(used_bytes=used.value, cell_class_steps=ccs.value, batch_steps=bs.value,
+                    running=r.value, queued=q.value)

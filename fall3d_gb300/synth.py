@@ -366,10 +366,11 @@ def make_scenario(name="cfg0", seed=0, **over) -> Scenario:
                     end_time=float(run_s), info=info)
 
 
-def ensemble_member(seed: int, run_h: float = 12.0, max_snapshots=None) -> Scenario:
+def ensemble_member(seed: int, run_h: float = 12.0, max_snapshots=None, met_dt_h: float = 1.0) -> Scenario:
     """One member of the batched ensemble: nx, ny ~ U[64,320], nz ~ U[20,60],
     spacing 0.02-0.05 deg, 4-20 classes over phi -2..6, column 3-20 km, MER
-    log-uniform 1e4-1e8 kg/s for 1-6 h, seeded wind perturbation."""
+    log-uniform 1e4-1e8 kg/s for 1-6 h, seeded wind perturbation; met
+    snapshots every met_dt_h hours."""
     r = np.random.default_rng(10_000 + seed)
     nx = int(r.integers(64, 321))
     ny = int(r.integers(64, 321))
@@ -382,4 +383,4 @@ def ensemble_member(seed: int, run_h: float = 12.0, max_snapshots=None) -> Scena
     ztop = float(max(10000.0, 1.3 * H))
     return make_scenario("cfg0", seed=seed, nx=nx, ny=ny, nz=nz, nc=nc, phimin=-2.0, phimax=6.0,
                          spacing=spacing, ztop=ztop, H=H, M0=M0, erupt_h=erupt_h, run_h=run_h,
-                         met_dt_h=1.0, pert=3.0, spectral=False, max_snapshots=max_snapshots)
+                         met_dt_h=met_dt_h, pert=3.0, spectral=False, max_snapshots=max_snapshots)

@@ -469,6 +469,37 @@ int f3d_batch_stats(const f3d_batch* b, long long* batch_steps,
                     double* cell_class_steps, int* n_running);
 int f3d_batch_stream(const f3d_batch* b, void** stream);
 
+/* ------------------------------------------------------------------------
+ * Serving form (no counterpart in the reference): continuous batching of
+ * forecast requests.  Requests are submitted as they arrive and wait in
+ * arrival order; f3d_server_progress admits waiting requests while the
+ * resident footprint (f3d_ctx_footprint of each precision-form context)
+ * stays under hbm_cap_bytes and a slot is free, then advances every running
+ * request by batch steps.  A finished request's outputs (LOAD, COL_MASS,
+ * C_GRND and the mass-budget log) are kept in host memory and its device
+ * memory is freed for the next admission.  The grid, met and source arrays
+ * of a request must stay valid until it completes.
+ */
+typedef struct f3d_server f3d_server;
+int f3d_server_create(long long hbm_cap_bytes, int max_running, f3d_server** out);
+int f3d_server_destroy(f3d_server* srv);
+int f3d_server_submit(f3d_server* srv, const f3d_grid* grid, const f3d_met_series* met,
+                      const f3d_src_series* src, double beg_time, double end_time,
+                      int log_cap, int* request_id);
+/* Admits, runs up to max_steps batch steps (fewer if a request completes),
+ * collects completed requests. */
+int f3d_server_progress(f3d_server* srv, int max_steps, int* n_running, int* n_queued);
+/* state: 0 queued, 1 running, 2 done, 3 failed, 4 forgotten; seconds of a
+ * monotonic clock at submission, admission and completion. */
+int f3d_server_poll(f3d_server* srv, int request_id, int* state, double* t_submit,
+                    double* t_admit, double* t_done, long long* steps);
+int f3d_server_result(f3d_server* srv, int request_id, double* load, double* col_mass,
+                      double* c_grnd, f3d_log_record* log, int log_cap, int* nlog);
+int f3d_server_forget(f3d_server* srv, int request_id);
+int f3d_server_stats(const f3d_server* srv, long long* used_bytes, double* cell_class_steps,
+                     long long* batch_steps, int* n_running, int* n_queued);
+int f3d_server_batch(f3d_server* srv, f3d_batch** batch);
+
 #ifdef __cplusplus
 }
 #endif
