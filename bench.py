@@ -16,7 +16,15 @@ setbcc, advection, diffusion, wet and dry deposition, clip, cmass2d).
              host buffers: meteorology and sources uploaded by the loop when
              their intervals begin, the deposit maps (LOAD, COL_MASS, C_GRND)
              read back at the end, all inside the timed region.
-``forms``    the plain binary64 form on the same workload.
+``forms``    the plain binary64 form on the same workload; the batched form
+             (64 ensemble members, nx, ny ~ U[64,320], nz ~ U[20,60], 4-20
+             classes, one persistent launch per batch step, 30 timed batch
+             steps); the served form on a bounded sample of the Poisson
+             request stream (p50/p99 latency, beside the same requests run
+             one after another in the FP64 form).
+``accuracy_vs_fp64``  relative L2 / Linf error of every output of the
+             precision form against the FP64 form over the e2e window, and
+             the mass drift |massvol+massdep+outmass-erumass|/erumass.
 ``--impl reference`` times the CPU oracle (the restatement of the reference's
 Fortran path; the Fortran itself cannot be built here) on all host cores.
 Multi-GPU: classes and scenarios are independent, so N GPUs run N replicas
@@ -284,6 +292,7 @@ def run_ours(args, rank, world, local_rank):
     t_e2e = max_over_ranks(t_e2e)
     st = ge.state()
     e2e_steps = st["iiter"]
+    f32_fields = ge.fields() if (rank == 0 and not args.no_forms) else None
     ge.close()
     nx, ny, nz, nc = s.grid["nx"], s.grid["ny"], s.grid["nz"], s.grid["nc"]
     times = s.met["times"]
@@ -339,6 +348,47 @@ def run_ours(args, rank, world, local_rank):
         "kernels_ms_per_step": {k: v[1] / max(1, v[0]) for k, v in prof.items()},
         "meteo_update_s": meteo_s,
     }
+    if rank == 0 and not args.no_forms:
+        # precision form vs the plain FP64 form over the same window: every
+        # output, and the mass drift |massvol+massdep+outmass-erumass|/erumass
+        g64 = F.Context(s, F.PREC_FP64)
+        log64 = g64.run(end_time=window, met=met, src=src)
+        outs64, f64_fields, st64 = g64.outputs(), g64.fields(), g64.state()
+        g64.close()
+        err = {}
+        pairs = [("LOAD", outs["load"], outs64["load"]), ("COL_MASS", outs["col_mass"], outs64["col_mass"]),
+                 ("C_GRND", outs["c_grnd"], outs64["c_grnd"]), ("c", f32_fields["c"], f64_fields["c"]),
+                 ("cdry", f32_fields["cdry"], f64_fields["cdry"]), ("cwet", f32_fields["cwet"], f64_fields["cwet"])]
+        for name, a32, a64 in pairs:
+            d = np.asarray(a32, dtype=np.float64) - a64
+            n64 = float(np.linalg.norm(a64.ravel()))
+            m64 = float(np.max(np.abs(a64)))
+            err[name] = {"rel_l2": float(np.linalg.norm(d.ravel())) / n64 if n64 > 0 else 0.0,
+                         "rel_linf": float(np.max(np.abs(d))) / m64 if m64 > 0 else 0.0}
+
+        def drift(lg):
+            eru = lg["erumass"][-1]
+            return abs(lg["massvol"][-1] + lg["massdep"][-1] + lg["outmass"][-1] - eru) / eru if eru else 0.0
+
+        line["accuracy_vs_fp64"] = {
+            "window": f"{window:.0f} s simulated ({e2e_steps} steps, identical step sequence: "
+                      f"{st['iiter'] == st64['iiter'] and st['dt'] == st64['dt']})",
+            "errors": err, "mass_drift_fp32": drift(log), "mass_drift_fp64": drift(log64),
+            "massvol_rel_diff": abs(log["massvol"][-1] - log64["massvol"][-1]) / abs(log64["massvol"][-1])}
+        from fall3d_gb300 import serve
+
+        try:
+            line["forms"]["fp32_batched"] = serve.ensemble(members=64, steps=30)
+            line["forms"]["fp32_batched"]["over_fp64_plain"] = line["forms"]["fp32_batched"]["value"] / value64
+        except Exception as e:
+            line["forms"]["fp32_batched"] = {"error": str(e)}
+        try:
+            sv = serve.serving(rate=2.0, window=10.0, dmin=0.3, dmax=4.8, met_dt_h=1.0)
+            sv["sample"] = ("Poisson 2 req/s for 10 s, ensemble-member requests with durations "
+                            "U(0.3, 4.8) h (one tenth of the serving config's 3-48 h), hourly met")
+            line["forms"]["served"] = sv
+        except Exception as e:
+            line["forms"]["served"] = {"error": str(e)}
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
             line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
@@ -355,6 +405,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the accuracy check and the batched and served forms")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
