@@ -188,6 +188,23 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks_of(x, dist=None, device="cpu"):
+    """The largest of every rank's x (the job's time is its slowest rank's)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_step, steps, world, ms):
+    """Whole-job throughput: every rank runs its own replica of the workload
+    (weak scaling), the job takes the slowest rank's time ms."""
+    return units_per_step * steps * world / (ms / 1e3)
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     import fall3d_gb300 as F
@@ -202,11 +219,7 @@ def run_ours(args, rank, world, local_rank):
             dist.barrier()
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks_of(x, dist, "cuda")
 
     s = _scenario()
     units_per_step = s.cell_classes
@@ -240,7 +253,7 @@ def run_ours(args, rank, world, local_rank):
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
     ms = max_over_ranks(ms)
-    value = units_per_step * args.steps * world / (ms / 1e3)
+    value = job_rate(units_per_step, args.steps, world, ms)
 
     # per-kernel durations with CUDA events on the same stream
     g.profile(True)
