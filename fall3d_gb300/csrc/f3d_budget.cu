@@ -292,30 +292,43 @@ __global__ void k_finddt(Dims d, int nc, double dX1, double dX2, const double* d
                          const double* vx, const double* vy, const double* vz,
                          const double* vset, const double* rkh1, const double* rkhor,
                          const double* rkver, unsigned long long* dtcn_bits) {
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int nx = d.nx, nz = d.nz;
   const long long s3 = d.cells();
   double best = 0.0;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < s3 * nc;
-       t += (long long)gridDim.x * blockDim.x) {
-    const long long m = t % s3;
-    const int ic = (int)(t / s3);
+  // one thread per cell: the five class-independent terms are summed once
+  // (the reference's left-to-right order keeps them as a prefix), then the
+  // two settling terms of every class are added to that prefix
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < s3;
+       m += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(m % nx) + 1;
     const long long r = m / nx;
-    const int j = (int)(r % ny) + 1, k = (int)(r / ny) + 1;
-    const double* vs = vset + (long long)ic * s3;
+    const int j = (int)(r % d.ny) + 1, k = (int)(r / d.ny) + 1;
     const double ddz = fmin2(dz[k - 1], dz[k]);
-    double dvsetdz;
-    if (k == 1)
-      dvsetdz = (vs[d.M(i, j, 2)] - vs[d.M(i, j, 1)]) / (dz[1]);
-    else if (k == nz)
-      dvsetdz = (vs[d.M(i, j, nz)] - vs[d.M(i, j, nz - 1)]) / (dz[nz - 1]);
-    else
-      dvsetdz = (vs[d.M(i, j, k + 1)] - vs[d.M(i, j, k - 1)]) / (dz[k] + dz[k - 1]);
-    const double dtcni = (2.0 * rkh1[m] / (dX1 * dX1)) + (fabs(vx[m]) / dX1) +
-                         (2.0 * rkhor[m] / (dX2 * dX2)) + (fabs(vy[m]) / dX2) +
-                         (2.0 * rkver[m] / (ddz * ddz)) + (fabs((vz[m] + vs[m])) / ddz) +
-                         (fabs(dvsetdz));
-    best = fmax2(best, dtcni);
+    const double pre = (2.0 * rkh1[m] / (dX1 * dX1)) + (fabs(vx[m]) / dX1) +
+                       (2.0 * rkhor[m] / (dX2 * dX2)) + (fabs(vy[m]) / dX2) +
+                       (2.0 * rkver[m] / (ddz * ddz));
+    long long mlo, mhi;
+    double den;
+    if (k == 1) {
+      mlo = d.M(i, j, 1);
+      mhi = d.M(i, j, 2);
+      den = dz[1];
+    } else if (k == nz) {
+      mlo = d.M(i, j, nz - 1);
+      mhi = d.M(i, j, nz);
+      den = dz[nz - 1];
+    } else {
+      mlo = d.M(i, j, k - 1);
+      mhi = d.M(i, j, k + 1);
+      den = dz[k] + dz[k - 1];
+    }
+    const double vzm = vz[m];
+    for (int ic = 0; ic < nc; ++ic) {
+      const double* vs = vset + (long long)ic * s3;
+      const double dvsetdz = (vs[mhi] - vs[mlo]) / den;
+      const double dtcni = pre + (fabs((vzm + vs[m])) / ddz) + (fabs(dvsetdz));
+      best = fmax2(best, dtcni);
+    }
   }
   for (int off = 16; off > 0; off >>= 1) best = fmax2(best, __shfl_down_sync(0xffffffffu, best, off));
   if ((threadIdx.x & 31) == 0 && best > 0.0)
@@ -326,7 +339,7 @@ void launch_finddt(Dims d, int nc, double dX1, double dX2, const double* dz, con
                    const double* vy, const double* vz, const double* vset, const double* rkh1,
                    const double* rkhor, const double* rkver, unsigned long long* dtcn_bits,
                    cudaStream_t s) {
-  const long long n = d.cells() * nc;
+  const long long n = d.cells();
   const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 8);
   k_finddt<<<nb, 256, 0, s>>>(d, nc, dX1, dX2, dz, vx, vy, vz, vset, rkh1, rkhor, rkver, dtcn_bits);
   count_launch();

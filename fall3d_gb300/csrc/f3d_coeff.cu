@@ -438,16 +438,23 @@ __device__ __forceinline__ double sutherland(double T) {
   return visc0 * ((Tair0 + 120.0) / (T + 120.0)) * pow(T / Tair0, 1.5);
 }
 
+// The air viscosity of every cell, shared by all classes (setvset.f90:95-97).
+__global__ void k_visc(long long s3, const double* tempe, double* visc) {
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < s3;
+       m += (long long)gridDim.x * blockDim.x)
+    visc[m] = sutherland(tempe[m]);
+}
+
 // Runs chain cells [q0, q1) from cd; writes outputs when `write`.
 __device__ void chain_run(const ChainGeom& g, long long q0, long long q1, int modv,
-                          const ClassConst* cc, const double* tempe, const double* rho,
+                          const ClassConst* cc, const double* viscs, const double* rho,
                           double* vset, int* iters, double& cd, bool write, int& nonconv) {
   const long long s3 = g.d.cells();
   for (long long q = q0; q < q1; ++q) {
     int ic;
     long long m;
     chain_cell(g, q, ic, m);
-    const double visc = sutherland(tempe[m]);
+    const double visc = viscs[m];
     double v;
     const int it = vsettl_dev(cc[ic], modv, rho[m], visc, cd, v);
     if (write) {
@@ -458,7 +465,7 @@ __device__ void chain_run(const ChainGeom& g, long long q0, long long q1, int mo
   }
 }
 
-__global__ void k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, const double* tempe,
+__global__ void k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, const double* visc,
                                  const double* rho, double* vset, int* iters,
                                  const double* cd_state, double* entry, double* exitv,
                                  int* nonconv) {
@@ -471,10 +478,10 @@ __global__ void k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, co
     cd = *cd_state;
   } else {
     cd = 1.0;
-    chain_run(g, max(0LL, q0 - g.W), q0, modv, cc, tempe, rho, vset, iters, cd, false, dummy);
+    chain_run(g, max(0LL, q0 - g.W), q0, modv, cc, visc, rho, vset, iters, cd, false, dummy);
   }
   entry[s] = cd;
-  chain_run(g, q0, q1, modv, cc, tempe, rho, vset, iters, cd, true, nc_flag);
+  chain_run(g, q0, q1, modv, cc, visc, rho, vset, iters, cd, true, nc_flag);
   exitv[s] = cd;
   nonconv[s] = nc_flag;
 }
@@ -493,7 +500,7 @@ __global__ void k_chain_check(ChainGeom g, const double* entry, const double* ex
 // Sequential repair in chain order (single thread).  Segments verified above
 // stay; a recomputed segment may change its exit, so its successor is
 // re-checked until the chain agrees again.  cap overflow -> full scan.
-__global__ void k_chain_fix(ChainGeom g, int modv, const ClassConst* cc, const double* tempe,
+__global__ void k_chain_fix(ChainGeom g, int modv, const ClassConst* cc, const double* visc,
                             const double* rho, double* vset, int* iters, double* entry,
                             double* exitv, int* nonconv, int* bad, const int* nbad, int cap,
                             double* cd_state) {
@@ -521,7 +528,7 @@ __global__ void k_chain_fix(ChainGeom g, int modv, const ClassConst* cc, const d
         int nc_flag = 0;
         entry[s] = cd;
         const long long q0 = s * g.S, q1 = min(g.L, q0 + g.S);
-        chain_run(g, q0, q1, modv, cc, tempe, rho, vset, iters, cd, true, nc_flag);
+        chain_run(g, q0, q1, modv, cc, visc, rho, vset, iters, cd, true, nc_flag);
         exitv[s] = cd;
         nonconv[s] = nc_flag;
         ++s;  // the successor must be re-checked
@@ -560,14 +567,30 @@ __global__ void k_vset_finish(long long s3, int nc, int np, int aggregate, doubl
   }
 }
 
+// Threads of k_chain_segments the device holds at once (blocks of 64).
+static long long chain_capacity() {
+  static long long cap = 0;
+  if (cap == 0) {
+    int dev = 0, nsm = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chain_segments, 64, 0);
+    cap = (long long)std::max(1, nsm) * std::max(1, per_sm) * 64;
+  }
+  return cap;
+}
+
 static ChainGeom chain_geom(Dims d, int np) {
   ChainGeom g;
   g.d = d;
   g.L = d.cells() * np;
-  // Aim for at least ~19k segments (about 4 warps per SM) so the FP64 pipes
-  // stay busy; the warm-up covers the contraction of the cd iteration.
-  long long S = g.L / 19456;
-  S = std::max<long long>(32, std::min<long long>(512, S));
+  // The segments are the threads of one launch: as many as the device holds
+  // at once (one wave, no tail) when the chain is long enough, else fewer,
+  // longer segments so that the warm-up (W cells recomputed from the
+  // preceding segment, enough for the cd iteration to forget its guess)
+  // stays a small fraction of the work.
+  long long S = (g.L + chain_capacity() - 1) / chain_capacity();
+  S = std::max<long long>(256, S);
   g.S = S;
   g.W = 64;
   g.nseg = (g.L + S - 1) / S;
@@ -581,6 +604,7 @@ size_t setvset_scratch_bytes(Dims d, int np) {
   size_t b = sizeof(ClassConst) * (size_t)(np + 1);
   b += 2 * sizeof(double) * (size_t)g.nseg + sizeof(int) * (size_t)g.nseg;
   b += sizeof(int) * (kBadCap + 8) + 1024;
+  b += sizeof(double) * (size_t)d.cells() + 256;  // viscosity per cell
   return b;
 }
 
@@ -601,18 +625,21 @@ void launch_setvset(Dims d, int nc, int np, int modv, const double* diam, const 
   int* nonconv = reinterpret_cast<int*>(take(sizeof(int) * (size_t)g.nseg));
   int* nbad = reinterpret_cast<int*>(take(sizeof(int) * 8));
   int* bad = reinterpret_cast<int*>(take(sizeof(int) * kBadCap));
+  double* visc = reinterpret_cast<double*>(take(sizeof(double) * (size_t)d.cells()));
   cudaMemsetAsync(nbad, 0, sizeof(int), s);
   cudaMemsetAsync(status, 0, sizeof(int), s);
   if (np > 0 && g.L > 0) {
     k_class_consts<<<(np + 31) / 32, 32, 0, s>>>(np, modv, diam, rhop, psi, sphe, cc);
+    k_visc<<<(int)std::min<long long>((d.cells() + 255) / 256, 152LL * 16), 256, 0, s>>>(d.cells(), tempe,
+                                                                                         visc);
     const int bs = 64;
     k_chain_segments<<<(unsigned)((g.nseg + bs - 1) / bs), bs, 0, s>>>(
-        g, modv, cc, tempe, rho, vset, iters, cd_state, entry, exitv, nonconv);
+        g, modv, cc, visc, rho, vset, iters, cd_state, entry, exitv, nonconv);
     k_chain_check<<<(unsigned)((g.nseg + 255) / 256), 256, 0, s>>>(g, entry, exitv, bad, nbad, kBadCap);
-    k_chain_fix<<<1, 32, 0, s>>>(g, modv, cc, tempe, rho, vset, iters, entry, exitv, nonconv, bad,
+    k_chain_fix<<<1, 32, 0, s>>>(g, modv, cc, visc, rho, vset, iters, entry, exitv, nonconv, bad,
                                  nbad, kBadCap, cd_state);
     k_chain_status<<<(unsigned)((g.nseg + 255) / 256), 256, 0, s>>>(g, nonconv, status);
-    count_launch(5);
+    count_launch(6);
   }
   const long long n = d.cells() * nc;
   k_vset_finish<<<(int)std::min<long long>((n + 255) / 256, 152LL * 16), 256, 0, s>>>(
