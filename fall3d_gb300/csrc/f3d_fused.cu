@@ -129,6 +129,62 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 __device__ __forceinline__ float shup(float v) { return __shfl_up_sync(FULL, v, 1); }
 __device__ __forceinline__ float shdn(float v) { return __shfl_down_sync(FULL, v, 1); }
 
+// Packed binary32 pairs (two rows of one lane): each lane of an f32x2
+// operation is rounded exactly as the scalar binary32 operation, so the
+// packed formulas below give the scalar ones' results bit for bit.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n .reg .b64 x, y, z;\n mov.b64 x, {%2, %3};\n mov.b64 y, {%4, %5};\n"
+      " sub.rn.f32x2 z, x, y;\n mov.b64 {%0, %1}, z;\n}\n"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 abs2(float2 v) { return make_float2(fabsf(v.x), fabsf(v.y)); }
+__device__ __forceinline__ float2 shup2(float2 v) { return make_float2(shup(v.x), shup(v.y)); }
+__device__ __forceinline__ float2 shdn2(float2 v) { return make_float2(shdn(v.x), shdn(v.y)); }
+
+__device__ __forceinline__ void zwork2(float2 cm, float2 c0, float2 cp, float2 vk, float2 vk_1,
+                                       const ZT32& z, float dt, float2& w1, float2& w2) {
+  const float2 vk_12 = mul2(splat(0.5f), add2(vk, vk_1));
+  w1 = mul2(mul2(splat(dt), sub2(mul2(vk, c0), mul2(vk_1, cm))), splat(z.dzz));
+  const float2 dr = mul2(sub2(cp, c0), splat(z.dzk)), dl = mul2(sub2(c0, cm), splat(z.dzk_1));
+  const float2 sigma = make_float2(minmod(dr.x, dl.x), minmod(dr.y, dl.y));
+  const float2 avk = abs2(vk_12);
+  const float2 Crk = mul2(mul2(avk, splat(dt)), splat(z.dzk_1));
+  w2 = mul2(mul2(mul2(mul2(splat(dt * 0.5f * z.dzm1), sub2(splat(1.0f), Crk)), sigma), avk), splat(z.dzz));
+}
+
+__device__ __forceinline__ void line_work2(float2 cm, float2 c0, float2 cp, float2 vq, float2 vq_1,
+                                           float auxv, float invd, float dt, float2& w1, float2& w2) {
+  const float2 vq_12 = mul2(splat(0.5f), add2(vq, vq_1));
+  w1 = mul2(splat(auxv), sub2(mul2(vq, c0), mul2(vq_1, cm)));
+  const float2 dr = mul2(sub2(cp, c0), splat(invd)), dl = mul2(sub2(c0, cm), splat(invd));
+  const float2 sigma = make_float2(minmod(dr.x, dl.x), minmod(dr.y, dl.y));
+  const float2 avq = abs2(vq_12);
+  const float2 Cri = mul2(splat(auxv), avq);
+  w2 = mul2(mul2(mul2(splat(dt * 0.5f), sub2(splat(1.0f), Cri)), sigma), avq);
+}
+
+__device__ __forceinline__ float2 line_update2(float2 c0, float2 vq, float2 w1, float2 w1p, float2 w2,
+                                               float2 w2m, float2 w2p) {
+  const float2 dm = sub2(w2, w2m), dp = sub2(w2p, w2);
+  const float2 a = make_float2(vq.x > 0.0f ? w1.x : w1p.x, vq.y > 0.0f ? w1.y : w1p.y);
+  const float2 b = make_float2(vq.x > 0.0f ? dm.x : dp.x, vq.y > 0.0f ? dm.y : dp.y);
+  return sub2(sub2(c0, a), b);
+}
+
+__device__ __forceinline__ float2 diff_mid2(float2 cm, float2 c0, float2 cp, float2 lm, float2 l0, float2 lp,
+                                            float2 Pm, float2 P0, float2 Pp, float dtdx2) {
+  const float2 c0l0 = mul2(c0, l0);
+  const float2 gradr = mul2(mul2(splat(0.5f), add2(Pp, P0)), sub2(mul2(cp, lp), c0l0));
+  const float2 gradl = mul2(mul2(splat(0.5f), add2(P0, Pm)), sub2(c0l0, mul2(cm, lm)));
+  return add2(c0, mul2(splat(dtdx2), sub2(gradr, gradl)));
+}
+
 // Staged fields of iteration t (plane index in parentheses).
 enum : int { F_C = 0, F_VK, F_VX, F_VY, F_L, F_PZ, F_L1, F_PX, F_PY, NF };
 //            c(t+2) vz+vset(t+1) vx(t) vy(t) 1/rho(t) K*rho_z(t) 1/rho(t-1) K*rho_x(t-1) K*rho_y(t-1)
@@ -287,7 +343,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
   }
 
   // ------------------------------------------------ one iteration of the march
-  auto plane = [&](auto edge_c, auto steady_c, const int t) {
+  auto plane_generic = [&](auto edge_c, auto steady_c, const int t) {
     constexpr bool EDGE = decltype(edge_c)::value;
     constexpr bool STEADY = decltype(steady_c)::value;  // 3 <= t <= nz-2
     cp_async_wait_all();  // own staged inputs of iteration t are in shared memory
@@ -582,6 +638,165 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
       }
       cout[cidx] = clip0(cnew);
     }
+  };
+
+  // The steady planes of interior tiles: the same formulas on pairs of rows
+  // (r = 2q, 2q+1) with packed f32x2 arithmetic.
+  auto plane_packed = [&](const int t) {
+    constexpr int RP = RPW / 2;
+    static_assert(RPW % 2 == 0, "rows per warp must pair up");
+    cp_async_wait_all();
+    const float* sb = stage + (t & 1) * (NF * NP);
+    auto rowpos = [&](int q) { return (warp + NW * 2 * q) * HX + lane; };  // row 2q; row 2q+1 is +NW*HX
+    auto ld2 = [&](const float* base, int p0) { return make_float2(base[p0], base[p0 + NW * HX]); };
+    auto pk = [](const float* v, int q) { return make_float2(v[2 * q], v[2 * q + 1]); };
+    auto up = [](float* v, int q, float2 x) {
+      v[2 * q] = x.x;
+      v[2 * q + 1] = x.y;
+    };
+    float2 s2v[RP];
+    {
+      const ZT32 zn = tab[t + 1];
+      float2 s1v[RP];
+#pragma unroll
+      for (int q = 0; q < RP; ++q) {  // A: advctzc
+        const int p0 = rowpos(q);
+        const float2 vkp = ld2(sb + F_VK * NP, p0), o2 = ld2(sb + F_C * NP, p0);
+        const float2 O0 = pk(o_0, q), O1 = pk(o_p1, q), VK0 = pk(vk0, q);
+        const float2 W1K = pk(w1k, q), W2KM = pk(w2km, q), W2K = pk(w2k, q);
+        float2 w1n, w2n;
+        zwork2(O0, O1, o2, vkp, VK0, zn, dt, w1n, w2n);
+        s1v[q] = line_update2(O0, VK0, W1K, w1n, W2K, W2KM, w2n);
+        up(w2km, q, W2K);
+        up(w2k, q, w2n);
+        up(w1k, q, w1n);
+        up(o_0, q, O1);
+        up(o_p1, q, o2);
+        up(vk0, q, vkp);
+      }
+      auto adv_x2 = [&](const float2* in, float2* out) {
+#pragma unroll
+        for (int q = 0; q < RP; ++q) {
+          const int p0 = rowpos(q);
+          const float2 c0 = in[q], v = ld2(sb + F_VX * NP, p0);
+          float2 w1, w2;
+          line_work2(shup2(c0), c0, shdn2(c0), v, shup2(v), auxvx, a.inv_dx, dt, w1, w2);
+          out[q] = line_update2(c0, v, w1, shdn2(w1), w2, shup2(w2), shdn2(w2));
+        }
+      };
+      auto adv_y2 = [&](const float2* in, float2* out) {
+#pragma unroll
+        for (int q = 0; q < RP; ++q) {
+          const int p0 = rowpos(q);
+          P0s[p0] = in[q].x;
+          P0s[p0 + NW * HX] = in[q].y;
+        }
+        __syncthreads();
+        prefetch(False_{}, t + 1);
+#pragma unroll
+        for (int q = 0; q < RP; ++q) {
+          const int p0 = rowpos(q);
+          float2 w1, w2;
+          line_work2(ld2(P0s - HX, p0), in[q], ld2(P0s + HX, p0), ld2(sb + F_VY * NP, p0),
+                     ld2(sb + F_VY * NP - HX, p0), auxvy, a.inv_dy, dt, w1, w2);
+          W1s[p0] = w1.x;
+          W1s[p0 + NW * HX] = w1.y;
+          W2s[p0] = w2.x;
+          W2s[p0 + NW * HX] = w2.y;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < RP; ++q) {
+          const int p0 = rowpos(q);
+          out[q] = line_update2(in[q], ld2(sb + F_VY * NP, p0), ld2(W1s, p0), ld2(W1s + HX, p0), ld2(W2s, p0),
+                                ld2(W2s - HX, p0), ld2(W2s + HX, p0));
+        }
+      };
+      float2 sav[RP];
+      if (xfirst) {  // sizloop.f90:42-48
+        adv_x2(s1v, sav);
+        adv_y2(sav, s2v);
+      } else {
+        adv_y2(s1v, sav);
+        adv_x2(sav, s2v);
+      }
+    }
+    // C: diffz for plane k = t-1 (an interior plane)
+    const int k = t - 1;
+    const ZT32 zk = tab[k];
+    float2 s3v[RP];
+#pragma unroll
+    for (int q = 0; q < RP; ++q) {
+      const int p0 = rowpos(q);
+      const float2 RB = pk(rc, q), RC = s2v[q];
+      up(rb, q, RB);
+      up(rc, q, RC);
+      const float2 lb = ld2(sb + F_L1 * NP, p0), lc = ld2(sb + F_L * NP, p0), pc = ld2(sb + F_PZ * NP, p0);
+      const float2 gradt =
+          mul2(mul2(mul2(splat(0.5f), add2(pc, pk(pb, q))), sub2(mul2(RC, lc), mul2(RB, lb))), splat(zk.l_dz));
+      const float2 work = mul2(mul2(splat(dt), sub2(gradt, pk(fprev, q))), splat(zk.l_dzdz));
+      up(fprev, q, gradt);
+      up(pb, q, pc);
+      s3v[q] = add2(RB, work);
+    }
+    // D: diffx and diffy
+    auto dif_x2 = [&](const float2* in, float2* out) {
+#pragma unroll
+      for (int q = 0; q < RP; ++q) {
+        const int p0 = rowpos(q);
+        const float2 l0 = ld2(sb + F_L1 * NP, p0), P0 = ld2(sb + F_PX * NP, p0), c0 = in[q];
+        out[q] = diff_mid2(shup2(c0), c0, shdn2(c0), shup2(l0), l0, shdn2(l0), shup2(P0), P0, shdn2(P0), a.dtdx2);
+      }
+    };
+    auto dif_y2 = [&](const float2* in, float2* out) {
+#pragma unroll
+      for (int q = 0; q < RP; ++q) {
+        const int p0 = rowpos(q);
+        P1s[p0] = in[q].x;
+        P1s[p0 + NW * HX] = in[q].y;
+      }
+      __syncthreads();
+      const float* L = sb + F_L1 * NP;
+      const float* PY = sb + F_PY * NP;
+#pragma unroll
+      for (int q = 0; q < RP; ++q) {
+        const int p0 = rowpos(q);
+        out[q] = diff_mid2(ld2(P1s - HX, p0), in[q], ld2(P1s + HX, p0), ld2(L - HX, p0), ld2(L, p0), ld2(L + HX, p0),
+                           ld2(PY - HX, p0), ld2(PY, p0), ld2(PY + HX, p0), a.dtdy2);
+      }
+    };
+    float2 s3a[RP], s4v[RP];
+    if (xfirst) {  // sizloop.f90:55-61
+      dif_x2(s3v, s3a);
+      dif_y2(s3a, s4v);
+    } else {
+      dif_y2(s3v, s3a);
+      dif_x2(s3a, s4v);
+    }
+    // E: wetdep, clip, store (plane k; no accum above k = 1)
+    const double dzk64 = a.dz64[k];
+    const bool lane_out = lane >= 3 && lane < 3 + TX;
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      const int hy = warp + NW * r;
+      if (!(lane_out && hy >= 3 && hy < 3 + TY)) continue;
+      float cnew = (r & 1) ? s4v[r >> 1].y : s4v[r >> 1].x;
+      if (wet) {
+        const int o = (lane - 3) + TX * (hy - 3);
+        if (k <= wkz[o]) {  // wetdep (wetdep.f90:37-49)
+          wacc[o] = wacc[o] + dzk64 * wlam[o] * (double)cnew;
+          cnew = (float)((double)cnew * (1.0 - wlam[o]));
+        }
+      }
+      cout[cb0 + NW * r * (nx + 2) + k * cs] = clip0(cnew);
+    }
+  };
+
+  auto plane = [&](auto edge_c, auto steady_c, const int t) {
+    if constexpr (!decltype(edge_c)::value && decltype(steady_c)::value)
+      plane_packed(t);
+    else
+      plane_generic(edge_c, steady_c, t);
   };
 
   auto march = [&](auto edge_c) {
