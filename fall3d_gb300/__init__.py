@@ -568,7 +568,7 @@ class Batch:
         """Picks the fastest tile shape on the running scenarios; returns
         (best shape, [ms per shape])."""
         best = C.c_int()
-        ms = (C.c_float * 3)()
+        ms = (C.c_float * 4)()
         _check(self.lib.f3d_batch_autotune(self.h, int(reps), C.byref(best), ms))
         return best.value, [float(v) for v in ms]
 

@@ -28,6 +28,7 @@ UNITS = {
     "f3d_budget.cu": ["--fmad=false"],
     "f3d_coeff.cu": ["--fmad=false"],
     "f3d_fused.cu": ["--fmad=false"],
+    "f3d_fused2.cu": ["--fmad=false"],
     "f3d_api.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
     "f3d_ctx.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
     "f3d_batch.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],

@@ -75,6 +75,8 @@ struct f3d_batch {
   bool tables_dirty = true, graph_dirty = true;
   int use_graph = 1;
   int shape = 0, grid = 0, max_nz = 0, max_nc = 0;
+  int split = 0, total = 0;  // items of the even-nx scenarios come first (shape 3)
+  int graph_kernels = 0;     // kernels in one replay of the graph
   long long batch_steps = 0;
   double cell_class_steps = 0.0;
 };
@@ -84,7 +86,12 @@ namespace {
 int table_rebuild(f3d_batch* b) {
   const int n = (int)b->active.size();
   BK(cudaStreamSynchronize(b->stream));  // the previous step no longer reads the tables
+  // batch order: scenarios with an even nx first (the shape-3 kernel runs
+  // them and the others in two launches)
+  std::stable_partition(b->active.begin(), b->active.end(),
+                        [&](int id) { return (b->slot[id].x->g.nx & 1) == 0; });
   int off = 0;
+  b->split = -1;
   b->max_nz = 0;
   b->max_nc = 0;
   for (int q = 0; q < n; ++q) {
@@ -120,6 +127,7 @@ int table_rebuild(f3d_batch* b) {
     u.n1 = 2LL * x->g.nc * x->g.ny * x->g.nz;
     u.n2 = 2LL * x->g.nc * x->g.nx * x->g.nz;
     u.n3 = (long long)x->g.nc * x->g.nx * x->g.ny;
+    if (b->split < 0 && (x->g.nx & 1)) b->split = off;
     b->h_item_off[q] = off;
     off += fused_tiles(x->g.nx, x->g.ny, b->shape) * x->g.nc;
     b->h_bstep[q] = s.bstep;
@@ -128,6 +136,8 @@ int table_rebuild(f3d_batch* b) {
     b->max_nc = std::max(b->max_nc, x->g.nc);
   }
   b->h_item_off[n] = off;
+  b->total = off;
+  if (b->split < 0) b->split = off;
   if (n > 0) {
     if (upload_batch_args(b->h_args, n, b->stream)) return ctx_error(F3D_ERR_CUDA, "constant table upload failed");
     BK(cudaMemcpyAsync(b->d_aux, b->h_aux, sizeof(BatchAux) * n, cudaMemcpyHostToDevice, b->stream));
@@ -143,10 +153,10 @@ int table_rebuild(f3d_batch* b) {
 // the kernels of one batch step, in stream order
 int enqueue_step(f3d_batch* b, int commit_only_fused) {
   const int n = (int)b->active.size();
-  BK(cudaMemsetAsync(b->d_counter, 0, sizeof(int), b->stream));
+  BK(cudaMemsetAsync(b->d_counter, 0, 2 * sizeof(int), b->stream));
   if (!commit_only_fused) launch_setsrc_batch(b->d_aux, b->d_bstep, n, b->max_nc, b->stream);
-  launch_step_fused_batch(b->shape, b->grid, b->d_item_off, n, b->d_counter, b->d_bstep, b->d_iiter0,
-                          commit_only_fused ? 0 : 1, b->max_nz, b->stream);
+  launch_step_fused_batch(b->shape, b->grid, b->d_item_off, n, b->split, b->total, b->d_counter, b->d_bstep,
+                          b->d_iiter0, commit_only_fused ? 0 : 1, b->max_nz, b->stream);
   if (!commit_only_fused) {
     launch_cmass2d_batch(b->d_aux, b->d_bstep, n, b->d_red, b->stream);
     launch_batch_advance(b->d_bstep, n, b->stream);
@@ -163,10 +173,12 @@ int graph_rebuild(f3d_batch* b) {
   if (b->grid < 1) return ctx_error(F3D_ERR_CUDA, "persistent kernel does not fit on the device");
   if (b->use_graph && !b->active.empty()) {
     cudaGraph_t g = nullptr;
+    const long long n0 = f3d_kernel_launches();
     BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const int rc = enqueue_step(b, 0);
     const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-    count_launch(-5);  // counted per replay instead
+    b->graph_kernels = (int)(f3d_kernel_launches() - n0);
+    count_launch(-b->graph_kernels);  // counted per replay instead
     if (rc) return rc;
     BK(e);
     const cudaError_t e2 = cudaGraphInstantiate(&b->exec, g, 0);
@@ -206,7 +218,7 @@ int f3d_batch_create(int max_scenarios, f3d_batch** out) {
   ok = ok && cudaMalloc(&b->d_item_off, sizeof(int) * (n + 1)) == cudaSuccess;
   ok = ok && cudaMalloc(&b->d_bstep, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMalloc(&b->d_iiter0, sizeof(int) * n) == cudaSuccess;
-  ok = ok && cudaMalloc(&b->d_counter, sizeof(int)) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_counter, 2 * sizeof(int)) == cudaSuccess;
   ok = ok && cudaMalloc(&b->d_red, cmass2d_batch_scratch_bytes(n)) == cudaSuccess;
   ok = ok && cudaMallocHost(&b->h_aux, sizeof(BatchAux) * n) == cudaSuccess;
   ok = ok && cudaMallocHost(&b->h_args, sizeof(FusedArgs) * n) == cudaSuccess;
@@ -323,7 +335,7 @@ int f3d_batch_step(f3d_batch* b, int* n_running) {
   }
   if (b->exec) {
     BK(cudaGraphLaunch(b->exec, b->stream));
-    count_launch(5);
+    count_launch(b->graph_kernels);
   } else {
     if (int rc = enqueue_step(b, 0)) return rc;
   }
@@ -382,7 +394,7 @@ int f3d_batch_sync(f3d_batch* b) {
 int f3d_batch_set_option(f3d_batch* b, int key, int value) {
   if (!b) return ctx_error(F3D_ERR_ARG, "NULL batch");
   if (key == F3D_OPT_TILE) {
-    if (value < 0 || value > 2) return ctx_error(F3D_ERR_ARG, "tile shape outside 0..2");
+    if (value < 0 || value > 3) return ctx_error(F3D_ERR_ARG, "tile shape outside 0..3");
     b->shape = value;
   } else if (key == F3D_OPT_GRAPH) {
     b->use_graph = value ? 1 : 0;
@@ -416,9 +428,10 @@ int f3d_batch_autotune(f3d_batch* b, int reps, int* best, float* ms) {
   BK(cudaEventCreate(&e1));
   float bestms = 1e30f;
   int bestshape = b->shape;
-  for (int shape = 0; shape < 3; ++shape) {
+  for (int shape = 0; shape < 4; ++shape) {
     b->shape = shape;
     if (int rc = table_rebuild(b)) return rc;
+
     b->grid = fused_batch_grid(shape, std::max(b->max_nz, 3));
     if (b->grid < 1) {
       if (ms) ms[shape] = -1.0f;

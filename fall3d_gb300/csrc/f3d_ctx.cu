@@ -261,7 +261,10 @@ void sizloop_fused(f3d_ctx* x) {
   const FusedArgs a = f3d::ctx_fused_args(x);
   {
     ProfScope ps(x, "step_fused");
-    launch_step_fused(a, x->opt_tile, s);
+    if (x->opt_tile == 3)
+      launch_step_fused2(a, s);
+    else
+      launch_step_fused(a, x->opt_tile, s);
   }
   std::swap(x->c32, x->c32b);
   {
@@ -314,6 +317,14 @@ FusedArgs ctx_fused_args(f3d_ctx* x) {
   a.cdry = x->cdry;
   a.vset64 = x->vset;
   a.vdep64 = x->vdep;
+  a.vxh = x->vxh;
+  a.vyh = x->vyh;
+  a.lrhoh = x->lrhoh;
+  a.pkxh = x->pkxh;
+  a.pkyh = x->pkyh;
+  a.pkzh = x->pkzh;
+  a.vkh = x->vkh;
+  a.pair_aligned = (d.nx % 2 == 0) ? 1 : 0;
   return a;
 }
 }  // namespace f3d
@@ -423,6 +434,13 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
     A(pky32, s3);
     A(pkz32, s3);
     A(vk32, s3 * nc);
+    A(vxh, hb);
+    A(vyh, hb);
+    A(lrhoh, hb);
+    A(pkxh, hb);
+    A(pkyh, hb);
+    A(pkzh, hb);
+    A(vkh, hb * nc);
     A(lambda2d, pl);
     A(wet_class, nc);
   } else {
@@ -542,6 +560,16 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
     launch_fp32_coeffs((long long)s3, x->rho, x->rkh1, x->rkhor, x->rkver, x->lrho32, x->pkx32,
                        x->pky32, x->pkz32, s);
     launch_vk32((long long)s3, g.nc, x->vz32, x->vset32, x->vk32, s);
+    {  // halo-layout copies for the two-columns-per-lane kernel
+      const float* src[6] = {x->vx32, x->vy32, x->lrho32, x->pkx32, x->pky32, x->pkz32};
+      float* dst[6] = {x->vxh, x->vyh, x->lrhoh, x->pkxh, x->pkyh, x->pkzh};
+      launch_to_halo(d, 6, src, dst, s);
+      for (int c = 0; c < g.nc; ++c) {
+        const float* vs = x->vk32 + (size_t)c * s3;
+        float* vd = x->vkh + (size_t)c * (size_t)d.halo();
+        launch_to_halo(d, 1, &vs, &vd, s);
+      }
+    }
   }
   CK(cudaGetLastError());
   struct {
@@ -818,7 +846,7 @@ int f3d_set_option(f3d_ctx* x, int key, int value) {
   if (key == F3D_OPT_FUSED) {
     x->opt_fused = value ? 1 : 0;
   } else if (key == F3D_OPT_TILE) {
-    if (value < 0 || value > 2) return f3d::ctx_error(F3D_ERR_ARG, "tile shape must be 0..2");
+    if (value < 0 || value > 3) return f3d::ctx_error(F3D_ERR_ARG, "tile shape must be 0..3");
     x->opt_tile = value;
   } else {
     return f3d::ctx_error(F3D_ERR_ARG, "unknown option");

@@ -38,9 +38,12 @@ struct f3d_ctx {
   float* c32b = nullptr;
   float *lrho32 = nullptr, *pkx32 = nullptr, *pky32 = nullptr, *pkz32 = nullptr;
   float* vk32 = nullptr;  // vz + vset per class
+  // the fused met fields in the halo layout of c (two-columns-per-lane kernel)
+  float *vxh = nullptr, *vyh = nullptr, *lrhoh = nullptr, *pkxh = nullptr, *pkyh = nullptr,
+        *pkzh = nullptr, *vkh = nullptr;
   double* lambda2d = nullptr;
   unsigned char* wet_class = nullptr;
-  int opt_fused = 1, opt_tile = 0;
+  int opt_fused = 1, opt_tile = 3;
   // the fused kernel applies: zlayer non-decreasing, 32-bit offsets in a class
   int fused_ok = 1;
   // sources

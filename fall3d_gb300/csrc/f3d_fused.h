@@ -35,23 +35,39 @@ struct FusedArgs {
   double* cdry;
   const double* vset64;  // class blocks, vstride apart
   const double* vdep64;  // class blocks of nx*ny
+  // the same binary32 fields in the halo layout of c ((nx+2)(ny+2)(nz+2),
+  // ghost entries zero), so that one offset addresses every field of a
+  // position: used by the two-columns-per-lane kernel (tile shape 3)
+  const float *vxh, *vyh, *lrhoh, *pkxh, *pkyh, *pkzh;
+  const float* vkh;  // class blocks of the halo size
+  int pair_aligned;  // nx even: every even column starts an 8-byte pair
 };
 
 // tile region (x by y) / threads: 0 = 32x32 / 256 (default), 1 = 32x64 / 512,
-// 2 = 32x32 / 512.
+// 2 = 32x32 / 512, 3 = 64x32 / 512 with two columns per lane.
 void launch_step_fused(const FusedArgs& a, int shape, cudaStream_t s);
+void launch_step_fused2(const FusedArgs& a, cudaStream_t s);
+// met fields (nx,ny,nz) -> halo layout (ghost entries untouched)
+void launch_to_halo(Dims d, int nfield, const float* const* src, float* const* dst, cudaStream_t s);
 // tiles of one class of an nx x ny grid for a tile shape
 int fused_tiles(int nx, int ny, int shape);
 
 // Batched form: the arguments of up to F3D_BATCH_MAX scenarios in constant
 // memory (c_in / c_out are the scenario's two buffers), then one persistent
 // launch over the work items of all of them.
-#define F3D_BATCH_MAX 160
+#define F3D_BATCH_MAX 128
 int upload_batch_args(const FusedArgs* h, int n, cudaStream_t s);
+int upload_batch_args2(const FusedArgs* h, int n, cudaStream_t s);  // the shape-3 kernel's table
+int fused2_batch_grid(int max_nz);
+// items [0, split) belong to scenarios with an even nx (two counters)
+void launch_step_fused2_batch(int grid, const int* item_off, int nscen, int split, int total, int* counter,
+                              const int* bstep, const int* iiter0, int commit, int max_nz, cudaStream_t s);
 // sets the kernel's shared-memory limit and returns its persistent grid (-1 on error)
 int fused_batch_grid(int shape, int max_nz);
-void launch_step_fused_batch(int shape, int grid, const int* item_off, int nscen, int* counter,
-                             const int* bstep, const int* iiter0, int commit, int max_nz, cudaStream_t s);
+// counter: two ints; split / total: see launch_step_fused2_batch (shape 3)
+void launch_step_fused_batch(int shape, int grid, const int* item_off, int nscen, int split, int total,
+                             int* counter, const int* bstep, const int* iiter0, int commit, int max_nz,
+                             cudaStream_t s);
 void launch_vk32(long long n, int nc, const float* vz, const float* vset, float* vk, cudaStream_t s);
 void launch_wet_lambda(long long n, double dt, const double* prate, double* lam, cudaStream_t s);
 void launch_fp32_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,

@@ -1,0 +1,734 @@
+// f3d_fused2.cu -- the precision form's whole transport step in one kernel,
+// two columns per lane.
+//
+// Same march as f3d_fused.cu (one CTA per tile and class, up the column;
+// iteration t: setbcc + advctzc and advctx/advcty on plane t, then diffz,
+// diffx/diffy, wetdep, accum, clip and store on plane t-1), laid out for
+// fewer instructions per cell:
+//
+//  * a lane owns two neighbouring columns, so every field of a position pair
+//    is one 64-bit value: f32x2 arithmetic, 64-bit shared-memory accesses
+//    and 8-byte asynchronous copies; an x neighbour costs one shuffle per
+//    pair instead of one per cell;
+//  * the tile region is 64 x 32 (58 x 26 output cells, 16 warps, two rows
+//    per warp), so fewer halo cells are recomputed per output cell;
+//  * the met fields come in the halo layout of c, so one offset addresses
+//    all nine staged fields of a position and interior tiles need no bounds
+//    logic at all.
+//
+// Every cell gets the bits of the scalar formulas (f3d_fused_math.cuh).
+#include <algorithm>
+#include <type_traits>
+
+#include "f3d_fused_math.cuh"
+
+namespace f3d {
+
+namespace {
+
+using namespace fz;
+
+constexpr int HX = 64, HY = 32, NW = 16, NT = 32 * NW, RPW = HY / NW, TX = HX - 6, TY = HY - 6,
+              NP = HX * HY;
+
+// value of the column to the left / right of each of the lane's two columns
+__device__ __forceinline__ float2 left2(float2 v) { return make_float2(shup(v.y), v.x); }
+__device__ __forceinline__ float2 right2(float2 v) { return make_float2(v.y, shdn(v.x)); }
+__device__ __forceinline__ float2 sel2(bool cx, bool cy, float2 a, float2 b) {
+  return make_float2(cx ? a.x : b.x, cy ? a.y : b.y);
+}
+__device__ __forceinline__ float cmp(const float2& v, int c) { return c ? v.y : v.x; }
+__device__ __forceinline__ float& cmp(float2& v, int c) { return c ? v.y : v.x; }
+
+__device__ __forceinline__ void cp_async8(unsigned dst, const float* src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 8 : 0));
+}
+__device__ __forceinline__ void cp_async4s(unsigned dst, const float* src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 4 : 0));
+}
+
+__device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void sts2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+
+size_t fused2_smem(int nz) {
+  return sizeof(float) * ((size_t)(2 * NF + 4) * NP + 2 * HX) + (2 * sizeof(double) + sizeof(int)) * TX * TY +
+         sizeof(ZT32) * (size_t)(nz + 1);
+}
+
+// One tile of one class (see fused_tile in f3d_fused.cu for the arguments).
+// P8: nx is even, so every column pair starts on an 8-byte boundary and lies
+// wholly inside or wholly outside the halo array; otherwise the pairs are
+// copied and stored one value at a time.
+template <bool P8>
+__device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_in, float* c_out, const int xfirst,
+                                            const int commit, const int cls, const int tile,
+                                            unsigned char* smem_raw) {
+  float* stage = reinterpret_cast<float*>(smem_raw) + HX;  // [2][NF][NP], after a guard row
+  float* P0s = stage + 2 * NF * NP;
+  float* W1s = P0s + NP;
+  float* W2s = W1s + NP;
+  float* P1s = W2s + NP;
+  double* wacc = reinterpret_cast<double*>(P1s + NP + HX);
+  double* wlam = wacc + TX * TY;
+  int* wkz = reinterpret_cast<int*>(wlam + TX * TY);
+  ZT32* tab = reinterpret_cast<ZT32*>(wkz + TX * TY);
+
+  const Dims d = a.d;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int tiles_x = (nx + TX - 1) / TX;
+  const int i0 = 1 + (tile % tiles_x) * TX, j0 = 1 + (tile / tiles_x) * TY;
+  const int gx0 = i0 - 3, gy0 = j0 - 3;
+  const int oi1 = min(nx, i0 + TX - 1), oj1 = min(ny, j0 + TY - 1);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gi = gx0 + 2 * lane;  // the lane's first column; the second is gi + 1
+  const int px = nx + 2;          // halo row pitch
+  const int cs = px * (ny + 2);   // halo plane
+  const int pl = nx * ny;
+  const bool edge = !(gx0 >= 1 && gx0 + HX - 1 <= nx && gy0 >= 1 && gy0 + HY - 1 <= ny);
+
+  for (int k = threadIdx.x; k <= nz; k += NT) {
+    ZT32 z;
+    const float dzk = a.dz[k];
+    const float dzkm = k > 0 ? a.dz[k - 1] : dzk;
+    z.dzz = 2.0f / (dzk + dzkm);
+    z.dzk = 1.0f / dzk;
+    z.dzk_1 = 1.0f / dzkm;
+    z.dzm1 = dzkm;
+    z.l_dz = 1.0f / dzk;
+    z.l_dzdz = 2.0f / (dzk + dzkm);
+    tab[k] = z;
+  }
+  const bool wet = a.wet_class && a.wet_class[cls];
+  for (int o = threadIdx.x; o < TX * TY; o += NT) {
+    const int oi = i0 + o % TX, oj = j0 + o / TX;
+    wacc[o] = 0.0;
+    wlam[o] = 0.0;
+    wkz[o] = 0;
+    if (!wet || oi > oi1 || oj > oj1) continue;
+    const int p2 = (oi - 1) + nx * (oj - 1);
+    wlam[o] = a.lambda2d[p2];
+    wacc[o] = a.cwet[(long long)(cls + 1) * pl + p2];
+    // zlayer is non-decreasing (checked on the host): the layers below the
+    // mixing height are a prefix of the column (wetdep.f90:37)
+    const double zi = a.zi[p2];
+    int kz = 0;
+    while (kz < nz && a.zlayer[kz] <= zi) ++kz;
+    wkz[o] = kz;
+  }
+
+  const float* __restrict__ cin = c_in + (long long)cls * a.cstride;
+  float* __restrict__ cout = c_out + (long long)cls * a.cstride;
+  const float* __restrict__ vkc = a.vkh + (long long)cls * a.cstride;
+  const float dt = a.dt;
+  const float dznz = 1.0f / a.dz[nz];
+  const float auxvx = a.auxvx, auxvy = a.auxvy;
+
+  // ------------------------------------------------ per-position state
+  // bit 2r+c: row r (gj = gy0 + warp + NW*r), column c (gi + c)
+  unsigned kin = 0, kgx = 0, kgy = 0, inr = 0;  // inr: the pair of row r lies in the halo array
+  int h0[RPW];                                  // halo offset of (gi, gj, plane 0), clamped
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    const int gj = gy0 + warp + NW * r;
+    const bool yin = gj >= 1 && gj <= ny;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int g = gi + c;
+      const bool xin = g >= 1 && g <= nx;
+      const unsigned bit = 1u << (2 * r + c);
+      if (xin && yin) kin |= bit;
+      else if ((g == 0 || g == nx + 1) && yin) kgx |= bit;
+      else if ((gj == 0 || gj == ny + 1) && xin) kgy |= bit;
+      if (g >= 0 && g <= nx + 1 && gj >= 0 && gj <= ny + 1) inr |= bit;
+    }
+    h0[r] = (inr >> (2 * r) & 1u) ? gi + px * gj : cs;  // clamped for pairs outside (plane 1 stays in range)
+  }
+  float2 o_0[RPW], o_p1[RPW], vk0[RPW], w1k[RPW], w2km[RPW], w2k[RPW], gtop[RPW];
+  float2 ra[RPW], rb[RPW], rc[RPW], fprev[RPW], gprev[RPW], pb[RPW];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    o_0[r] = o_p1[r] = vk0[r] = w1k[r] = w2km[r] = w2k[r] = gtop[r] = make_float2(0.0f, 0.0f);
+    ra[r] = rb[r] = rc[r] = fprev[r] = gprev[r] = pb[r] = make_float2(0.0f, 0.0f);
+  }
+  const unsigned sbase = (unsigned)__cvta_generic_to_shared(stage) + 4u * (unsigned)(warp * HX + 2 * lane);
+
+  // the staged inputs of iteration t into buffer t&1 (fields as in
+  // f3d_fused.cu); positions outside the halo array copy nothing (zero fill)
+  auto prefetch = [&](auto edge_c, const int t) {
+    constexpr bool EDGE = decltype(edge_c)::value;
+    const unsigned sb = sbase + 4u * (unsigned)((t & 1) * NF * NP);
+    const bool okc = t + 2 <= nz, okk = t + 1 <= nz, okm = t <= nz, okl = t >= 2;
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      const unsigned dst = sb + 4u * (unsigned)(NW * r * HX);
+      const int ht = h0[r] + t * cs;  // this row's offset at plane t
+      const bool v0 = !EDGE || (inr >> (2 * r) & 1u), v1 = !EDGE || (inr >> (2 * r + 1) & 1u);
+      auto cp = [&](int field, const float* base, int off) {
+        const unsigned dd = dst + 4u * (unsigned)(field * NP);
+        if constexpr (P8) {
+          cp_async8(dd, base + off, v0);
+        } else {  // an odd nx: a pair may straddle the last ghost column
+          cp_async4s(dd, base + off, v0);
+          cp_async4s(dd + 4u, v1 ? base + off + 1 : base + off, v1);
+        }
+      };
+      if (okc) cp(F_C, cin, ht + 2 * cs);
+      if (okk) cp(F_VK, vkc, ht + cs);
+      if (okm) {
+        cp(F_VX, a.vxh, ht);
+        cp(F_VY, a.vyh, ht);
+        cp(F_L, a.lrhoh, ht);
+        cp(F_PZ, a.pkzh, ht);
+      }
+      if (okl) {
+        cp(F_L1, a.lrhoh, ht - cs);
+        cp(F_PX, a.pkxh, ht - cs);
+        cp(F_PY, a.pkyh, ht - cs);
+      }
+    }
+    cp_async_commit();
+  };
+  if (edge)
+    prefetch(True_{}, 1);
+  else
+    prefetch(False_{}, 1);
+
+  __syncthreads();  // tables and wet state
+  // bottom ghost, first window (setbcc.f90:19-33, advctzc work(1))
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    const int gj = gy0 + warp + NW * r;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      if (!(kin >> (2 * r + c) & 1u)) continue;
+      const int g = gi + c;
+      const int hb = g + px * gj, mb = (g - 1) + nx * (gj - 1);
+      const float c1 = cin[hb + cs], c2 = cin[hb + 2 * cs];
+      const float vk1 = __ldg(vkc + hb + cs);
+      float gb;
+      if (vk1 >= 0.0f)
+        gb = 0.0f;
+      else
+        gb = c1 * (1.0f + a.dz[0] * __ldg(a.vdep + (long long)cls * a.dstride + mb) / __ldg(a.rkver1 + mb));
+      cmp(o_0[r], c) = c1;
+      cmp(o_p1[r], c) = c2;
+      cmp(vk0[r], c) = vk1;
+      float w1, w2;
+      zwork(gb, c1, c2, vk1, vk1, tab[1], dt, w1, w2);
+      cmp(w1k[r], c) = w1;
+      cmp(w2k[r], c) = w2;
+      cmp(w2km[r], c) = w2;
+      cmp(rc[r], c) = gb;
+      if (g >= i0 && g <= oi1 && gj >= j0 && gj <= oj1) {
+        cout[hb] = clip0(gb);  // clipped ghost (sizloop.f90:77)
+        if (g == 1 && gj == 1) cout[d.C(0, 0, 0)] = clip0(c1);  // setbcc.f90:87-91
+        if (g == nx && gj == 1) cout[d.C(nx + 1, 0, 0)] = clip0(c1);
+        if (g == 1 && gj == ny) cout[d.C(0, ny + 1, 0)] = clip0(c1);
+        if (g == nx && gj == ny) cout[d.C(nx + 1, ny + 1, 0)] = clip0(c1);
+      }
+    }
+  }
+
+  // ------------------------------------------------ one iteration of the march
+  auto plane = [&](auto edge_c, auto steady_c, const int t) {
+    constexpr bool EDGE = decltype(edge_c)::value;
+    constexpr bool STEADY = decltype(steady_c)::value;  // 3 <= t <= nz-2
+    cp_async_wait_all();
+    const float* sb = stage + (t & 1) * (NF * NP) + warp * HX + 2 * lane;  // this lane's row-0 position
+    auto at = [&](int field, int r) { return sb + field * NP + NW * r * HX; };
+    auto km = [&](int r, int c) { return (kin >> (2 * r + c) & 1u) != 0; };
+    float2 s2[RPW];
+    if (STEADY || t <= nz) {
+      float2 s1[RPW];
+      const ZT32 zn = tab[(STEADY || t + 1 <= nz) ? t + 1 : nz];
+      // ---------------- A: setbcc ghosts + advctzc for plane t
+#pragma unroll
+      for (int r = 0; r < RPW; ++r) {
+        const int gj = gy0 + warp + NW * r;
+        float2 ghost = make_float2(0.0f, 0.0f);
+        if constexpr (EDGE) {
+          // x-face ghosts from the neighbouring column's original c and vx (setbcc.f90:53-66)
+          const float2 cL = left2(o_0[r]), cR = right2(o_0[r]);
+          const float2 vxo = lds2(at(F_VX, r));
+          const float2 vL = left2(vxo), vR = right2(vxo);
+#pragma unroll
+          for (int c = 0; c < 2; ++c)
+            cmp(ghost, c) = (gi + c == 0) ? (cmp(vR, c) >= 0.0f ? 0.0f : cmp(cR, c))
+                                          : (cmp(vL, c) <= 0.0f ? 0.0f : cmp(cL, c));
+          if (gj == 0 || gj == ny + 1) {  // y-face ghosts (setbcc.f90:70-83)
+            const int ja = gj == 0 ? 1 : ny;
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+              const int g = gi + c;
+              float gv = 0.0f;
+              if (g >= 1 && g <= nx) {
+                const int hh = g + px * ja + t * cs;
+                const float cadj = cin[hh];
+                const float v = __ldg(a.vyh + hh);
+                gv = (gj == 0) ? (v >= 0.0f ? 0.0f : cadj) : (v <= 0.0f ? 0.0f : cadj);
+              }
+              cmp(ghost, c) = gv;
+            }
+          }
+        }
+        {  // the column update, on every position
+          float2 w1n, w2n, o_p2 = make_float2(0.0f, 0.0f), vkp = make_float2(0.0f, 0.0f);
+          if (STEADY || t + 1 <= nz) {
+            vkp = lds2(at(F_VK, r));
+            if (STEADY || t + 2 <= nz) {
+              o_p2 = lds2(at(F_C, r));
+            } else {  // the top ghost (setbcc.f90:37-49), vkp = vk(nz)
+#pragma unroll
+              for (int c = 0; c < 2; ++c) {
+                cmp(o_p2, c) = (cmp(vkp, c) <= 0.0f) ? 0.0f : cmp(o_p1[r], c);
+                const int g = gi + c;
+                if (g >= i0 && g <= oi1 && gj >= j0 && gj <= oj1) {  // an interior position
+                  const int hb = g + px * gj;
+                  const float top = cmp(o_p1[r], c);
+                  cout[hb + (nz + 1) * cs] = clip0(cmp(o_p2, c));
+                  if (g == 1 && gj == 1) cout[d.C(0, 0, nz + 1)] = clip0(top);
+                  if (g == nx && gj == 1) cout[d.C(nx + 1, 0, nz + 1)] = clip0(top);
+                  if (g == 1 && gj == ny) cout[d.C(0, ny + 1, nz + 1)] = clip0(top);
+                  if (g == nx && gj == ny) cout[d.C(nx + 1, ny + 1, nz + 1)] = clip0(top);
+                }
+              }
+              gtop[r] = o_p2;
+            }
+            zwork2(o_0[r], o_p1[r], o_p2, vkp, vk0[r], zn, dt, w1n, w2n);
+          } else {  // t == nz: work(nz+1,1) (advctzc.f90:58-64)
+            w1n = mul2(mul2(mul2(splat(dt), vk0[r]), sub2(gtop[r], o_0[r])), splat(dznz));
+            w2n = w2k[r];
+          }
+          s1[r] = line_update2(o_0[r], vk0[r], w1k[r], w1n, w2k[r], w2km[r], w2n);
+          w2km[r] = w2k[r];
+          w2k[r] = w2n;
+          w1k[r] = w1n;
+          o_0[r] = o_p1[r];
+          o_p1[r] = o_p2;
+          vk0[r] = vkp;
+        }
+        if constexpr (EDGE) {
+          const unsigned gm = (kgx | kgy) >> (2 * r);
+          s1[r] = sel2(gm & 1u, gm & 2u, ghost, s1[r]);
+        }
+      }
+      // ---------------- B: advctx (shuffles) and advcty (shared memory)
+      auto adv_x = [&](const float2* in, float2* out) {
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+          const float2 c0 = in[r];
+          const float2 v = lds2(at(F_VX, r));
+          const float2 cm = left2(c0), cp = right2(c0), vmr = left2(v);
+          float2 w1, w2;
+          if constexpr (EDGE) {
+            const float2 vm = sel2(gi == 1, gi + 1 == 1, v, vmr);  // v(max(1,q-1))
+            line_work2(cm, c0, cp, v, vm, auxvx, a.inv_dx, dt, w1, w2);
+#pragma unroll
+            for (int c = 0; c < 2; ++c)  // work(nx+1,1) (advctx.f90:46)
+              if (gi + c == nx + 1) cmp(w1, c) = auxvx * cmp(vmr, c) * (cmp(c0, c) - cmp(cm, c));
+          } else {
+            line_work2(cm, c0, cp, v, vmr, auxvx, a.inv_dx, dt, w1, w2);
+          }
+          const float2 w1p = right2(w1);
+          float2 w2m = left2(w2), w2p = right2(w2);
+          if constexpr (EDGE) {
+            w2m = sel2(gi == 1, gi + 1 == 1, w2, w2m);
+            w2p = sel2(gi == nx, gi + 1 == nx, w2, w2p);
+            const float2 u = line_update2(c0, v, w1, w1p, w2, w2m, w2p);
+            out[r] = sel2(km(r, 0), km(r, 1), u, c0);
+          } else {
+            out[r] = line_update2(c0, v, w1, w1p, w2, w2m, w2p);
+          }
+        }
+      };
+      auto adv_y = [&](const float2* in, float2* out) {
+        float* P0 = P0s + warp * HX + 2 * lane;
+        float* W1 = W1s + warp * HX + 2 * lane;
+        float* W2 = W2s + warp * HX + 2 * lane;
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) sts2(P0 + NW * r * HX, in[r]);
+        __syncthreads();
+        // every thread is past iteration t-1: its staging buffer may be refilled
+        prefetch(edge_c, t + 1);
+        float2 w1s[RPW], w2s[RPW], vs[RPW];
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+          const int gj = gy0 + warp + NW * r;
+          const float2 c0 = in[r];
+          const float2 cm = lds2(P0 + NW * r * HX - HX), cp = lds2(P0 + NW * r * HX + HX);
+          const float2 v = lds2(at(F_VY, r)), vmr = lds2(at(F_VY, r) - HX);  // vy(i, j-1)
+          vs[r] = v;
+          if constexpr (EDGE) {  // row conditions are uniform across the warp
+            line_work2(cm, c0, cp, v, gj == 1 ? v : vmr, auxvy, a.inv_dy, dt, w1s[r], w2s[r]);
+            if (gj == ny + 1) w1s[r] = mul2(mul2(splat(auxvy), vmr), sub2(c0, cm));  // advcty.f90:45
+          } else {
+            line_work2(cm, c0, cp, v, vmr, auxvy, a.inv_dy, dt, w1s[r], w2s[r]);
+          }
+          sts2(W1 + NW * r * HX, w1s[r]);
+          sts2(W2 + NW * r * HX, w2s[r]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+          const float2 w1p = lds2(W1 + NW * r * HX + HX);
+          float2 w2m = lds2(W2 + NW * r * HX - HX), w2p = lds2(W2 + NW * r * HX + HX);
+          if constexpr (EDGE) {
+            const int gj = gy0 + warp + NW * r;
+            if (gj == 1) w2m = w2s[r];
+            if (gj == ny) w2p = w2s[r];
+            const float2 u = line_update2(in[r], vs[r], w1s[r], w1p, w2s[r], w2m, w2p);
+            out[r] = sel2(km(r, 0), km(r, 1), u, in[r]);
+          } else {
+            out[r] = line_update2(in[r], vs[r], w1s[r], w1p, w2s[r], w2m, w2p);
+          }
+        }
+      };
+      float2 sa[RPW];
+      if (xfirst) {  // sizloop.f90:42-48
+        adv_x(s1, sa);
+        adv_y(sa, s2);
+      } else {
+        adv_y(s1, sa);
+        adv_x(sa, s2);
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < RPW; ++r) s2[r] = make_float2(0.0f, 0.0f);
+      __syncthreads();  // the y-sweep plane of the previous iteration is read by all warps
+    }
+    if (!STEADY && t < 2) {
+#pragma unroll
+      for (int r = 0; r < RPW; ++r) {
+        if (EDGE) gprev[r] = s2[r];  // ghost value of plane t
+        ra[r] = rb[r];
+        rb[r] = rc[r];
+        rc[r] = s2[r];
+        pb[r] = lds2(at(F_PZ, r));  // rkver*rho at plane 1
+      }
+      return;
+    }
+    // ---------------- C: diffz for plane k = t-1 (diffz.f90:22-62)
+    const int k = t - 1;
+    float2 s3[RPW], lbv[RPW];
+    const ZT32 zk = tab[k];
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      ra[r] = rb[r];
+      rb[r] = rc[r];
+      rc[r] = (STEADY || t <= nz) ? s2[r] : gtop[r];  // c(nz+1) is the top ghost (diffz.f90:54)
+      const float2 lb = lds2(at(F_L1, r));
+      lbv[r] = lb;
+      float2 work;
+      if (STEADY || (k > 1 && k < nz)) {
+        const float2 lc = lds2(at(F_L, r)), pc = lds2(at(F_PZ, r));
+        const float2 gradt =
+            mul2(mul2(mul2(splat(0.5f), add2(pc, pb[r])), sub2(mul2(rc[r], lc), mul2(rb[r], lb))), splat(zk.l_dz));
+        work = mul2(mul2(splat(dt), sub2(gradt, fprev[r])), splat(zk.l_dzdz));
+        fprev[r] = gradt;
+        pb[r] = pc;
+      } else if (k == 1) {
+        const float2 lc = lds2(at(F_L, r)), pc = lds2(at(F_PZ, r));
+        const float2 qt = sub2(mul2(rc[r], lc), mul2(rb[r], lb));
+        const float2 gradt = mul2(mul2(pc, qt), splat(tab[1].l_dz));
+        const float2 g = mul2(mul2(pb[r], sub2(mul2(rb[r], lb), mul2(ra[r], lb))), splat(tab[0].l_dz));
+        const float2 gradb = make_float2(g.x > 0.0f ? g.x : 0.0f, g.y > 0.0f ? g.y : 0.0f);  // MAX(0,g)
+        work = mul2(mul2(splat(dt), sub2(gradt, gradb)), splat(tab[1].l_dzdz));
+        fprev[r] = mul2(mul2(mul2(splat(0.5f), add2(pc, pb[r])), qt), splat(tab[1].l_dz));
+        pb[r] = pc;
+      } else {  // k == nz
+        float2 la, pa;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const bool ok = (inr >> (2 * r + c) & 1u) != 0;
+          const int hh = ok ? gi + c + px * (gy0 + warp + NW * r) + (nz - 1) * cs : 0;
+          cmp(la, c) = __ldg(a.lrhoh + hh);
+          cmp(pa, c) = __ldg(a.pkzh + hh);
+        }
+        const float2 g = mul2(mul2(pb[r], sub2(mul2(rc[r], lb), mul2(rb[r], lb))), splat(tab[nz].l_dz));
+        const float2 gradt = make_float2(g.x < 0.0f ? g.x : 0.0f, g.y < 0.0f ? g.y : 0.0f);
+        const float2 gradb = mul2(mul2(pa, sub2(mul2(rb[r], lb), mul2(ra[r], la))), splat(tab[nz - 1].l_dz));
+        work = mul2(mul2(splat(dt), sub2(gradt, gradb)), splat(tab[nz].l_dz));
+      }
+      s3[r] = add2(rb[r], work);
+      if constexpr (EDGE) {
+        s3[r] = sel2(km(r, 0), km(r, 1), s3[r], gprev[r]);  // ghosts keep their value
+        gprev[r] = s2[r];
+      }
+    }
+    // ---------------- D: diffx (shuffles) and diffy (shared memory)
+    auto dif_x = [&](const float2* in, float2* out) {
+#pragma unroll
+      for (int r = 0; r < RPW; ++r) {
+        const float2 l0 = lbv[r], P0 = lds2(at(F_PX, r)), c0 = in[r];
+        const float2 cm = left2(c0), cp = right2(c0), lm = left2(l0), lp = right2(l0), Pm = left2(P0),
+                     Pp = right2(P0);
+        float2 u = diff_mid2(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2);
+        if constexpr (EDGE) {
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            const int g = gi + c;
+            if (g == 1 || g == nx)
+              cmp(u, c) = diff_cell(g == 1, g == nx, cmp(cm, c), cmp(c0, c), cmp(cp, c), cmp(lm, c), cmp(l0, c),
+                                    cmp(lp, c), cmp(Pm, c), cmp(P0, c), cmp(Pp, c), a.dtdx2);
+          }
+          out[r] = sel2(km(r, 0), km(r, 1), u, c0);
+        } else {
+          out[r] = u;
+        }
+      }
+    };
+    auto dif_y = [&](const float2* in, float2* out) {
+      float* P1 = P1s + warp * HX + 2 * lane;
+#pragma unroll
+      for (int r = 0; r < RPW; ++r) sts2(P1 + NW * r * HX, in[r]);
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < RPW; ++r) {
+        const float* L = at(F_L1, r);
+        const float* PY = at(F_PY, r);
+        const float2 cm = lds2(P1 + NW * r * HX - HX), cp = lds2(P1 + NW * r * HX + HX);
+        const float2 lm = lds2(L - HX), lp = lds2(L + HX), Pm = lds2(PY - HX), P0 = lds2(PY), Pp = lds2(PY + HX);
+        if constexpr (EDGE) {
+          const int gj = gy0 + warp + NW * r;
+          float2 u;
+          if (gj == 1 || gj == ny) {  // uniform across the warp
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+              cmp(u, c) = diff_cell(gj == 1, gj == ny, cmp(cm, c), cmp(in[r], c), cmp(cp, c), cmp(lm, c),
+                                    cmp(lbv[r], c), cmp(lp, c), cmp(Pm, c), cmp(P0, c), cmp(Pp, c), a.dtdy2);
+          } else {
+            u = diff_mid2(cm, in[r], cp, lm, lbv[r], lp, Pm, P0, Pp, a.dtdy2);
+          }
+          out[r] = sel2(km(r, 0), km(r, 1), u, in[r]);
+        } else {
+          out[r] = diff_mid2(cm, in[r], cp, lm, lbv[r], lp, Pm, P0, Pp, a.dtdy2);
+        }
+      }
+    };
+    float2 s3a[RPW], s4[RPW];
+    if (xfirst) {  // sizloop.f90:55-61
+      dif_x(s3, s3a);
+      dif_y(s3a, s4);
+    } else {
+      dif_y(s3, s3a);
+      dif_x(s3a, s4);
+    }
+    // ---------------- E: wetdep, accum, clip, store (plane k)
+    const double dzk64 = a.dz64[k];
+    if constexpr (!EDGE && STEADY) {  // interior tile, no accum: predicated stores, no divergence
+      // the pair's columns inside the output tile (columns 3 .. 3+TX-1 of the region)
+      const bool o0 = 2 * lane >= 3 && 2 * lane < 3 + TX, o1 = 2 * lane + 1 >= 3 && 2 * lane + 1 < 3 + TX;
+#pragma unroll
+      for (int r = 0; r < RPW; ++r) {
+        const int hy = warp + NW * r;
+        if (hy < 3 || hy >= 3 + TY) continue;  // uniform across the warp
+        float2 res = s4[r];
+        if (wet) {
+          const int o = (2 * lane - 3) + TX * (hy - 3);
+          if (o0 && k <= wkz[o]) {  // wetdep (wetdep.f90:37-49)
+            wacc[o] = wacc[o] + dzk64 * wlam[o] * (double)res.x;
+            res.x = (float)((double)res.x * (1.0 - wlam[o]));
+          }
+          if (o1 && k <= wkz[o + 1]) {
+            wacc[o + 1] = wacc[o + 1] + dzk64 * wlam[o + 1] * (double)res.y;
+            res.y = (float)((double)res.y * (1.0 - wlam[o + 1]));
+          }
+        }
+        res = make_float2(clip0(res.x), clip0(res.y));
+        float* q = cout + gi + px * (gy0 + hy) + k * cs;
+        if (P8 && o0 && o1) {
+          *reinterpret_cast<float2*>(q) = res;
+        } else {
+          if (o0) q[0] = res.x;
+          if (o1) q[1] = res.y;
+        }
+      }
+      return;
+    }
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      const int hy = warp + NW * r;
+      const int gj = gy0 + hy;
+      const int hrow = gi + px * gj + k * cs;  // halo index of the first column
+      float2 res = s4[r];
+      bool st[2];
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int g = gi + c;
+        bool out_cell;
+        st[c] = false;
+        if constexpr (EDGE) {
+          const bool rows_out = gj >= j0 && gj <= oj1;
+          const bool cols_out = g >= i0 && g <= oi1;
+          const unsigned bit = 1u << (2 * r + c);
+          if (((kgx & bit) && rows_out && ((g == 0 && i0 == 1) || (g == nx + 1 && oi1 == nx))) ||
+              ((kgy & bit) && cols_out && ((gj == 0 && j0 == 1) || (gj == ny + 1 && oj1 == ny)))) {
+            cmp(res, c) = clip0(cmp(s3[r], c));  // an outer ghost keeps its setbcc value
+            st[c] = true;
+            continue;
+          }
+          out_cell = (kin & bit) && rows_out && cols_out;
+        } else {
+          const int col = 2 * lane + c;
+          out_cell = col >= 3 && col < 3 + TX && hy >= 3 && hy < 3 + TY;
+        }
+        if (!out_cell) continue;
+        float cnew = cmp(res, c);
+        if (wet) {
+          const int o = (g - i0) + TX * (gj - j0);
+          if (k <= wkz[o]) {  // wetdep (wetdep.f90:37-49)
+            wacc[o] = wacc[o] + dzk64 * wlam[o] * (double)cnew;
+            cnew = (float)((double)cnew * (1.0 - wlam[o]));
+          }
+        }
+        if (!STEADY && k == 1 && commit) {  // accum (accum.f90:17-25), binary64
+          const int mb = (g - 1) + nx * (gj - 1);
+          double* cd = a.cdry + (long long)(cls + 1) * pl + mb;
+          const double vsd = a.vset64[(long long)cls * a.vstride + mb] + a.vdep64[(long long)cls * pl + mb];
+          *cd = *cd - a.dt64 * (double)cnew * fmin2(0.0, vsd);
+        }
+        cmp(res, c) = clip0(cnew);
+        st[c] = true;
+      }
+      if (P8 && st[0] && st[1])
+        *reinterpret_cast<float2*>(cout + hrow) = res;
+      else {
+        if (st[0]) cout[hrow] = res.x;
+        if (st[1]) cout[hrow + 1] = res.y;
+      }
+    }
+  };
+
+  auto march = [&](auto edge_c) {
+    for (int t = 1; t <= 2; ++t) plane(edge_c, False_{}, t);
+    for (int t = 3; t <= nz - 2; ++t) plane(edge_c, True_{}, t);
+    for (int t = max(3, nz - 1); t <= nz + 1; ++t) plane(edge_c, False_{}, t);
+  };
+  if (edge)
+    march(True_{});
+  else
+    march(False_{});
+
+  if (wet && commit) {
+    __syncthreads();
+    for (int o = threadIdx.x; o < TX * TY; o += NT) {
+      const int oi = i0 + o % TX, oj = j0 + o / TX;
+      if (oi > oi1 || oj > oj1) continue;
+      a.cwet[(long long)(cls + 1) * pl + (oi - 1) + nx * (oj - 1)] = wacc[o];
+    }
+  }
+}
+
+template <bool P8>
+__global__ void __launch_bounds__(NT, 1) k_step_fused2(const FusedArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  fused2_tile<P8>(a, a.c_in, a.c_out, a.xfirst, 1, (int)(blockIdx.x % a.ncls), (int)(blockIdx.x / a.ncls),
+                  smem_raw);
+}
+
+// Batched form (see k_step_fused_batch in f3d_fused.cu).  The scenarios with
+// an even nx come first in the batch; their items [0, split) run in the P8
+// kernel, the rest in the other one (counter[0] and counter[1]).
+__constant__ FusedArgs c_batch2[F3D_BATCH_MAX];
+static_assert(sizeof(FusedArgs) * F3D_BATCH_MAX <= 48 * 1024, "batch argument table exceeds constant memory");
+
+template <bool P8>
+__global__ void __launch_bounds__(NT, 1)
+    k_step_fused2_batch(const int* __restrict__ item_off, int nscen, int begin, int end, int* counter,
+                        const int* __restrict__ bstep, const int* __restrict__ iiter0, int commit) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  for (;;) {
+    __syncthreads();  // the previous item is done with shared memory
+    if (threadIdx.x == 0) s_item = begin + atomicAdd(counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= end) break;
+    int lo = 0, hi = nscen;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (item_off[mid] <= item) lo = mid;
+      else hi = mid;
+    }
+    const FusedArgs& a = c_batch2[lo];
+    const int local = item - item_off[lo];
+    const int bs = bstep[lo];
+    const float* cin = (bs & 1) ? a.c_out : a.c_in;
+    float* cout = (bs & 1) ? const_cast<float*>(a.c_in) : a.c_out;
+    const int iiter = iiter0[lo] + bs + 1;
+    fused2_tile<P8>(a, cin, cout, (iiter % 2 == 0) ? 1 : 0, commit, local % a.ncls, local / a.ncls, smem_raw);
+  }
+}
+
+// met field (nx,ny,nz) -> halo layout
+__global__ void k_to_halo(Dims d, const float* src, float* dst) {
+  const long long s3 = d.cells();
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < s3;
+       m += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(m % d.nx) + 1;
+    const long long r = m / d.nx;
+    const int j = (int)(r % d.ny) + 1, k = (int)(r / d.ny) + 1;
+    dst[d.C(i, j, k)] = src[m];
+  }
+}
+
+}  // namespace
+
+void launch_step_fused2(const FusedArgs& a, cudaStream_t s) {
+  const int tiles = ((a.d.nx + TX - 1) / TX) * ((a.d.ny + TY - 1) / TY);
+  const size_t sm = fused2_smem(a.d.nz);
+  if (a.pair_aligned) {
+    cudaFuncSetAttribute(k_step_fused2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_step_fused2<true><<<tiles * a.ncls, NT, sm, s>>>(a);
+  } else {
+    cudaFuncSetAttribute(k_step_fused2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_step_fused2<false><<<tiles * a.ncls, NT, sm, s>>>(a);
+  }
+  count_launch();
+}
+
+int upload_batch_args2(const FusedArgs* h, int n, cudaStream_t s) {
+  if (n > F3D_BATCH_MAX) return 1;
+  return cudaMemcpyToSymbolAsync(c_batch2, h, sizeof(FusedArgs) * (size_t)n, 0, cudaMemcpyHostToDevice, s) ==
+                 cudaSuccess
+             ? 0
+             : 1;
+}
+
+int fused2_batch_grid(int max_nz) {
+  const size_t sm = fused2_smem(max_nz);
+  if (cudaFuncSetAttribute(k_step_fused2_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_step_fused2_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+          cudaSuccess)
+    return -1;
+  int per_sm = 0, nsm = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_fused2_batch<true>, NT, sm) != cudaSuccess)
+    return -1;
+  return per_sm < 1 ? -1 : per_sm * nsm;
+}
+
+void launch_step_fused2_batch(int grid, const int* item_off, int nscen, int split, int total, int* counter,
+                              const int* bstep, const int* iiter0, int commit, int max_nz, cudaStream_t s) {
+  const size_t sm = fused2_smem(max_nz);
+  if (split > 0) {
+    k_step_fused2_batch<true><<<grid, NT, sm, s>>>(item_off, nscen, 0, split, counter, bstep, iiter0, commit);
+    count_launch();
+  }
+  if (total > split) {
+    k_step_fused2_batch<false><<<grid, NT, sm, s>>>(item_off, nscen, split, total, counter + 1, bstep, iiter0,
+                                                     commit);
+    count_launch();
+  }
+}
+
+void launch_to_halo(Dims d, int nfield, const float* const* src, float* const* dst, cudaStream_t s) {
+  const int nb = (int)std::min<long long>((d.cells() + 255) / 256, 152LL * 16);
+  for (int f = 0; f < nfield; ++f) {
+    k_to_halo<<<nb, 256, 0, s>>>(d, src[f], dst[f]);
+    count_launch();
+  }
+}
+
+}  // namespace f3d

@@ -403,8 +403,9 @@ int f3d_run_reset(f3d_ctx* ctx);
                             with a decreasing zlayer or >= 2^31 cells per
                             class always use the per-routine kernels.     */
 #define F3D_OPT_TILE  2  /* fused kernel tile region x by y / threads:
-                            0 = 32x32/256 (default), 1 = 32x64/512,
-                            2 = 32x32/512; results do not depend on it   */
+                            0 = 32x32/256, 1 = 32x64/512, 2 = 32x32/512,
+                            3 = 64x32/512 with two columns per lane
+                            (default); results do not depend on it       */
 #define F3D_OPT_GRAPH 3  /* batches: 1 = replay one CUDA graph per batch step
                             (default), 0 = launch the kernels one by one   */
 int f3d_set_option(f3d_ctx* ctx, int key, int value);
@@ -462,8 +463,8 @@ int f3d_batch_set_option(f3d_batch* b, int key, int value);
 int f3d_batch_get_option(const f3d_batch* b, int key, int* value);
 /* Times the step kernel of the running scenarios for each tile shape (reps
  * launches each, without changing any result), keeps the fastest and
- * returns it and the per-shape milliseconds (ms[3]).  Call it after the
- * first batch step. */
+ * returns it and the per-shape milliseconds (ms[4]; -1 for a shape that
+ * does not apply).  Call it after the first batch step. */
 int f3d_batch_autotune(f3d_batch* b, int reps, int* best, float* ms);
 int f3d_batch_stats(const f3d_batch* b, long long* batch_steps,
                     double* cell_class_steps, int* n_running);

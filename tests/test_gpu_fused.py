@@ -31,13 +31,14 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("name,over", [("tiny", {}), ("small", dict(nx=61, ny=45, nz=9)),
-                                       ("small", dict(wetdep=True))])
+                                       ("small", dict(wetdep=True)),
+                                       ("small", dict(nx=150, ny=80, nz=12, wetdep=True))])
 def test_tile_shapes_agree_bitwise(name, over):
     s = synth.make_scenario(name, seed=7, **over)
     if s.grid["wetdep"]:
         s.met["prate"][:] = np.float32(3.0 / 3600.0)
     res = []
-    for tile in (0, 1, 2):
+    for tile in (0, 1, 2, 3):
         g, _ = _run(s, F.PREC_FP32, 1, tile, max_steps=12)
         f = g.fields()
         res.append((f["c"], f["cdry"], f["cwet"], g.state()["outmass"]))

@@ -18,7 +18,7 @@ def _requests():
     return [
         synth.make_scenario("small", seed=31, run_h=0.5),
         synth.make_scenario("small", seed=32, nx=44, ny=30, nz=12, nc=5, run_h=0.6, wetdep=True, M0=3e6),
-        synth.make_scenario("tiny", seed=33, nx=24, ny=20, nz=10, nc=3, run_h=0.3),
+        synth.make_scenario("tiny", seed=33, nx=25, ny=20, nz=10, nc=3, run_h=0.3),  # an odd nx
         synth.make_scenario("small", seed=34, nx=30, ny=36, nz=16, nc=4, run_h=0.4, H=6000.0),
     ]
 
