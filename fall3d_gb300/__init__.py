@@ -105,6 +105,8 @@ def load(build_if_missing: bool = False):
         "f3d_get_option": [VP, I, IP],
         "f3d_profile_enable": [VP, I],
         "f3d_profile_read": [VP, I, C.c_char_p, I, C.POINTER(C.c_longlong), DP, IP],
+        "f3d_ctx_save": [VP, C.c_char_p],
+        "f3d_ctx_restore": [VP, C.c_char_p],
         "f3d_batch_create": [I, C.POINTER(VP)],
         "f3d_batch_destroy": [VP],
         "f3d_batch_add": [VP, VP, VP, VP, D, D, I, VP, I, IP],
@@ -449,6 +451,14 @@ class Context:
                                 self.s.end_time if end_time is None else float(end_time),
                                 int(max_steps), C.addressof(recs), log_cap, C.byref(n)))
         return _abi.log_array(recs, n.value)
+
+    def save(self, path):
+        """Lossless checkpoint of the run's state (f3d_ctx_save)."""
+        _check(self.lib.f3d_ctx_save(self.h, str(path).encode()))
+
+    def restore(self, path):
+        """Restores a checkpoint; the next run() continues the saved run."""
+        _check(self.lib.f3d_ctx_restore(self.h, str(path).encode()))
 
     def run_reset(self):
         _check(self.lib.f3d_run_reset(self.h))

@@ -11,6 +11,7 @@
 // Everything of one step is enqueued on the context's stream without a host
 // synchronisation; the host keeps only the scalars of the time loop.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -37,6 +38,7 @@ namespace {
 double* small_outmass(f3d_ctx* x) { return x->small; }
 double* small_budget(f3d_ctx* x) { return x->small + 1; }
 double* small_cd(f3d_ctx* x) { return x->small + 8; }
+double* small_cd_prev(f3d_ctx* x) { return x->small + 9; }  // cd before the latest meteo update
 unsigned long long* small_dtcn(f3d_ctx* x) {
   return reinterpret_cast<unsigned long long*>(x->small + 16);
 }
@@ -474,6 +476,8 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
   const double cd0 = 1.0;  // setvset.f90:89
   if (!rc && cudaMemcpyAsync(small_cd(x), &cd0, sizeof cd0, cudaMemcpyHostToDevice, x->stream) != cudaSuccess)
     rc = f3d::ctx_error(F3D_ERR_CUDA, "upload failed");
+  if (!rc && cudaMemcpyAsync(small_cd_prev(x), &cd0, sizeof cd0, cudaMemcpyHostToDevice, x->stream) != cudaSuccess)
+    rc = f3d::ctx_error(F3D_ERR_CUDA, "upload failed");
   // LDU defaults to -99 (Master.f90:176)
   if (!rc) {
     std::vector<double> l(pl, -99.0);
@@ -534,6 +538,8 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
                 x->dz, x->zlayer, x->Hm1, x->vx, x->vy, x->vptemp, x->ustar, x->zi, x->rl, x->rkver,
                 x->rkhor, s);
   // meteo.f90:81 setvset (unscaled rho), continuing the cd chain
+  // the chain state this update starts from (a checkpoint replays the update)
+  CK(cudaMemcpyAsync(small_cd_prev(x), small_cd(x), sizeof(double), cudaMemcpyDeviceToDevice, x->stream));
   launch_setvset(d, g.nc, g.np, g.modv, x->diam, x->rhop, x->psi, x->sphe, x->tempe, x->rho,
                  g.aggregate, g.vset_factor, x->vset, x->iters, small_cd(x), x->vset_scratch,
                  small_status(x), s);
@@ -787,6 +793,104 @@ int f3d_upload_state(f3d_ctx* x, const double* c, const double* cdry, const doub
   CK(cudaMemcpyAsync(small_outmass(x), &outmass, sizeof outmass, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(small_cd(x), &cd, sizeof cd, cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));
+  return F3D_OK;
+}
+
+// ---------------------------------------------------------------- checkpoint
+// A lossless checkpoint of the state a run carries from step to step (the
+// reference's restart, wrirst.f90 / rearst.f90, keeps only c and cload in
+// binary32 and the two mass scalars).  The coefficients are not stored: the
+// restored run replays the meteo and source updates of the current
+// intervals from the drag-coefficient chain state they started from, which
+// rebuilds them bit for bit, so a restored run continues exactly as the
+// uninterrupted one.
+namespace {
+struct CkptHeader {
+  char magic[8];
+  int version, nx, ny, nz, nc, precision, iiter, pad;
+  double time, erumass, outmass, cd_prev;
+};
+const char kCkptMagic[8] = {'F', '3', 'D', 'C', 'K', 'P', 'T', '1'};
+}  // namespace
+
+int f3d_ctx_save(f3d_ctx* x, const char* path) {
+  if (!x || !path) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  const Dims d = x->d;
+  const size_t hb = (size_t)d.halo() * x->g.nc, pl2 = (size_t)d.plane() * (x->g.nc + 1);
+  const size_t esz = x->prec == F3D_PREC_FP32 ? sizeof(float) : sizeof(double);
+  CkptHeader h{};
+  memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.nx = d.nx;
+  h.ny = d.ny;
+  h.nz = d.nz;
+  h.nc = x->g.nc;
+  h.precision = x->prec;
+  h.iiter = x->iiter;
+  h.time = x->time;
+  h.erumass = x->erumass;
+  std::vector<unsigned char> c(hb * esz);
+  std::vector<double> cdry(pl2), cwet(pl2);
+  cudaStream_t s = x->stream;
+  CK(cudaMemcpyAsync(&h.outmass, small_outmass(x), sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&h.cd_prev, small_cd_prev(x), sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(c.data(), x->prec == F3D_PREC_FP32 ? (const void*)x->c32 : (const void*)x->c64, hb * esz,
+                     cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(cdry.data(), x->cdry, pl2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(cwet.data(), x->cwet, pl2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  FILE* f = fopen(path, "wb");
+  if (!f) return f3d::ctx_error(F3D_ERR_ARG, "cannot open the checkpoint file for writing");
+  bool ok = fwrite(&h, sizeof h, 1, f) == 1 && fwrite(c.data(), 1, c.size(), f) == c.size() &&
+            fwrite(cdry.data(), sizeof(double), pl2, f) == pl2 && fwrite(cwet.data(), sizeof(double), pl2, f) == pl2;
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) return f3d::ctx_error(F3D_ERR_ARG, "checkpoint write failed");
+  return F3D_OK;
+}
+
+int f3d_ctx_restore(f3d_ctx* x, const char* path) {
+  if (!x || !path) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  FILE* f = fopen(path, "rb");
+  if (!f) return f3d::ctx_error(F3D_ERR_ARG, "cannot open the checkpoint file");
+  CkptHeader h{};
+  const Dims d = x->d;
+  bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, kCkptMagic, 8) == 0 && h.version == 1;
+  if (!ok) {
+    fclose(f);
+    return f3d::ctx_error(F3D_ERR_ARG, "not a checkpoint of this library");
+  }
+  if (h.nx != d.nx || h.ny != d.ny || h.nz != d.nz || h.nc != x->g.nc || h.precision != x->prec) {
+    fclose(f);
+    return f3d::ctx_error(F3D_ERR_ARG, "checkpoint of a different grid, class count or precision");
+  }
+  const size_t hb = (size_t)d.halo() * x->g.nc, pl2 = (size_t)d.plane() * (x->g.nc + 1);
+  const size_t esz = x->prec == F3D_PREC_FP32 ? sizeof(float) : sizeof(double);
+  std::vector<unsigned char> c(hb * esz);
+  std::vector<double> cdry(pl2), cwet(pl2);
+  ok = fread(c.data(), 1, c.size(), f) == c.size() && fread(cdry.data(), sizeof(double), pl2, f) == pl2 &&
+       fread(cwet.data(), sizeof(double), pl2, f) == pl2;
+  fclose(f);
+  if (!ok) return f3d::ctx_error(F3D_ERR_ARG, "truncated checkpoint file");
+  cudaStream_t s = x->stream;
+  CK(cudaMemcpyAsync(x->prec == F3D_PREC_FP32 ? (void*)x->c32 : (void*)x->c64, c.data(), hb * esz,
+                     cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(x->cdry, cdry.data(), pl2 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(x->cwet, cwet.data(), pl2 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(small_outmass(x), &h.outmass, sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(small_cd(x), &h.cd_prev, sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(small_cd_prev(x), &h.cd_prev, sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  x->time = h.time;
+  x->iiter = h.iiter;
+  x->erumass = h.erumass;
+  // the next f3d_run replays the updates of the current meteo and source
+  // intervals (Fall3d.f90:83-101 select them from the time)
+  x->run_started = 1;
+  x->meteo_time = h.time;
+  x->source_time = h.time;
+  x->meteotime = 1;
+  x->sourcetime = 1;
+  x->have_met = 0;
   return F3D_OK;
 }
 

@@ -397,6 +397,17 @@ int f3d_run(f3d_ctx* ctx, const f3d_met_series* met,
  * called repeatedly to continue (each call resumes where the last ended). */
 int f3d_run_reset(f3d_ctx* ctx);
 
+/* Lossless checkpoint of a run's state (c in the context's precision, cdry,
+ * cwet, time, iiter, erumass, outmass and the settling-velocity chain state)
+ * to a file, and its restore into a context created with the same grid and
+ * precision.  Replaces the reference's restart (Sources/wrirst.f90:1,
+ * Sources/rearst.f90:1: c and cload in binary32, no chain state).  After
+ * f3d_ctx_restore, f3d_run with the run's met and source series continues
+ * exactly as the uninterrupted run: it replays the current meteo and source
+ * updates from the saved chain state, which rebuilds every coefficient. */
+int f3d_ctx_save(f3d_ctx* ctx, const char* path);
+int f3d_ctx_restore(f3d_ctx* ctx, const char* path);
+
 /* Options of a context (f3d_set_option / f3d_get_option). */
 #define F3D_OPT_FUSED 1  /* FP32 form: 1 = one fused kernel per step (default),
                             0 = one kernel per reference routine.  Grids
