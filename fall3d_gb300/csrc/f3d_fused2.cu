@@ -460,6 +460,14 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
         const float2 l0 = lbv[r], P0 = lds2(at(F_PX, r)), c0 = in[r];
+        if constexpr (!EDGE) {
+          // the face flux 0.5*(P(q)+P(q+1))*(c(q+1)/rho(q+1) - c(q)/rho(q)) is gradr at q and
+          // gradl at q+1 (diffx.f90:34-40): computed once per face, the left one by shuffle
+          const float2 q0 = mul2(c0, l0);
+          const float2 fr = mul2(mul2(splat(0.5f), add2(right2(P0), P0)), sub2(right2(q0), q0));
+          out[r] = add2(c0, mul2(splat(a.dtdx2), sub2(fr, left2(fr))));
+          continue;
+        }
         const float2 cm = left2(c0), cp = right2(c0), lm = left2(l0), lp = right2(l0), Pm = left2(P0),
                      Pp = right2(P0);
         float2 u = diff_mid2(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2);
@@ -479,6 +487,28 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     };
     auto dif_y = [&](const float2* in, float2* out) {
       float* P1 = P1s + warp * HX + 2 * lane;
+      if constexpr (!EDGE) {
+        // neighbours read c/rho: the products c*(1/rho) of diffy.f90:34-40,
+        // each computed once by its owner
+        float2 q[RPW];
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+          q[r] = mul2(in[r], lbv[r]);
+          sts2(P1 + NW * r * HX, q[r]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+          const float* PY = at(F_PY, r);
+          const float2 Pm = lds2(PY - HX), P0 = lds2(PY), Pp = lds2(PY + HX);
+          const float2 gradr =
+              mul2(mul2(splat(0.5f), add2(Pp, P0)), sub2(lds2(P1 + NW * r * HX + HX), q[r]));
+          const float2 gradl =
+              mul2(mul2(splat(0.5f), add2(P0, Pm)), sub2(q[r], lds2(P1 + NW * r * HX - HX)));
+          out[r] = add2(in[r], mul2(splat(a.dtdy2), sub2(gradr, gradl)));
+        }
+        return;
+      }
 #pragma unroll
       for (int r = 0; r < RPW; ++r) sts2(P1 + NW * r * HX, in[r]);
       __syncthreads();
