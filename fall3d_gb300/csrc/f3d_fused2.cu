@@ -154,10 +154,18 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
 
   // the staged inputs of iteration t into buffer t&1 (fields as in
   // f3d_fused.cu); positions outside the halo array copy nothing (zero fill)
-  auto prefetch = [&](auto edge_c, const int t) {
+  // group 0: the fields the advection phases read (c, vz+vset, vx, vy);
+  // group 1: those the diffusion phases read (1/rho, K*rho); 2: both.
+  // Group 0 of iteration t+1 is issued as iteration t starts where every
+  // warp has passed the last barrier of iteration t-1 (after which nobody
+  // reads those fields of that buffer), group 1 after the first barrier of
+  // iteration t.
+  auto prefetch = [&](auto edge_c, const int t, const int group) {
     constexpr bool EDGE = decltype(edge_c)::value;
     const unsigned sb = sbase + 4u * (unsigned)((t & 1) * NF * NP);
-    const bool okc = t + 2 <= nz, okk = t + 1 <= nz, okm = t <= nz, okl = t >= 2;
+    const bool g0 = group != 1, g1 = group != 0;
+    const bool okc = g0 && t + 2 <= nz, okk = g0 && t + 1 <= nz, okv = g0 && t <= nz, okm = g1 && t <= nz,
+               okl = g1 && t >= 2;
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
       const unsigned dst = sb + 4u * (unsigned)(NW * r * HX);
@@ -174,9 +182,11 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
       };
       if (okc) cp(F_C, cin, ht + 2 * cs);
       if (okk) cp(F_VK, vkc, ht + cs);
-      if (okm) {
+      if (okv) {
         cp(F_VX, a.vxh, ht);
         cp(F_VY, a.vyh, ht);
+      }
+      if (okm) {
         cp(F_L, a.lrhoh, ht);
         cp(F_PZ, a.pkzh, ht);
       }
@@ -189,9 +199,9 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     cp_async_commit();
   };
   if (edge)
-    prefetch(True_{}, 1);
+    prefetch(True_{}, 1, 2);
   else
-    prefetch(False_{}, 1);
+    prefetch(False_{}, 1, 2);
 
   __syncthreads();  // tables and wet state
   // bottom ghost, first window (setbcc.f90:19-33, advctzc work(1))
@@ -234,6 +244,10 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     constexpr bool EDGE = decltype(edge_c)::value;
     constexpr bool STEADY = decltype(steady_c)::value;  // 3 <= t <= nz-2
     cp_async_wait_all();
+    // from iteration 3 on, the previous iteration ended with the diffy
+    // barrier, after which no warp reads its advection fields
+    const bool early = STEADY || (t >= 3 && t <= nz);
+    if (early) prefetch(edge_c, t + 1, 0);
     const float* sb = stage + (t & 1) * (NF * NP) + warp * HX + 2 * lane;  // this lane's row-0 position
     auto at = [&](int field, int r) { return sb + field * NP + NW * r * HX; };
     auto km = [&](int r, int c) { return (kin >> (2 * r + c) & 1u) != 0; };
@@ -349,7 +363,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
         for (int r = 0; r < RPW; ++r) sts2(P0 + NW * r * HX, in[r]);
         __syncthreads();
         // every thread is past iteration t-1: its staging buffer may be refilled
-        prefetch(edge_c, t + 1);
+        prefetch(edge_c, t + 1, early ? 1 : 2);
         float2 w1s[RPW], w2s[RPW], vs[RPW];
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
