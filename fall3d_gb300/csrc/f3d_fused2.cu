@@ -99,6 +99,9 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     tab[k] = z;
   }
   const bool wet = a.wet_class && a.wet_class[cls];
+  __shared__ int s_kzmax;  // the highest wet layer of the tile: above it the wet code is skipped
+  if (threadIdx.x == 0) s_kzmax = 0;
+  __syncthreads();
   for (int o = threadIdx.x; o < TX * TY; o += NT) {
     const int oi = i0 + o % TX, oj = j0 + o / TX;
     wacc[o] = 0.0;
@@ -114,6 +117,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     int kz = 0;
     while (kz < nz && a.zlayer[kz] <= zi) ++kz;
     wkz[o] = kz;
+    if (kz > 0) atomicMax(&s_kzmax, kz);
   }
 
   const float* __restrict__ cin = c_in + (long long)cls * a.cstride;
@@ -567,7 +571,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
         const int hy = warp + NW * r;
         if (hy < 3 || hy >= 3 + TY) continue;  // uniform across the warp
         float2 res = s4[r];
-        if (wet) {
+        if (wet && k <= s_kzmax) {  // uniform across the block
           const int o = (2 * lane - 3) + TX * (hy - 3);
           if (o0 && k <= wkz[o]) {  // wetdep (wetdep.f90:37-49)
             wacc[o] = wacc[o] + dzk64 * wlam[o] * (double)res.x;
@@ -618,7 +622,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
         }
         if (!out_cell) continue;
         float cnew = cmp(res, c);
-        if (wet) {
+        if (wet && k <= s_kzmax) {
           const int o = (g - i0) + TX * (gj - j0);
           if (k <= wkz[o]) {  // wetdep (wetdep.f90:37-49)
             wacc[o] = wacc[o] + dzk64 * wlam[o] * (double)cnew;
