@@ -517,12 +517,14 @@ int f3d_setsrc(double* c, const int* nx, const int* ny, const int* nz, const int
   const int* di = m.arr(isrc, (size_t)n, false);
   const int* dj = m.arr(jsrc, (size_t)n, false);
   const int* dk = m.arr(ksrc, (size_t)n, false);
+  const std::vector<int> link = source_links(n, hi.data(), hj.data(), hk.data(), *nz);
+  const int* dln = m.arr(link.data(), link.size(), false);
   const double* dtm = m.arr(tmrat, (size_t)n * *nc, false);
   const double* ddz = m.arr(dz, (size_t)(*nz + 1), false);
   const double* dzl = m.arr(zlayer, (size_t)*nz, false);
   const double* dh = m.arr(Hm1, (size_t)d.plane(), false);
   if (m.error()) return m.error();
-  launch_setsrc<double>(dc, d.halo(), d, *nc, n, di, dj, dk, dtm, ddz, dzl, dh, *dX1, *dX2, *dt, 0);
+  launch_setsrc<double>(dc, d.halo(), d, *nc, n, di, dj, dk, dln, dtm, ddz, dzl, dh, *dX1, *dX2, *dt, 0);
   return m.finish();
 }
 

@@ -74,7 +74,7 @@ struct f3d_batch {
   cudaEvent_t ev = nullptr;  // hands a finished scenario's context back to its own stream
   bool tables_dirty = true, graph_dirty = true;
   int use_graph = 1;
-  int shape = 0, grid = 0, max_nz = 0, max_nc = 0;
+  int shape = 0, grid = 0, max_nz = 0, max_nc = 0, max_nsou = 0;
   int split = 0, total = 0;  // items of the even-nx scenarios come first (shape 3)
   int graph_kernels = 0;     // kernels in one replay of the graph
   long long batch_steps = 0;
@@ -94,6 +94,8 @@ int table_rebuild(f3d_batch* b) {
   b->split = -1;
   b->max_nz = 0;
   b->max_nc = 0;
+  const int nsou_blocks = (b->max_nsou + 127) / 128;
+  b->max_nsou = 0;
   for (int q = 0; q < n; ++q) {
     Scen& s = b->slot[b->active[q]];
     f3d_ctx* x = s.x;
@@ -113,6 +115,7 @@ int table_rebuild(f3d_batch* b) {
     u.isrc = x->isrc;
     u.jsrc = x->jsrc;
     u.ksrc = x->ksrc;
+    u.link = x->slink;
     u.tmrat = x->tmrat;
     u.dz = x->dz;
     u.zlayer = x->zlayer;
@@ -124,9 +127,6 @@ int table_rebuild(f3d_batch* b) {
     u.vz = x->vz;
     u.vset = x->vset;
     u.outmass = ctx_outmass(x);
-    u.n1 = 2LL * x->g.nc * x->g.ny * x->g.nz;
-    u.n2 = 2LL * x->g.nc * x->g.nx * x->g.nz;
-    u.n3 = (long long)x->g.nc * x->g.nx * x->g.ny;
     if (b->split < 0 && (x->g.nx & 1)) b->split = off;
     b->h_item_off[q] = off;
     off += fused_tiles(x->g.nx, x->g.ny, b->shape) * x->g.nc;
@@ -134,7 +134,9 @@ int table_rebuild(f3d_batch* b) {
     b->h_iiter0[q] = s.iiter0;
     b->max_nz = std::max(b->max_nz, x->g.nz);
     b->max_nc = std::max(b->max_nc, x->g.nc);
+    b->max_nsou = std::max(b->max_nsou, x->nsou);
   }
+  if ((b->max_nsou + 127) / 128 != nsou_blocks) b->graph_dirty = true;  // setsrc's grid changed
   b->h_item_off[n] = off;
   b->total = off;
   if (b->split < 0) b->split = off;
@@ -154,7 +156,7 @@ int table_rebuild(f3d_batch* b) {
 int enqueue_step(f3d_batch* b, int commit_only_fused) {
   const int n = (int)b->active.size();
   BK(cudaMemsetAsync(b->d_counter, 0, 2 * sizeof(int), b->stream));
-  if (!commit_only_fused) launch_setsrc_batch(b->d_aux, b->d_bstep, n, b->max_nc, b->stream);
+  if (!commit_only_fused) launch_setsrc_batch(b->d_aux, b->d_bstep, n, b->max_nc, b->max_nsou, b->stream);
   launch_step_fused_batch(b->shape, b->grid, b->d_item_off, n, b->split, b->total, b->d_counter, b->d_bstep,
                           b->d_iiter0, commit_only_fused ? 0 : 1, b->max_nz, b->stream);
   if (!commit_only_fused) {

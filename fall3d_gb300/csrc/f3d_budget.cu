@@ -83,83 +83,112 @@ size_t reduce_scratch_bytes(long long nterms, int nsums) {
 
 // ----------------------------------------------------------- cmass2d
 // Terms of Sources/cmass2d.f90:42-102: x faces (ic, j, k, left/right),
-// y faces (ic, i, k, down/up), top (ic, i, j).
+// y faces (ic, i, k, down/up), top (ic, i, j).  The work is split by face
+// cell ("item"): an item computes its class-independent factor
+// (dt*area)*velo (faces) or dt*area (top) once and walks the classes, so
+// each term is still ((dt*area)*velo)*conc rounded as the reference writes
+// it.  Items: [0, nT) top (i fastest), then x faces (j fastest, left half
+// first), then y faces (i fastest, down half first).
+struct Cm2Items {
+  int nT, nX, nY;  // top items, x-face items, y-face items
+};
+__host__ __device__ inline Cm2Items cm2_items(const Dims& d, int iz_loc, int nz_loc) {
+  Cm2Items r;
+  r.nT = (iz_loc + nz_loc - 1 == d.nz) ? d.nx * d.ny : 0;
+  r.nX = 2 * d.ny * nz_loc;
+  r.nY = 2 * d.nx * nz_loc;
+  return r;
+}
+
+// Cascaded TwoSum (Ogita, Rump and Oishi, "Accurate sum and dot product",
+// SIAM J. Sci. Comput. 26 (2005), Algorithm 4.4): s carries the running
+// binary64 sum, e the exact rounding errors of its additions summed in
+// binary64; s + e is as accurate as a sum in twice the working precision.
+struct DS {
+  double s, e;
+};
+__device__ __forceinline__ void ds_add(DS& a, double b) {
+  const double s = a.s + b;
+  const double bb = s - a.s;
+  a.e = a.e + ((a.s - (s - bb)) + (b - bb));
+  a.s = s;
+}
+__device__ __forceinline__ DD ds_dd(DS a) {
+  const double hi = a.s + a.e;
+  return DD{hi, a.e - (hi - a.s)};
+}
+
 template <class T>
-__device__ __forceinline__ double cmass2d_term(long long t, const T* c, const double* vx,
-                                               const double* vy, const double* vz, const double* vset,
-                                               const Dims& d, int ic_loc, int iz_loc, int nz_loc,
-                                               double dx, double dy, const double* dz, double dt,
-                                               long long n1, long long n2) {
+__device__ __forceinline__ void cmass2d_item(int u, const Cm2Items& it, const T* c, const double* vx,
+                                             const double* vy, const double* vz, const double* vset,
+                                             const Dims& d, int ic_loc, int nc_loc, int iz_loc,
+                                             int nz_loc, double dx, double dy, const double* dz,
+                                             double dt, DS& acc) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const long long hb = d.halo(), s3 = d.cells();
-  double term;
-  if (t < n1) {
-    const int side = (int)(t & 1);
-    long long r = t >> 1;
-    const int k = (int)(r % nz_loc) + iz_loc;
-    r /= nz_loc;
-    const int j = (int)(r % ny) + 1;
-    const int ic = (int)(r / ny) + ic_loc;
-    double faty = 1.0;
-    if (j == 1 || j == ny) faty = 0.5;
-    const double area = faty * dy * 0.5 * (dz[k] + dz[k - 1]);
-    const T* cc = c + (long long)(ic - 1) * hb;
-    if (side == 0) {
-      const double velo = vx[d.M(1, j, k)], conc = (double)cc[d.C(0, j, k)];
-      term = -(dt * area * velo * conc);
-    } else {
-      const double velo = vx[d.M(nx, j, k)], conc = (double)cc[d.C(nx + 1, j, k)];
-      term = dt * area * velo * conc;
-    }
-  } else if (t < n1 + n2) {
-    const long long u = t - n1;
-    const int side = (int)(u & 1);
-    long long r = u >> 1;
-    const int k = (int)(r % nz_loc) + iz_loc;
-    r /= nz_loc;
-    const int i = (int)(r % nx) + 1;
-    const int ic = (int)(r / nx) + ic_loc;
-    double fatx = 1.0;
-    if (i == 1 || i == nx) fatx = 0.5;
-    const double area = fatx * dx * 0.5 * (dz[k] + dz[k - 1]);
-    const T* cc = c + (long long)(ic - 1) * hb;
-    if (side == 0) {
-      const double velo = vy[d.M(i, 1, k)], conc = (double)cc[d.C(i, 0, k)];
-      term = -(dt * area * velo * conc);
-    } else {
-      const double velo = vy[d.M(i, ny, k)], conc = (double)cc[d.C(i, ny + 1, k)];
-      term = dt * area * velo * conc;
-    }
-  } else {
-    long long r = t - n1 - n2;
-    const int i = (int)(r % nx) + 1;
-    r /= nx;
-    const int j = (int)(r % ny) + 1;
-    const int ic = (int)(r / ny) + ic_loc;
+  const T* c0 = c + (long long)(ic_loc - 1) * hb;
+  if (u < it.nT) {
+    const int i = u % nx + 1, j = u / nx + 1;
     double faty = 1.0;
     if (j == 1 || j == ny) faty = 0.5;
     double fatx = 1.0;
     if (i == 1 || i == nx) fatx = 0.5;
     const double area = fatx * faty * dx * dy;
-    const double velo = vz[d.M(i, j, nz)] + vset[(long long)(ic - 1) * s3 + d.M(i, j, nz)];
-    const double conc = (double)c[(long long)(ic - 1) * hb + d.C(i, j, nz + 1)];
-    term = dt * area * velo * conc;
+    const double da = dt * area;
+    const long long m = d.M(i, j, nz);
+    const double w = vz[m];
+    const double* vs = vset + (long long)(ic_loc - 1) * s3 + m;
+    const T* cc = c0 + d.C(i, j, nz + 1);
+    for (int q = 0; q < nc_loc; ++q) {
+      const double velo = w + vs[q * s3];
+      ds_add(acc, da * velo * (double)cc[q * hb]);
+    }
+    return;
   }
-  return term;
+  u -= it.nT;
+  if (u < it.nX) {
+    const int half = it.nX / 2, side = u >= half;
+    const int v = side ? u - half : u;
+    const int j = v % ny + 1, k = v / ny + iz_loc;
+    double faty = 1.0;
+    if (j == 1 || j == ny) faty = 0.5;
+    const double area = faty * dy * 0.5 * (dz[k] + dz[k - 1]);
+    const double w = dt * area * vx[d.M(side ? nx : 1, j, k)];
+    const T* cc = c0 + d.C(side ? nx + 1 : 0, j, k);
+    for (int q = 0; q < nc_loc; ++q) {
+      const double t = w * (double)cc[q * hb];
+      ds_add(acc, side ? t : -t);
+    }
+    return;
+  }
+  u -= it.nX;
+  const int half = it.nY / 2, side = u >= half;
+  const int v = side ? u - half : u;
+  const int i = v % nx + 1, k = v / nx + iz_loc;
+  double fatx = 1.0;
+  if (i == 1 || i == nx) fatx = 0.5;
+  const double area = fatx * dx * 0.5 * (dz[k] + dz[k - 1]);
+  const double w = dt * area * vy[d.M(i, side ? ny : 1, k)];
+  const T* cc = c0 + d.C(i, side ? ny + 1 : 0, k);
+  for (int q = 0; q < nc_loc; ++q) {
+    const double t = w * (double)cc[q * hb];
+    ds_add(acc, side ? t : -t);
+  }
 }
 
 template <class T>
 __global__ void k_cmass2d(const T* c, const double* vx, const double* vy, const double* vz,
                           const double* vset, Dims d, int ic_loc, int nc_loc, int iz_loc,
                           int nz_loc, double dx, double dy, const double* dz, double dt,
-                          long long n1, long long n2, long long n3, DD* partial) {
-  DD acc[1] = {dd_zero()};
-  const long long ntot = n1 + n2 + n3;
-  for (long long t = blockIdx.x * (long long)RB + threadIdx.x; t < ntot;
-       t += (long long)gridDim.x * RB)
-    acc[0] = dd_add_d(acc[0], cmass2d_term<T>(t, c, vx, vy, vz, vset, d, ic_loc, iz_loc, nz_loc, dx, dy,
-                                              dz, dt, n1, n2));
-  block_store_dd<1>(acc, partial);
+                          DD* partial) {
+  const Cm2Items it = cm2_items(d, iz_loc, nz_loc);
+  const int ntot = it.nT + it.nX + it.nY;
+  DS acc{0.0, 0.0};
+  for (int u = blockIdx.x * RB + threadIdx.x; u < ntot; u += gridDim.x * RB)
+    cmass2d_item<T>(u, it, c, vx, vy, vz, vset, d, ic_loc, nc_loc, iz_loc, nz_loc, dx, dy, dz, dt,
+                    acc);
+  DD v[1] = {ds_dd(acc)};
+  block_store_dd<1>(v, partial);
 }
 
 // Batched form: scenario blockIdx.y, its outflow summed over gridDim.x
@@ -168,13 +197,15 @@ __global__ void k_cmass2d(const T* c, const double* vx, const double* vy, const 
 __global__ void k_cmass2d_batch(const BatchAux* tab, const int* bstep, DD* partial) {
   const BatchAux& b = tab[blockIdx.y];
   const float* c = (bstep[blockIdx.y] & 1) ? b.c_a : b.c_b;
-  DD acc[1] = {dd_zero()};
-  const long long ntot = b.n1 + b.n2 + b.n3;
-  for (long long t = blockIdx.x * (long long)RB + threadIdx.x; t < ntot;
-       t += (long long)gridDim.x * RB)
-    acc[0] = dd_add_d(acc[0], cmass2d_term<float>(t, c, b.vx, b.vy, b.vz, b.vset, b.d, 1, 1, b.d.nz, b.dX1,
-                                                  b.dX2, b.dz, b.dt, b.n1, b.n2));
-  block_store_dd<1>(acc, partial + (long long)blockIdx.y * gridDim.x);
+  const Dims d = b.d;
+  const Cm2Items it = cm2_items(d, 1, d.nz);
+  const int ntot = it.nT + it.nX + it.nY;
+  DS acc{0.0, 0.0};
+  for (int u = blockIdx.x * RB + threadIdx.x; u < ntot; u += gridDim.x * RB)
+    cmass2d_item<float>(u, it, c, b.vx, b.vy, b.vz, b.vset, d, 1, b.nc, 1, d.nz, b.dX1, b.dX2, b.dz,
+                        b.dt, acc);
+  DD v[1] = {ds_dd(acc)};
+  block_store_dd<1>(v, partial + (long long)blockIdx.y * gridDim.x);
 }
 
 // outmass = outmass + sum (cmass2d.f90:104), one block per scenario
@@ -200,13 +231,11 @@ void launch_cmass2d(const T* c, const double* vx, const double* vy, const double
                     const double* vset, Dims d, int ic_loc, int nc_loc, int iz_loc, int nz_loc,
                     double dx, double dy, const double* dz, double dt, void* scratch,
                     double* out, cudaStream_t s) {
-  const long long n1 = 2LL * nc_loc * d.ny * nz_loc;
-  const long long n2 = 2LL * nc_loc * d.nx * nz_loc;
-  const long long n3 = (iz_loc + nz_loc - 1 == d.nz) ? (long long)nc_loc * d.nx * d.ny : 0;
-  const int nb = reduce_blocks(n1 + n2 + n3);
+  const Cm2Items it = cm2_items(d, iz_loc, nz_loc);
+  const int nb = reduce_blocks((long long)it.nT + it.nX + it.nY);
   DD* partial = reinterpret_cast<DD*>(scratch);
   k_cmass2d<T><<<nb, RB, 0, s>>>(c, vx, vy, vz, vset, d, ic_loc, nc_loc, iz_loc, nz_loc, dx, dy, dz,
-                                 dt, n1, n2, n3, partial);
+                                 dt, partial);
   k_reduce_finish<1><<<1, RB, 0, s>>>(partial, nb, 1.0, 1.0, out, 1);
   count_launch(2);
 }

@@ -639,12 +639,15 @@ int f3d_source(f3d_ctx* x, int nsou, const int* isrc, const int* jsrc, const int
     int rc = dalloc(x, &x->isrc, cap);
     if (!rc) rc = dalloc(x, &x->jsrc, cap);
     if (!rc) rc = dalloc(x, &x->ksrc, cap);
+    if (!rc) rc = dalloc(x, &x->slink, 2 * (size_t)cap);
     if (!rc) rc = dalloc(x, &x->tmrat, (size_t)cap * nc);
     if (rc) return rc;
     x->src_cap = cap;
   }
   x->nsou = nsou;
   if (nsou > 0) {
+    const std::vector<int> link = f3d::source_links(nsou, hi.data(), hj.data(), hk.data(), nz);
+    CK(cudaMemcpyAsync(x->slink, link.data(), sizeof(int) * 2 * nsou, cudaMemcpyHostToDevice, x->stream));
     CK(cudaMemcpyAsync(x->isrc, hi.data(), sizeof(int) * nsou, cudaMemcpyHostToDevice, x->stream));
     CK(cudaMemcpyAsync(x->jsrc, hj.data(), sizeof(int) * nsou, cudaMemcpyHostToDevice, x->stream));
     CK(cudaMemcpyAsync(x->ksrc, hk.data(), sizeof(int) * nsou, cudaMemcpyHostToDevice, x->stream));
@@ -664,12 +667,12 @@ int f3d_step(f3d_ctx* x) {
   if (x->prof) prof_drain(x);  // bounded event backlog: resolve the previous step
   if (x->prec == F3D_PREC_FP32) {
     ProfScope ps(x, "setsrc");
-    launch_setsrc<float>(x->c32, d.halo(), d, x->g.nc, x->nsou, x->isrc, x->jsrc, x->ksrc, x->tmrat,
-                         x->dz, x->zlayer, x->Hm1, x->g.dX1, x->g.dX2, x->dt, x->stream);
+    launch_setsrc<float>(x->c32, d.halo(), d, x->g.nc, x->nsou, x->isrc, x->jsrc, x->ksrc, x->slink,
+                         x->tmrat, x->dz, x->zlayer, x->Hm1, x->g.dX1, x->g.dX2, x->dt, x->stream);
   } else {
     ProfScope ps(x, "setsrc");
-    launch_setsrc<double>(x->c64, d.halo(), d, x->g.nc, x->nsou, x->isrc, x->jsrc, x->ksrc, x->tmrat,
-                          x->dz, x->zlayer, x->Hm1, x->g.dX1, x->g.dX2, x->dt, x->stream);
+    launch_setsrc<double>(x->c64, d.halo(), d, x->g.nc, x->nsou, x->isrc, x->jsrc, x->ksrc, x->slink,
+                          x->tmrat, x->dz, x->zlayer, x->Hm1, x->g.dX1, x->g.dX2, x->dt, x->stream);
   }
   if (x->prec == F3D_PREC_FP32 && x->opt_fused && x->fused_ok)
     sizloop_fused(x);

@@ -48,6 +48,7 @@ struct f3d_ctx {
   int fused_ok = 1;
   // sources
   int *isrc = nullptr, *jsrc = nullptr, *ksrc = nullptr;
+  int* slink = nullptr;  // source_links of the current sources (2 * nsou)
   double* tmrat = nullptr;
   int src_cap = 0, nsou = 0;
   // scratch

@@ -7,6 +7,9 @@
 
 #include <cuda_runtime.h>
 
+#include <unordered_map>
+#include <vector>
+
 #include "f3d_common.cuh"
 
 namespace f3d {
@@ -50,11 +53,35 @@ void launch_accum(const T* c, long long cstride, double* cdry, int ic0, Dims d, 
                   long long dstride, int ncls, cudaStream_t s);
 template <class T>
 void launch_clip(T* c, long long n, cudaStream_t s);
+// setsrc.f90:20-35 adds the sources in file order; only sources in one
+// cell need that order.  source_links gives link[0..n) = the next source in
+// the same cell (-1: none) and link[n..2n) = 1 for the first source of its
+// cell, so that one thread per first source walks its cell's chain; sources
+// with k outside 1..nz are in no chain (the reference skips them).
+inline std::vector<int> source_links(int n, const int* isrc, const int* jsrc, const int* ksrc,
+                                     int nz) {
+  std::vector<int> link(2 * (size_t)n, 0);
+  std::unordered_map<long long, int> last;  // cell -> last source seen in it
+  for (int s = 0; s < n; ++s) {
+    link[s] = -1;
+    if (ksrc[s] < 1 || ksrc[s] > nz) continue;
+    const long long key = ((long long)ksrc[s] << 42) | ((long long)jsrc[s] << 21) | isrc[s];
+    auto it = last.find(key);
+    if (it == last.end()) {
+      link[n + s] = 1;
+      last.emplace(key, s);
+    } else {
+      link[it->second] = s;
+      it->second = s;
+    }
+  }
+  return link;
+}
 template <class T>
 void launch_setsrc(T* c, long long cstride, Dims d, int nc, int nsou, const int* isrc,
-                   const int* jsrc, const int* ksrc, const double* tmrat, const double* dz,
-                   const double* zlayer, const double* Hm1, double dX1, double dX2, double dt,
-                   cudaStream_t s);
+                   const int* jsrc, const int* ksrc, const int* link, const double* tmrat,
+                   const double* dz, const double* zlayer, const double* Hm1, double dX1, double dX2,
+                   double dt, cudaStream_t s);
 
 // Batched form: per scenario of a batch, the arguments of setsrc and cmass2d
 // (global memory, one entry per scenario in batch order).  c_a / c_b are
@@ -69,16 +96,16 @@ struct BatchAux {
   double dt;
   // setsrc.f90:20-35
   int nsou;
-  const int *isrc, *jsrc, *ksrc;
+  const int *isrc, *jsrc, *ksrc, *link;
   const double* tmrat;
   const double *dz, *zlayer, *Hm1;
   double dX1, dX2;
   // cmass2d.f90:42-104 (binary64 velocities, device outmass)
   const double *vx, *vy, *vz, *vset;
   double* outmass;
-  long long n1, n2, n3;
 };
-void launch_setsrc_batch(const BatchAux* tab, const int* bstep, int nscen, int max_nc, cudaStream_t s);
+void launch_setsrc_batch(const BatchAux* tab, const int* bstep, int nscen, int max_nc, int max_nsou,
+                         cudaStream_t s);
 size_t cmass2d_batch_scratch_bytes(int nscen);
 void launch_cmass2d_batch(const BatchAux* tab, const int* bstep, int nscen, void* scratch,
                           cudaStream_t s);

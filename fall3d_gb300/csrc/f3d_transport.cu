@@ -639,66 +639,68 @@ void launch_clip(T* c, long long n, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------- setsrc
-// Sources/setsrc.f90:20-35.  One thread per class walks the sources in
-// file order, so several sources in one cell add in the reference's order.
+// Sources/setsrc.f90:20-35.  One thread per (first source of a cell, class)
+// walks the sources of that cell in file order (source_links), so several
+// sources in one cell add in the reference's order.
+constexpr int SRC_B = 128;
+
 template <class T>
-__global__ void k_setsrc(T* c, long long cstride, Dims d, int nc, int nsou, const int* isrc,
-                         const int* jsrc, const int* ksrc, const double* tmrat, const double* dz,
+__device__ __forceinline__ void setsrc_chain(T* cc, int s0, int ic, Dims d, int nsou, const int* isrc,
+                                             const int* jsrc, const int* ksrc, const int* link,
+                                             const double* tmrat, const double* dz,
+                                             const double* zlayer, const double* Hm1, double dX1,
+                                             double dX2, double dt) {
+  const int i = isrc[s0], j = jsrc[s0], k = ksrc[s0];
+  double dzeta;
+  if (k == 1)
+    dzeta = 0.5 * dz[k] + zlayer[k - 1];
+  else
+    dzeta = 0.5 * (dz[k - 1] + dz[k]);
+  const double vol0 = Hm1[d.P(i, j)] * dX1 * dX2 * dzeta;
+  const long long q = d.C(i, j, k);
+  double v = (double)cc[q];
+  for (int is = s0; is >= 0; is = link[is])
+    v = (double)(T)(v + dt * tmrat[is + (long long)nsou * ic] / vol0);
+  cc[q] = (T)v;
+}
+
+template <class T>
+__global__ void k_setsrc(T* c, long long cstride, Dims d, int nsou, const int* isrc, const int* jsrc,
+                         const int* ksrc, const int* link, const double* tmrat, const double* dz,
                          const double* zlayer, const double* Hm1, double dX1, double dX2,
                          double dt) {
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ic >= nc) return;
-  T* cc = c + (long long)ic * cstride;
-  for (int is = 0; is < nsou; ++is) {
-    const int i = isrc[is], j = jsrc[is], k = ksrc[is];
-    if (k < 1 || k > d.nz) continue;
-    double dzeta;
-    if (k == 1)
-      dzeta = 0.5 * dz[k] + zlayer[k - 1];
-    else
-      dzeta = 0.5 * (dz[k - 1] + dz[k]);
-    const double vol0 = Hm1[d.P(i, j)] * dX1 * dX2 * dzeta;
-    const long long q = d.C(i, j, k);
-    cc[q] = (T)((double)cc[q] + dt * tmrat[is + (long long)nsou * ic] / vol0);
-  }
+  const int s0 = blockIdx.x * SRC_B + threadIdx.x, ic = blockIdx.y;
+  if (s0 >= nsou || !link[nsou + s0]) return;
+  setsrc_chain<T>(c + (long long)ic * cstride, s0, ic, d, nsou, isrc, jsrc, ksrc, link, tmrat, dz,
+                  zlayer, Hm1, dX1, dX2, dt);
 }
 
 template <class T>
 void launch_setsrc(T* c, long long cstride, Dims d, int nc, int nsou, const int* isrc,
-                   const int* jsrc, const int* ksrc, const double* tmrat, const double* dz,
-                   const double* zlayer, const double* Hm1, double dX1, double dX2, double dt,
-                   cudaStream_t s) {
-  if (nsou <= 0) return;
-  k_setsrc<T><<<(nc + 63) / 64, 64, 0, s>>>(c, cstride, d, nc, nsou, isrc, jsrc, ksrc, tmrat, dz,
-                                             zlayer, Hm1, dX1, dX2, dt);
+                   const int* jsrc, const int* ksrc, const int* link, const double* tmrat,
+                   const double* dz, const double* zlayer, const double* Hm1, double dX1, double dX2,
+                   double dt, cudaStream_t s) {
+  if (nsou <= 0 || nc <= 0) return;
+  k_setsrc<T><<<dim3((nsou + SRC_B - 1) / SRC_B, nc), SRC_B, 0, s>>>(
+      c, cstride, d, nsou, isrc, jsrc, ksrc, link, tmrat, dz, zlayer, Hm1, dX1, dX2, dt);
   count_launch();
 }
 
-// Batched form: scenario blockIdx.y, one thread per class; the state before
+// Batched form: scenario blockIdx.y, class blockIdx.z; the state before
 // the step is in c_a after an even number of batch steps, else in c_b.
 __global__ void k_setsrc_batch(const BatchAux* tab, const int* bstep) {
   const BatchAux& b = tab[blockIdx.y];
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ic >= b.nc || b.nsou <= 0) return;
-  const Dims d = b.d;
+  const int s0 = blockIdx.x * SRC_B + threadIdx.x, ic = blockIdx.z;
+  if (ic >= b.nc || s0 >= b.nsou || !b.link[b.nsou + s0]) return;
   float* cc = ((bstep[blockIdx.y] & 1) ? b.c_b : b.c_a) + (long long)ic * b.cstride;
-  for (int is = 0; is < b.nsou; ++is) {
-    const int i = b.isrc[is], j = b.jsrc[is], k = b.ksrc[is];
-    if (k < 1 || k > d.nz) continue;
-    double dzeta;
-    if (k == 1)
-      dzeta = 0.5 * b.dz[k] + b.zlayer[k - 1];
-    else
-      dzeta = 0.5 * (b.dz[k - 1] + b.dz[k]);
-    const double vol0 = b.Hm1[d.P(i, j)] * b.dX1 * b.dX2 * dzeta;
-    const long long q = d.C(i, j, k);
-    cc[q] = (float)((double)cc[q] + b.dt * b.tmrat[is + (long long)b.nsou * ic] / vol0);
-  }
+  setsrc_chain<float>(cc, s0, ic, b.d, b.nsou, b.isrc, b.jsrc, b.ksrc, b.link, b.tmrat, b.dz, b.zlayer,
+                      b.Hm1, b.dX1, b.dX2, b.dt);
 }
 
-void launch_setsrc_batch(const BatchAux* tab, const int* bstep, int nscen, int max_nc, cudaStream_t s) {
-  if (nscen <= 0) return;
-  k_setsrc_batch<<<dim3((max_nc + 63) / 64, nscen), 64, 0, s>>>(tab, bstep);
+void launch_setsrc_batch(const BatchAux* tab, const int* bstep, int nscen, int max_nc, int max_nsou,
+                         cudaStream_t s) {
+  if (nscen <= 0 || max_nsou <= 0 || max_nc <= 0) return;
+  k_setsrc_batch<<<dim3((max_nsou + SRC_B - 1) / SRC_B, nscen, max_nc), SRC_B, 0, s>>>(tab, bstep);
   count_launch();
 }
 
@@ -762,8 +764,9 @@ void launch_f2d(double* dst, const float* src, long long n, cudaStream_t s) {
                                 cudaStream_t);                                                   \
   template void launch_clip<T>(T*, long long, cudaStream_t);                                     \
   template void launch_setsrc<T>(T*, long long, Dims, int, int, const int*, const int*,          \
-                                 const int*, const double*, const double*, const double*,        \
-                                 const double*, double, double, double, cudaStream_t);
+                                 const int*, const int*, const double*, const double*,           \
+                                 const double*, const double*, double, double, double,           \
+                                 cudaStream_t);
 
 F3D_INST(double)
 F3D_INST(float)
