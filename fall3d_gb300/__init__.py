@@ -28,6 +28,9 @@ LIB_PATH = os.path.join(HERE, "libfall3d_gb300.so")
 
 PREC_FP64, PREC_FP32 = 64, 32
 OPT_FUSED, OPT_TILE, OPT_GRAPH = 1, 2, 3
+# output variables of printres_nc.f90 (f3d_output)
+(OUT_LOAD, OUT_WET, OUT_THICK, OUT_COL_MASS, OUT_PM_COL, OUT_C_GRND, OUT_PM_GRND, OUT_AOT05,
+ OUT_CON) = range(1, 10)
 
 
 class F3DError(RuntimeError):
@@ -96,6 +99,8 @@ def load(build_if_missing: bool = False):
         "f3d_download_iters": [VP, VP],
         "f3d_get_cd": [VP, DP],
         "f3d_outputs": [VP, VP, VP, VP],
+        "f3d_output": [VP, I, I, I, VP, I],
+        "f3d_output_fl": [VP, D, VP, VP, I],
         "f3d_run": [VP, VP, VP, D, D, I, VP, I, IP],
         "f3d_run_reset": [VP],
         "f3d_sync": [VP],
@@ -434,6 +439,25 @@ class Context:
         a = [np.zeros((self.ny, self.nx)) for _ in range(3)]
         _check(self.lib.f3d_outputs(self.h, *[_addr(x) for x in a]))
         return dict(load=a[0], col_mass=a[1], c_grnd=a[2])
+
+    def output(self, var, index=0, asl=False, binary32=False):
+        """One output variable of printres_nc.f90 (OUT_*): (ny, nx), or
+        (nz, ny, nx) for OUT_CON; binary32 as the netCDF file holds it."""
+        shape = (self.nz, self.ny, self.nx) if var == OUT_CON else (self.ny, self.nx)
+        a = np.zeros(shape, np.float32 if binary32 else np.float64)
+        _check(self.lib.f3d_output(self.h, int(var), int(index), int(bool(asl)), a.ctypes.data,
+                                   1 if binary32 else 0))
+        return a
+
+    def output_fl(self, flight_level, p, binary32=False):
+        """Particle concentration at a flight level (hundreds of feet), with
+        p the pressure (nz, ny, nx) of the model levels in Pa."""
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        assert p.shape == (self.nz, self.ny, self.nx)
+        a = np.zeros((self.ny, self.nx), np.float32 if binary32 else np.float64)
+        _check(self.lib.f3d_output_fl(self.h, float(flight_level), p.ctypes.data, a.ctypes.data,
+                                      1 if binary32 else 0))
+        return a
 
     def upload_state(self, c=None, cdry=None, cwet=None, erumass=0.0, outmass=0.0, cd=1.0):
         _check(self.lib.f3d_upload_state(self.h, _addr(c), _addr(cdry), _addr(cwet), float(erumass),

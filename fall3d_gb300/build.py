@@ -33,6 +33,7 @@ UNITS = {
     "f3d_ctx.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
     "f3d_batch.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
     "f3d_serve.cu": ["-Xcompiler", "-fvisibility=default"],
+    "f3d_output.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
 }
 
 

@@ -87,8 +87,10 @@ size_t reduce_scratch_bytes(long long nterms, int nsums) {
 // cell ("item"): an item computes its class-independent factor
 // (dt*area)*velo (faces) or dt*area (top) once and walks the classes, so
 // each term is still ((dt*area)*velo)*conc rounded as the reference writes
-// it.  Items: [0, nT) top (i fastest), then x faces (j fastest, left half
-// first), then y faces (i fastest, down half first).
+// it.  A zero concentration (inflow faces, cells the plume has not
+// reached) gives an exact zero term, which leaves the sum unchanged and is
+// skipped.  Items: [0, nT) top (i fastest), then x faces (j fastest, left
+// half first), then y faces (i fastest, down half first).
 struct Cm2Items {
   int nT, nX, nY;  // top items, x-face items, y-face items
 };
@@ -118,6 +120,43 @@ __device__ __forceinline__ DD ds_dd(DS a) {
   return DD{hi, a.e - (hi - a.s)};
 }
 
+// the terms of one side-face cell, classes in order: +-(w*conc)
+template <class T>
+__device__ __forceinline__ void face_terms(const T* cc, long long hb, int nc_loc, double w, int side,
+                                           DS& acc) {
+  for (int q0 = 0; q0 < nc_loc; q0 += 4) {
+    T cv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) cv[u] = q0 + u < nc_loc ? cc[(q0 + u) * hb] : T(0);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (cv[u] == T(0)) continue;
+      const double t = w * (double)cv[u];
+      ds_add(acc, side ? t : -t);
+    }
+  }
+}
+
+// Block sum of the threads' accumulators into partial[blockIdx.x]; a warp
+// whose accumulators are all zero contributes an exact zero without the
+// binary64 shuffle reduction.
+__device__ void block_store_ds(DS a, DD* partial) {
+  __shared__ DD sh[RB / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  DD v = dd_zero();
+  if (__any_sync(0xffffffffu, a.s != 0.0 || a.e != 0.0)) {
+    v = ds_dd(a);
+    for (int off = 16; off > 0; off >>= 1) v = dd_add(v, dd_shfl_down(v, off));
+  }
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DD r = sh[0];
+    for (int w = 1; w < RB / 32; ++w) r = dd_add(r, sh[w]);
+    partial[blockIdx.x] = r;
+  }
+}
+
 template <class T>
 __device__ __forceinline__ void cmass2d_item(int u, const Cm2Items& it, const T* c, const double* vx,
                                              const double* vy, const double* vz, const double* vset,
@@ -139,9 +178,16 @@ __device__ __forceinline__ void cmass2d_item(int u, const Cm2Items& it, const T*
     const double w = vz[m];
     const double* vs = vset + (long long)(ic_loc - 1) * s3 + m;
     const T* cc = c0 + d.C(i, j, nz + 1);
-    for (int q = 0; q < nc_loc; ++q) {
-      const double velo = w + vs[q * s3];
-      ds_add(acc, da * velo * (double)cc[q * hb]);
+    for (int q0 = 0; q0 < nc_loc; q0 += 4) {
+      T cv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) cv[u] = q0 + u < nc_loc ? cc[(q0 + u) * hb] : T(0);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (cv[u] == T(0)) continue;  // an exact zero term (finite velocities)
+        const double velo = w + vs[(q0 + u) * s3];
+        ds_add(acc, da * velo * (double)cv[u]);
+      }
     }
     return;
   }
@@ -155,10 +201,7 @@ __device__ __forceinline__ void cmass2d_item(int u, const Cm2Items& it, const T*
     const double area = faty * dy * 0.5 * (dz[k] + dz[k - 1]);
     const double w = dt * area * vx[d.M(side ? nx : 1, j, k)];
     const T* cc = c0 + d.C(side ? nx + 1 : 0, j, k);
-    for (int q = 0; q < nc_loc; ++q) {
-      const double t = w * (double)cc[q * hb];
-      ds_add(acc, side ? t : -t);
-    }
+    face_terms<T>(cc, hb, nc_loc, w, side, acc);
     return;
   }
   u -= it.nX;
@@ -170,10 +213,7 @@ __device__ __forceinline__ void cmass2d_item(int u, const Cm2Items& it, const T*
   const double area = fatx * dx * 0.5 * (dz[k] + dz[k - 1]);
   const double w = dt * area * vy[d.M(i, side ? ny : 1, k)];
   const T* cc = c0 + d.C(i, side ? ny + 1 : 0, k);
-  for (int q = 0; q < nc_loc; ++q) {
-    const double t = w * (double)cc[q * hb];
-    ds_add(acc, side ? t : -t);
-  }
+  face_terms<T>(cc, hb, nc_loc, w, side, acc);
 }
 
 template <class T>
@@ -187,8 +227,7 @@ __global__ void k_cmass2d(const T* c, const double* vx, const double* vy, const 
   for (int u = blockIdx.x * RB + threadIdx.x; u < ntot; u += gridDim.x * RB)
     cmass2d_item<T>(u, it, c, vx, vy, vz, vset, d, ic_loc, nc_loc, iz_loc, nz_loc, dx, dy, dz, dt,
                     acc);
-  DD v[1] = {ds_dd(acc)};
-  block_store_dd<1>(v, partial);
+  block_store_ds(acc, partial);
 }
 
 // Batched form: scenario blockIdx.y, its outflow summed over gridDim.x
@@ -204,8 +243,7 @@ __global__ void k_cmass2d_batch(const BatchAux* tab, const int* bstep, DD* parti
   for (int u = blockIdx.x * RB + threadIdx.x; u < ntot; u += gridDim.x * RB)
     cmass2d_item<float>(u, it, c, b.vx, b.vy, b.vz, b.vset, d, 1, b.nc, 1, d.nz, b.dX1, b.dX2, b.dz,
                         b.dt, acc);
-  DD v[1] = {ds_dd(acc)};
-  block_store_dd<1>(v, partial + (long long)blockIdx.y * gridDim.x);
+  block_store_ds(acc, partial + (long long)blockIdx.y * gridDim.x);
 }
 
 // outmass = outmass + sum (cmass2d.f90:104), one block per scenario
@@ -374,47 +412,6 @@ void launch_finddt(Dims d, int nc, double dX1, double dX2, const double* dz, con
   count_launch();
 }
 
-// ----------------------------------------------------------- outputs
-// Sources/printres_nc.f90:104-122 (LOAD), :218-246 (COL_MASS),
-// :391-410 (C_GRND).
-template <class T>
-__global__ void k_outputs(const T* c, const double* cload, Dims d, int np, const double* dz,
-                          const double* Hm1, double* load, double* col_mass, double* c_grnd) {
-  const long long pl = d.plane();
-  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p >= pl) return;
-  const int i = (int)(p % d.nx) + 1, j = (int)(p / d.nx) + 1;
-  const long long hb = d.halo();
-  const double h = Hm1[p];
-  if (load) load[p] = cload[p] / h;
-  if (col_mass) {
-    double colm = 0.0, wprev = 0.0;
-    for (int ic = 1; ic <= np; ++ic) wprev = wprev + (double)c[(ic - 1) * hb + d.C(i, j, 1)] / h;
-    for (int k = 1; k <= d.nz - 1; ++k) {
-      double wnext = 0.0;
-      for (int ic = 1; ic <= np; ++ic) wnext = wnext + (double)c[(ic - 1) * hb + d.C(i, j, k + 1)] / h;
-      colm = colm + dz[k] * 0.5 * (wprev + wnext);
-      wprev = wnext;
-    }
-    col_mass[p] = 1e3 * colm;
-  }
-  if (c_grnd) {
-    double sum = 0.0;
-    for (int ic = 1; ic <= np; ++ic) sum = sum + (double)c[(ic - 1) * hb + d.C(i, j, 1)] / h;
-    c_grnd[p] = 1e3 * sum;
-  }
-}
-
-template <class T>
-void launch_outputs(const T* c, const double* cload, Dims d, int np, const double* dz,
-                    const double* Hm1, double* load, double* col_mass, double* c_grnd,
-                    cudaStream_t s) {
-  const long long pl = d.plane();
-  k_outputs<T><<<(unsigned)((pl + 127) / 128), 128, 0, s>>>(c, cload, d, np, dz, Hm1, load, col_mass,
-                                                           c_grnd);
-  count_launch();
-}
-
 size_t cmass2d_batch_scratch_bytes(int nscen) { return sizeof(DD) * (size_t)nscen * 64 + 256; }
 
 void launch_cmass2d_batch(const BatchAux* tab, const int* bstep, int nscen, void* scratch,
@@ -438,9 +435,5 @@ template void launch_cmass3d<double>(const double*, const double*, const double*
 template void launch_cmass3d<float>(const float*, const double*, const double*, const double*,
                                     Dims, int, double, double, const double*, void*, double*,
                                     cudaStream_t);
-template void launch_outputs<double>(const double*, const double*, Dims, int, const double*,
-                                     const double*, double*, double*, double*, cudaStream_t);
-template void launch_outputs<float>(const float*, const double*, Dims, int, const double*,
-                                    const double*, double*, double*, double*, cudaStream_t);
 
 }  // namespace f3d

@@ -374,6 +374,8 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
   x->g.diam = x->g.rhop = x->g.psi = x->g.sphe = nullptr;
   x->d = Dims{g->nx, g->ny, g->nz};
   x->prec = g->precision;
+  x->h_diam.assign(g->diam, g->diam + g->nc);
+  x->h_rhop.assign(g->rhop, g->rhop + g->nc);
   for (int k = 1; k < g->nz; ++k)
     if (!(g->zlayer[k] >= g->zlayer[k - 1])) x->fused_ok = 0;
   if (x->d.halo() >= (1LL << 31) || x->d.cells() >= (1LL << 31)) x->fused_ok = 0;
@@ -930,22 +932,11 @@ int f3d_download_iters(f3d_ctx* x, int* iters) {
 
 int f3d_outputs(f3d_ctx* x, double* load, double* col_mass, double* c_grnd) {
   if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
-  const Dims d = x->d;
-  const size_t pl = (size_t)d.plane();
-  cudaStream_t s = x->stream;
-  launch_getc0(x->cdry, x->cwet, x->cload, d, x->g.nc, x->g.np, s);
-  double* tmp = nullptr;
-  CK(cudaMallocAsync((void**)&tmp, 3 * pl * sizeof(double), s));
-  if (x->prec == F3D_PREC_FP32)
-    launch_outputs<float>(x->c32, x->cload, d, x->g.np, x->dz, x->Hm1, tmp, tmp + pl, tmp + 2 * pl, s);
-  else
-    launch_outputs<double>(x->c64, x->cload, d, x->g.np, x->dz, x->Hm1, tmp, tmp + pl, tmp + 2 * pl, s);
-  if (load) CK(cudaMemcpyAsync(load, tmp, pl * sizeof(double), cudaMemcpyDefault, s));
-  if (col_mass) CK(cudaMemcpyAsync(col_mass, tmp + pl, pl * sizeof(double), cudaMemcpyDefault, s));
-  if (c_grnd) CK(cudaMemcpyAsync(c_grnd, tmp + 2 * pl, pl * sizeof(double), cudaMemcpyDefault, s));
-  CK(cudaFreeAsync(tmp, s));
-  CK(cudaStreamSynchronize(s));
-  return F3D_OK;
+  int rc = F3D_OK;
+  if (load) rc = f3d_output(x, F3D_OUT_LOAD, 0, 0, load, F3D_OUT_BINARY64);
+  if (!rc && col_mass) rc = f3d_output(x, F3D_OUT_COL_MASS, 0, 0, col_mass, F3D_OUT_BINARY64);
+  if (!rc && c_grnd) rc = f3d_output(x, F3D_OUT_C_GRND, 0, 0, c_grnd, F3D_OUT_BINARY64);
+  return rc;
 }
 
 int f3d_set_option(f3d_ctx* x, int key, int value) {

@@ -18,6 +18,7 @@ struct f3d_ctx {
   // static
   double *dz = nullptr, *zlayer = nullptr, *Hm1 = nullptr, *topg = nullptr;
   double *diam = nullptr, *rhop = nullptr, *psi = nullptr, *sphe = nullptr;
+  std::vector<double> h_diam, h_rhop;  // host copies (output class selections)
   // met and coefficients (binary64)
   double *vx = nullptr, *vy = nullptr, *vz = nullptr, *tempe = nullptr, *vptemp = nullptr;
   double *rho = nullptr, *rkhor = nullptr, *rkh1 = nullptr, *rkver = nullptr, *divu = nullptr;

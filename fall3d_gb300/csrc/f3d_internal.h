@@ -134,10 +134,6 @@ void launch_finddt(Dims d, int nc, double dX1, double dX2, const double* dz, con
                    const double* vy, const double* vz, const double* vset, const double* rkh1,
                    const double* rkhor, const double* rkver, unsigned long long* dtcn_bits,
                    cudaStream_t s);
-template <class T>
-void launch_outputs(const T* c, const double* cload, Dims d, int np, const double* dz,
-                    const double* Hm1, double* load, double* col_mass, double* c_grnd,
-                    cudaStream_t s);
 
 // Coefficient chain (binary64).
 void launch_kappa3(Dims d, int modkv, int modkh, int coord_sys, double rkv0, double rkh0,

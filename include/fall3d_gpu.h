@@ -380,10 +380,54 @@ int f3d_download_iters(f3d_ctx* ctx, int* iters);
 int f3d_get_cd(const f3d_ctx* ctx, double* cd);
 
 /* Output quantities of Sources/printres_nc.f90 on the device:
- * LOAD = cload(:,:,0)/Hm1 (:104-122), COL_MASS (:218-246),
- * C_GRND (:391-410).  Each (nx,ny); NULL skips. */
+ * LOAD = cload(:,:,0)/Hm1 (:105-123), COL_MASS (:216-247),
+ * C_GRND (:389-411).  Each (nx,ny) binary64; NULL skips. */
 int f3d_outputs(f3d_ctx* ctx, double* load, double* col_mass,
                 double* c_grnd);
+
+/* One output variable of Sources/printres_nc.f90, computed on the device
+ * in binary64 in the reference's order of operations and written to dst
+ * (host or device memory) as binary64 or, like the reference's NF90_FLOAT
+ * netCDF variables (printres_nc.f90:805-841), as binary32.  2-D variables
+ * are (nx,ny), x fastest; F3D_OUT_CON is (nx,ny,nz).  `index` selects:
+ *   F3D_OUT_LOAD      deposit load kg/m2, cload(:,:,index)/Hm1 with
+ *                     index 0 = all particles, 1..np one class (:105-146)
+ *   F3D_OUT_WET       wet deposit kg/m2, cwet(:,:,index)/Hm1 (:148-189)
+ *   F3D_OUT_THICK     deposit thickness in cm (:191-214); index unused
+ *   F3D_OUT_COL_MASS  column mass g/m2: index 0 = particles (:216-247),
+ *                     g = 1..nc-np the g-th gas class (:249-279)
+ *   F3D_OUT_PM_COL    column mass of the particles with diameter <= index
+ *                     micrometres, index 5, 10 or 20 (:281-387)
+ *   F3D_OUT_C_GRND    first-layer particle concentration g/m3 (:389-411)
+ *   F3D_OUT_PM_GRND   first-layer PM concentration, index 5/10/20 (:413-493)
+ *   F3D_OUT_AOT05     aerosol optical thickness (:495-540, get_AOT_prop
+ *                     :2066-2123); index unused
+ *   F3D_OUT_CON       concentration g/m3: index 0 = all particles
+ *                     (:575-601), 1..nc one class (:646-671); asl != 0
+ *                     moves it from terrain-following levels to heights
+ *                     above sea level (Sources/ter2asl.f90:1-55, used when
+ *                     terrain_following is false)
+ * The deposit variables first form cload = cdry + cwet and the class sums
+ * (endstep.f90:35,60). */
+#define F3D_OUT_LOAD      1
+#define F3D_OUT_WET       2
+#define F3D_OUT_THICK     3
+#define F3D_OUT_COL_MASS  4
+#define F3D_OUT_PM_COL    5
+#define F3D_OUT_C_GRND    6
+#define F3D_OUT_PM_GRND   7
+#define F3D_OUT_AOT05     8
+#define F3D_OUT_CON       9
+#define F3D_OUT_BINARY64  0
+#define F3D_OUT_BINARY32  1
+int f3d_output(f3d_ctx* ctx, int var, int index, int asl, void* dst,
+               int dst_type);
+/* Particle concentration g/m3 at a flight level (hundreds of feet) of the
+ * ICAO standard atmosphere (printres_nc.f90:542-573, Sources/setcut.f90):
+ * interpolated in the pressure p(nx,ny,nz) of the model levels (Pa, the
+ * DBS variable P; host or device memory); (nx,ny). */
+int f3d_output_fl(f3d_ctx* ctx, double flight_level, const double* p,
+                  void* dst, int dst_type);
 
 /* Sources/Fall3d.f90:73-121: the time loop from beg_time to end_time
  * (at most max_steps steps if max_steps > 0), reading meteorology and

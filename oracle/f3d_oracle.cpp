@@ -949,39 +949,246 @@ void orc_meteo_scale(int nx, int ny, int nz, int coord_sys, double dX1,
 }
 
 /* --------------------------------------------------------- output fields */
-/* Sources/printres_nc.f90:104-122 (LOAD), :218-246 (COL_MASS), :391-410
- * (C_GRND): the particle-class sums divided by Hm1, in kg/m2 (LOAD),
- * g/m2 (COL_MASS) and g/m3 (C_GRND). */
-void orc_outputs(const double* c, const double* cload, int nx, int ny, int nz,
-                 int np, const double* dz, const double* Hm1, double* load,
-                 double* col_mass, double* c_grnd) {
+/* Sources/printres_nc.f90.  Class sums run from 0 in class order over the
+ * selected classes and are divided by Hm1 afterwards ("work3d = work3d +
+ * c(...,ic)" then "work3d = work3d/Hm1"), the column trapezoid runs from
+ * the first layer upwards, and the unit factor multiplies the finished sum. */
+static double orc_class_sum(const double* c, const Dims& d, int i, int j, int k, const int* cls,
+                            int ncls) {
+  double s = 0.0;
+  for (int n = 0; n < ncls; ++n) s = s + c[(size_t)cls[n] * d.halo() + d.C(i, j, k)];
+  return s;
+}
+
+/* z-cumulative concentration, g/m2: :216-247 (particles), :249-279 (one
+ * gas), :281-387 (PM05/PM10/PM20); cls are 0-based class indices. */
+void orc_out_column(const double* c, int nx, int ny, int nz, const int* cls, int ncls,
+                    const double* dz, const double* Hm1, double* out) {
   Dims d{nx, ny, nz};
-  const size_t h = d.halo();
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= nx; ++i) {
       const size_t p = d.P(i, j);
-      if (load) load[p] = cload[p] / Hm1[p];
-      if (col_mass) {
-        // w(k) = sum over particle classes of c(i,j,k,ic)/Hm1, then a
-        // trapezoid in z, times 1e3 (kg -> g).
-        double colm = 0.0;
-        double wprev = 0.0;
-        for (int ic = 1; ic <= np; ++ic) wprev = wprev + c[(size_t)(ic - 1) * h + d.C(i, j, 1)] / Hm1[p];
-        for (int k = 1; k <= nz - 1; ++k) {
-          double wnext = 0.0;
-          for (int ic = 1; ic <= np; ++ic)
-            wnext = wnext + c[(size_t)(ic - 1) * h + d.C(i, j, k + 1)] / Hm1[p];
-          colm = colm + dz[k] * 0.5 * (wprev + wnext);
-          wprev = wnext;
-        }
-        col_mass[p] = 1e3 * colm;
+      double work2d = 0.0;
+      for (int iz = 1; iz <= nz - 1; ++iz) {
+        const double w0 = orc_class_sum(c, d, i, j, iz, cls, ncls) / Hm1[p];
+        const double w1 = orc_class_sum(c, d, i, j, iz + 1, cls, ncls) / Hm1[p];
+        work2d = work2d + dz[iz] * 0.5 * (w0 + w1);
       }
-      if (c_grnd) {
-        double s = 0.0;
-        for (int ic = 1; ic <= np; ++ic) s = s + c[(size_t)(ic - 1) * h + d.C(i, j, 1)] / Hm1[p];
-        c_grnd[p] = 1e3 * s;
+      out[p] = 1e3 * work2d;
+    }
+}
+
+/* first-layer concentration, g/m3: :389-411 (particles), :413-493 (PM) */
+void orc_out_ground(const double* c, int nx, int ny, int nz, const int* cls, int ncls,
+                    const double* Hm1, double* out) {
+  Dims d{nx, ny, nz};
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      const size_t p = d.P(i, j);
+      const double work2d = orc_class_sum(c, d, i, j, 1, cls, ncls);
+      out[p] = 1e3 * work2d / Hm1[p];
+    }
+}
+
+/* PM selections of :284-370 and :416-479: particle classes (1..np) with
+ * diam <= 5e-6, 1e-5 or 2e-5 m; returns their count, 0-based in cls. */
+int orc_pm_classes(int np, const double* diam, int microns, int* cls) {
+  const double thr = microns == 5 ? 5e-6 : microns == 10 ? 1e-5 : 2e-5;
+  int n = 0;
+  for (int ic = 1; ic <= np; ++ic)
+    if (diam[ic - 1] <= thr) cls[n++] = ic - 1;
+  return n;
+}
+
+/* get_AOT_prop, :2066-2123: effective radii (um -> m) and efficiencies */
+static void orc_aot_prop(double* reff, double* qeff) {
+  static const double r[20] = {0.014, 0.020, 0.028, 0.040, 0.056, 0.079, 0.112, 0.158, 0.224, 0.316,
+                               0.447, 0.631, 0.891, 1.259, 1.778, 2.512, 3.548, 5.012, 7.079, 10.000};
+  static const double q[20] = {0.00213, 0.00386, 0.00864, 0.02324, 0.06674, 0.18285, 0.44613,
+                               0.93225, 1.63000, 2.35760, 2.83130, 2.90880, 2.72340, 2.50530,
+                               2.35970, 2.27100, 2.21020, 2.16410, 2.12830, 2.10050};
+  for (int b = 0; b < 20; ++b) {
+    reff[b] = r[b] * 1e-6;
+    qeff[b] = q[b];
+  }
+}
+
+/* aerosol optical thickness, :495-540 */
+void orc_out_aot(const double* c, int nx, int ny, int nz, int np, const double* diam,
+                 const double* rhop, const double* dz, const double* Hm1, double* out) {
+  Dims d{nx, ny, nz};
+  double reff[20], qeff[20];
+  orc_aot_prop(reff, qeff);
+  const size_t pl = d.plane();
+  std::vector<double> work2d(pl, 0.0), work3d(d.cells());
+  for (int ic = 1; ic <= np; ++ic) {
+    if (!(0.5 * diam[ic - 1] >= reff[0] && 0.5 * diam[ic - 1] <= reff[19])) continue;
+    int ieff = 0;  /* 1-based as in the reference */
+    for (int i = 1; i <= 19; ++i)
+      if (0.5 * diam[ic - 1] >= reff[i - 1] && 0.5 * diam[ic - 1] <= reff[i]) ieff = i + 1;
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i)
+          work3d[d.M(i, j, k)] = c[(size_t)(ic - 1) * d.halo() + d.C(i, j, k)] / Hm1[d.P(i, j)];
+    for (int iz = 1; iz <= nz - 1; ++iz)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i) {
+          const size_t p = d.P(i, j);
+          work2d[p] = work2d[p] + dz[iz] * 0.5 * (work3d[d.M(i, j, iz)] + work3d[d.M(i, j, iz + 1)]) *
+                                      0.75 * qeff[ieff - 1] / (rhop[ic - 1] * reff[ieff - 1]);
+        }
+  }
+  for (size_t p = 0; p < pl; ++p) out[p] = work2d[p];
+}
+
+/* deposit thickness, cm, :191-214 (cload is (nx,ny,0:nc)) */
+void orc_out_thick(const double* cload, int nx, int ny, int np, const double* rhop,
+                   const double* Hm1, double* out) {
+  const size_t pl = (size_t)nx * ny;
+  for (size_t p = 0; p < pl; ++p) {
+    double work2d = 0.0;
+    for (int ic = 1; ic <= np; ++ic) work2d = work2d + cload[(size_t)ic * pl + p] / rhop[ic - 1];
+    out[p] = 1e2 * work2d / Hm1[p];
+  }
+}
+
+/* Sources/setcut.f90:60-107 (standard_atm): ICAO pressure at height z */
+double orc_standard_pressure(double z) {
+  const double goo = 9.80665, Roo = 8.31432, Moo = 0.0289644;
+  const double zoo = 0.0, Too = 288.15, poo = 101325.0, Loo = -0.0065;
+  const double zo1 = 11000.0, To1 = 216.65, po1 = 22632.0;
+  const double zo2 = 20000.0, To2 = 216.65, po2 = 5474.0, Lo2 = 0.001;
+  double T, P;
+  if (z < zo1) {
+    T = Too + Loo * (z - zoo);
+    P = poo * std::pow(Too / T, goo * Moo / (Roo * Loo));
+  } else if (z < zo2) {
+    T = To1;
+    P = po1 * std::exp(-(goo * Moo * (z - zo1) / (Roo * To1)));
+  } else {
+    T = To2 + Lo2 * (z - zo2);
+    P = po2 * std::pow(To2 / T, goo * Moo / (Roo * Lo2));
+  }
+  (void)T;
+  return P;
+}
+
+/* Sources/setcut.f90:1-54 (setcut_FL) on a precomputed var3d (nx,ny,nz) */
+void orc_setcut_fl(int nx, int ny, int nz, double* var2d, const double* var3d, const double* p,
+                   double fl) {
+  const double pnom = orc_standard_pressure(fl);
+  const size_t pl = (size_t)nx * ny;
+  for (size_t q = 0; q < pl; ++q) {
+    if (pnom > p[q]) {
+      var2d[q] = 0.0;
+      continue;
+    }
+    bool go_on = true;
+    int iz = 0;
+    while (go_on) {
+      iz = iz + 1;
+      const double p0 = p[(size_t)(iz - 1) * pl + q], p1 = p[(size_t)iz * pl + q];
+      if (pnom <= p0 && pnom > p1) {
+        go_on = false;
+        const double s = (pnom - p0) / (p1 - p0);
+        var2d[q] = var3d[(size_t)(iz - 1) * pl + q] * (1.0 - s) + var3d[(size_t)iz * pl + q] * s;
+      }
+      if (iz + 1 == nz && go_on) {
+        var2d[q] = 0.0;
+        go_on = false;
       }
     }
+  }
+}
+
+/* Sources/ter2asl.f90:1-55 in place on conc (nx,ny,nz) */
+void orc_ter2asl(double* conc, const double* topg, const double* zlayer, int nx, int ny, int nz) {
+  const size_t pl = (size_t)nx * ny;
+  std::vector<double> c(conc, conc + pl * nz);
+  for (size_t q = 0; q < pl; ++q) {
+    const double zo = fmax2(0.0, topg[q]);
+    for (int iz = 1; iz <= nz; ++iz) {
+      const double zasl = zlayer[iz - 1];
+      double& o = conc[(size_t)(iz - 1) * pl + q];
+      if (zasl < zo + zlayer[0]) {
+        o = 0.0;
+        continue;
+      }
+      bool found = false;
+      int izz = 0;
+      while (!found) {
+        izz = izz + 1;
+        if (zasl >= zo + zlayer[izz - 1] && zasl <= zo + zlayer[izz]) {
+          found = true;
+          const double s = (zo + zlayer[izz] - zasl) / (zlayer[izz] - zlayer[izz - 1]);
+          o = s * c[(size_t)(izz - 1) * pl + q] + (1.0 - s) * c[(size_t)izz * pl + q];
+        }
+        if (izz + 1 == nz && !found) {
+          o = 0.0;
+          found = true;
+        }
+      }
+    }
+  }
+}
+
+/* particle concentration w = (sum_{ic<=np} c)/Hm1 on the model levels
+ * (the work3d of :545-556, :577-584) */
+static void orc_particle_conc(const double* c, const Dims& d, int np, const double* Hm1,
+                              std::vector<double>& w) {
+  w.assign(d.cells(), 0.0);
+  for (int ic = 1; ic <= np; ++ic)
+    for (int k = 1; k <= d.nz; ++k)
+      for (int j = 1; j <= d.ny; ++j)
+        for (int i = 1; i <= d.nx; ++i)
+          w[d.M(i, j, k)] = w[d.M(i, j, k)] + c[(size_t)(ic - 1) * d.halo() + d.C(i, j, k)];
+  for (int k = 1; k <= d.nz; ++k)
+    for (int j = 1; j <= d.ny; ++j)
+      for (int i = 1; i <= d.nx; ++i) w[d.M(i, j, k)] = w[d.M(i, j, k)] / Hm1[d.P(i, j)];
+}
+
+/* flight-level cut, g/m3, :542-573 (fl in hundreds of feet) */
+void orc_out_fl(const double* c, int nx, int ny, int nz, int np, const double* p, double fl,
+                const double* Hm1, double* out) {
+  Dims d{nx, ny, nz};
+  std::vector<double> w;
+  orc_particle_conc(c, d, np, Hm1, w);
+  const double flm = fl * 30.48;
+  orc_setcut_fl(nx, ny, nz, out, w.data(), p, flm);
+  for (size_t q = 0; q < d.plane(); ++q) out[q] = 1e3 * out[q];
+}
+
+/* 3-D concentration, g/m3: ic 0 = all particles (:575-601), else class ic
+ * (:646-671); asl: ter2asl as when terrain_following is false */
+void orc_out_con(const double* c, int nx, int ny, int nz, int np, int ic, const double* Hm1,
+                 const double* zlayer, const double* topg, int asl, double* out) {
+  Dims d{nx, ny, nz};
+  std::vector<double> w;
+  if (ic == 0) {
+    orc_particle_conc(c, d, np, Hm1, w);
+  } else {
+    w.assign(d.cells(), 0.0);
+    for (int k = 1; k <= nz; ++k)
+      for (int j = 1; j <= ny; ++j)
+        for (int i = 1; i <= nx; ++i)
+          w[d.M(i, j, k)] = c[(size_t)(ic - 1) * d.halo() + d.C(i, j, k)] / Hm1[d.P(i, j)];
+  }
+  for (size_t q = 0; q < d.cells(); ++q) out[q] = 1e3 * w[q];
+  if (asl) orc_ter2asl(out, topg, zlayer, nx, ny, nz);
+}
+
+/* LOAD, COL_MASS and C_GRND of the context's state (:105-123, :216-247,
+ * :389-411) */
+void orc_outputs(const double* c, const double* cload, int nx, int ny, int nz,
+                 int np, const double* dz, const double* Hm1, double* load,
+                 double* col_mass, double* c_grnd) {
+  std::vector<int> cls(np);
+  for (int ic = 0; ic < np; ++ic) cls[ic] = ic;
+  const size_t pl = (size_t)nx * ny;
+  if (load)
+    for (size_t p = 0; p < pl; ++p) load[p] = cload[p] / Hm1[p];
+  if (col_mass) orc_out_column(c, nx, ny, nz, cls.data(), np, dz, Hm1, col_mass);
+  if (c_grnd) orc_out_ground(c, nx, ny, nz, cls.data(), np, Hm1, c_grnd);
 }
 
 /* ===================================================================== */

@@ -47,12 +47,13 @@ MODULE_FILES = ["KindType.f90", "Numeric.f90", "Master.f90", "InpOut.f90"]
 UNIT_FILES = ["setbcc.f90", "advctzc.f90", "advctx.f90", "advcty.f90", "diffz.f90", "diffx.f90",
               "diffy.f90", "wetdep.f90", "accum.f90", "cmass2d.f90", "cmass3d.f90", "finddt.f90",
               "kappa3.f90", "setvset.f90", "setpsi.f90", "setvdrydep.f90", "corvver.f90",
-              "setdivu.f90", "setsrc.f90", "sizloop.f90", "meteo.f90", "source.f90", "endstep.f90"]
+              "setdivu.f90", "setsrc.f90", "sizloop.f90", "meteo.f90", "source.f90", "endstep.f90",
+              "setcut.f90", "ter2asl.f90"]
 # units from those files that are translated (others in the files are skipped)
 WANTED = {"setbcc", "advctzc", "advctx", "advcty", "diffz", "diffx", "diffy", "wetdep", "accum",
           "cmass2d", "cmass3d", "finddt", "kappa3", "setvset", "vsettl", "setpsi", "get_gama",
           "setvdrydep", "corvver", "setdivu", "setsrc", "sizloop", "meteo", "source", "getc0",
-          "getmem1", "getmem2", "outmem2"}
+          "getmem1", "getmem2", "outmem2", "setcut_fl", "standard_atm", "ter2asl"}
 NOOP_CALLS = {"bcast", "parallel_sum", "exchange_1layer", "exchange_2layer", "collect_cz",
               "collect_c", "collect_cload", "addtime", "wriwar", "flush", "reamet", "reasrc",
               "addradialwind", "settemplume", "agrsrc", "cpu_time"}

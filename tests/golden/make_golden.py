@@ -240,7 +240,52 @@ def scenario(workload, seed, over):
     return s
 
 
+def cuts():
+    """Sources/setcut.f90 (setcut_FL, standard_atm) and Sources/ter2asl.f90
+    of the translated reference on a seeded 9x7x12 case: heights around the
+    three ICAO layers, topography below, at and above sea level, flight
+    levels below the ground and above the top, and an unsorted-pressure
+    column.  Stored in output_cuts.npz."""
+    R = RefLib()
+    rng = np.random.default_rng(7)
+    nx, ny, nz = 9, 7, 12
+    zl = np.concatenate([[0.0, 150.0, 400.0], np.linspace(800.0, 16000.0, nz - 3)])
+    topg = rng.uniform(-200.0, 3000.0, (ny, nx))
+    topg[0, 0], topg[0, 1], topg[1, 0] = 0.0, -50.0, 12000.0
+    var3d = rng.uniform(0.0, 1.0, (nz, ny, nx))
+    zabs = zl[:, None, None] + np.maximum(topg, 0.0)[None]
+    _, pres, _ = synth.standard_atmosphere(zabs)
+    pres = pres * (1.0 + 0.01 * rng.standard_normal(pres.shape))
+    pres[:, 2, 3] = pres[::-1, 2, 3]  # increasing with height: no bracket
+    pres = np.ascontiguousarray(pres)
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    ni, nj, nk = C.c_int(nx), C.c_int(ny), C.c_int(nz)
+    fls = np.array([0.0, 5.0, 50.0, 100.0, 200.0, 350.0, 450.0, 700.0, 1200.0])
+    cut = np.zeros((len(fls), ny, nx))
+    for n, fl in enumerate(fls):
+        out = np.zeros((ny, nx))
+        R.call("setcut_fl", C.byref(ni), C.byref(nj), C.byref(nk), dp(zl), dp(out), dp(var3d), dp(topg),
+               dp(pres), C.byref(C.c_double(fl * 30.48)))
+        cut[n] = out
+    zs = np.array([-100.0, 0.0, 1524.0, 10999.0, 11000.0, 15000.0, 19999.5, 20000.0, 30000.0])
+    patm = np.zeros(len(zs))
+    for n, z in enumerate(zs):
+        pp, tt = C.c_double(), C.c_double()
+        R.call("standard_atm", C.byref(pp), C.byref(tt), C.byref(C.c_double(z)))
+        patm[n] = pp.value
+    conc = np.ascontiguousarray(rng.uniform(0.0, 1.0, (nz, ny, nx)))
+    asl = conc.copy()
+    R.call("ter2asl", dp(asl), dp(topg), dp(zl), C.byref(ni), C.byref(nj), C.byref(nk))
+    path = os.path.join(HERE, "output_cuts.npz")
+    np.savez_compressed(path, zlayer=zl, topg=topg, var3d=var3d, pres=pres, fls=fls, cut=cut, zs=zs,
+                        patm=patm, conc=conc, asl=asl)
+    print(f"output_cuts: {os.path.getsize(path) / 1024:.0f} KB")
+
+
 def main():
+    cuts()
+    if "--cuts" in sys.argv:
+        return
     meta = {}
     for name, workload, seed, over, max_steps in CASES:
         s = scenario(workload, seed, over)

@@ -57,6 +57,16 @@ def load():
         "orc_setvdrydep": [I, I, I, DP, DP, DP, DP, DP, DP, DP, DP, DP],
         "orc_meteo_scale": [I, I, I, I, D, D, DP, DP, DP, DP, DP, DP, DP, DP, DP, DP],
         "orc_outputs": [DP, DP, I, I, I, I, DP, DP, DP, DP, DP],
+        "orc_out_column": [DP, I, I, I, IP, I, DP, DP, DP],
+        "orc_out_ground": [DP, I, I, I, IP, I, DP, DP],
+        "orc_pm_classes": [I, DP, I, IP],
+        "orc_out_aot": [DP, I, I, I, I, DP, DP, DP, DP, DP],
+        "orc_out_thick": [DP, I, I, I, DP, DP, DP],
+        "orc_standard_pressure": [D],
+        "orc_setcut_fl": [I, I, I, DP, DP, DP, D],
+        "orc_ter2asl": [DP, DP, DP, I, I, I],
+        "orc_out_fl": [DP, I, I, I, I, DP, D, DP, DP],
+        "orc_out_con": [DP, I, I, I, I, I, DP, DP, DP, I, DP],
         "orc_ctx_create": [VP, I],
         "orc_ctx_destroy": [VP],
         "orc_meteo": [VP] + [DP] * 12,
@@ -74,7 +84,8 @@ def load():
         "orc_run": [VP, VP, VP, D, D, I, VP, I, IP],
     }
     ret = {"orc_get_gama": I, "orc_vsettl": I, "orc_setvset": I, "orc_setsrc": I,
-           "orc_ctx_create": VP, "orc_meteo": I, "orc_source": I, "orc_step": I, "orc_run": I}
+           "orc_ctx_create": VP, "orc_meteo": I, "orc_source": I, "orc_step": I, "orc_run": I,
+           "orc_pm_classes": I, "orc_standard_pressure": D}
     for name, args in sig.items():
         f = getattr(lib, name)
         f.argtypes = args
@@ -89,6 +100,59 @@ def p(a):
 
 def ip(a):
     return _abi.iptr(a)
+
+
+def output(grid, fields, var, index=0, asl=False, p_levels=None, flight_level=None):
+    """The oracle's printres_nc.f90 variable `var` (fall3d_gb300.OUT_*) of a
+    state: fields = dict(c (nc, nz+2, ny+2, nx+2), cdry, cwet (nc+1, ny, nx))
+    as f3d_download returns them; p_levels and flight_level for the cut."""
+    import fall3d_gb300 as F
+
+    lib = load()
+    nx, ny, nz, nc, np_ = grid["nx"], grid["ny"], grid["nz"], grid["nc"], grid["np"]
+    c = np.ascontiguousarray(fields["c"], dtype=np.float64)
+    dz = np.ascontiguousarray(grid["dz"], dtype=np.float64)
+    hm = np.ascontiguousarray(grid["Hm1"], dtype=np.float64)
+    diam = np.ascontiguousarray(grid["diam"], dtype=np.float64)
+    rhop = np.ascontiguousarray(grid["rhop"], dtype=np.float64)
+    out2 = np.zeros((ny, nx))
+    if var in (F.OUT_LOAD, F.OUT_WET, F.OUT_THICK):
+        cdry = np.array(fields["cdry"], dtype=np.float64)
+        cwet = np.array(fields["cwet"], dtype=np.float64)
+        cload = np.zeros_like(cdry)
+        lib.orc_getc0(p(cdry), p(cwet), p(cload), nx, ny, nc, np_)
+        if var == F.OUT_THICK:
+            lib.orc_out_thick(p(cload), nx, ny, np_, p(rhop), p(hm), p(out2))
+            return out2
+        f = cload if var == F.OUT_LOAD else cwet
+        return f[index] / hm
+    if var in (F.OUT_COL_MASS, F.OUT_C_GRND, F.OUT_PM_COL, F.OUT_PM_GRND):
+        if var in (F.OUT_PM_COL, F.OUT_PM_GRND):
+            cls = np.zeros(max(np_, 1), np.int32)
+            n = lib.orc_pm_classes(np_, p(diam), int(index), ip(cls))
+        elif var == F.OUT_COL_MASS and index > 0:
+            cls, n = np.array([np_ + index - 1], np.int32), 1
+        else:
+            cls, n = np.arange(max(np_, 1), dtype=np.int32), np_
+        if var in (F.OUT_COL_MASS, F.OUT_PM_COL):
+            lib.orc_out_column(p(c), nx, ny, nz, ip(cls), n, p(dz), p(hm), p(out2))
+        else:
+            lib.orc_out_ground(p(c), nx, ny, nz, ip(cls), n, p(hm), p(out2))
+        return out2
+    if var == F.OUT_AOT05:
+        lib.orc_out_aot(p(c), nx, ny, nz, np_, p(diam), p(rhop), p(dz), p(hm), p(out2))
+        return out2
+    if var == F.OUT_CON:
+        out3 = np.zeros((nz, ny, nx))
+        zl = np.ascontiguousarray(grid["zlayer"], dtype=np.float64)
+        tg = np.ascontiguousarray(grid["topg"], dtype=np.float64)
+        lib.orc_out_con(p(c), nx, ny, nz, np_, int(index), p(hm), p(zl), p(tg), int(bool(asl)), p(out3))
+        return out3
+    if var == "fl":
+        pl = np.ascontiguousarray(p_levels, dtype=np.float64)
+        lib.orc_out_fl(p(c), nx, ny, nz, np_, p(pl), float(flight_level), p(hm), p(out2))
+        return out2
+    raise ValueError(var)
 
 
 class OracleCtx:

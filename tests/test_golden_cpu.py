@@ -63,3 +63,23 @@ def test_oracle_coefficients_match_reference_golden(name):
     assert_same_bits(f["vset"].ravel()[::stride], g["coef_vset"].ravel(), "vset")
     assert_same_bits(f["vdep"].ravel(), g["coef_vdep"].ravel(), "vdep")
     assert o.state()["dt"] == float(g["coef_dt"])
+
+
+def test_output_cuts_match_reference_golden():
+    """Flight-level cuts (setcut_FL with standard_atm) and the terrain-following
+    to sea-level conversion (ter2asl) of the oracle against the reference's
+    own Fortran of Sources/setcut.f90 and Sources/ter2asl.f90."""
+    g = np.load(os.path.join(HERE, "output_cuts.npz"))
+    lib = O.load()
+    nz, ny, nx = g["var3d"].shape
+    zl, topg = np.ascontiguousarray(g["zlayer"]), np.ascontiguousarray(g["topg"])
+    var3d, pres = np.ascontiguousarray(g["var3d"]), np.ascontiguousarray(g["pres"])
+    for n, fl in enumerate(g["fls"]):
+        out = np.zeros((ny, nx))
+        lib.orc_setcut_fl(nx, ny, nz, O.p(out), O.p(var3d), O.p(pres), float(fl) * 30.48)
+        assert_same_bits(out, g["cut"][n], f"FL{fl:g}")
+    patm = np.array([lib.orc_standard_pressure(float(z)) for z in g["zs"]])
+    assert_same_bits(patm, g["patm"], "standard_atm")
+    conc = np.array(g["conc"])
+    lib.orc_ter2asl(O.p(conc), O.p(topg), O.p(zl), nx, ny, nz)
+    assert_same_bits(conc, g["asl"], "ter2asl")
