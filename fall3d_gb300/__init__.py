@@ -101,6 +101,7 @@ def load(build_if_missing: bool = False):
         "f3d_outputs": [VP, VP, VP, VP],
         "f3d_output": [VP, I, I, I, VP, I],
         "f3d_output_fl": [VP, D, VP, VP, I],
+        "f3d_set_gravity_current": [VP, VP],
         "f3d_run": [VP, VP, VP, D, D, I, VP, I, IP],
         "f3d_run_reset": [VP],
         "f3d_sync": [VP],
@@ -439,6 +440,15 @@ class Context:
         a = [np.zeros((self.ny, self.nx)) for _ in range(3)]
         _check(self.lib.f3d_outputs(self.h, *[_addr(x) for x in a]))
         return dict(load=a[0], col_mass=a[1], c_grnd=a[2])
+
+    def set_gravity_current(self, params=None):
+        """GRAVITY_CURRENT = YES with the parameters of synth.gravity_current
+        (a dict with the f3d_gravity_current fields); None switches it off."""
+        if params is None:
+            _check(self.lib.f3d_set_gravity_current(self.h, None))
+        else:
+            st = _abi.make_gravity_current(params)
+            _check(self.lib.f3d_set_gravity_current(self.h, C.addressof(st)))
 
     def output(self, var, index=0, asl=False, binary32=False):
         """One output variable of printres_nc.f90 (OUT_*): (ny, nx), or

@@ -44,6 +44,18 @@ class F3DSrcSeries(C.Structure):
     ]
 
 
+class F3DGravityCurrent(C.Structure):
+    """f3d_gravity_current (include/fall3d_gpu.h)."""
+
+    _fields_ = [(n, C.c_double) for n in ("c_flow_rate", "lambda_grav", "k_entrain", "brunt_vaisala",
+                                          "center_x", "center_y", "xorigr", "yorigr", "h_tot",
+                                          "beg_time")]
+
+
+def make_gravity_current(p: dict) -> F3DGravityCurrent:
+    return F3DGravityCurrent(**{k: float(p[k]) for k, _ in F3DGravityCurrent._fields_})
+
+
 class F3DLogRecord(C.Structure):
     _fields_ = [
         ("iiter", C.c_int), ("time", C.c_double), ("dt", C.c_double), ("dtc", C.c_double),

@@ -296,6 +296,14 @@ void launch_meteo_scale(Dims d, int coord_sys, double dX1, double dX2, const dou
   }
 }
 
+void launch_setdivu(Dims d, double dX1, double dX2, const double* dz, const double* Hm1,
+                    const double* vx, const double* vy, const double* vz, double* divu,
+                    cudaStream_t s) {
+  const long long n = d.cells();
+  k_setdivu<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, dX1, dX2, dz, Hm1, vx, vy, vz, divu);
+  count_launch();
+}
+
 // reamet.f90:146 (PRATE mm/s -> mm/h when wet deposition is on) and
 // reamet.f90:153 (vz(:,:,1) = 0).
 __global__ void k_reamet_fix(Dims d, int wetdep, double* vz, double* prate) {

@@ -376,6 +376,8 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
   x->prec = g->precision;
   x->h_diam.assign(g->diam, g->diam + g->nc);
   x->h_rhop.assign(g->rhop, g->rhop + g->nc);
+  x->h_zlayer.assign(g->zlayer, g->zlayer + g->nz);
+  x->hm11 = g->Hm1[0];
   for (int k = 1; k < g->nz; ++k)
     if (!(g->zlayer[k] >= g->zlayer[k - 1])) x->fused_ok = 0;
   if (x->d.halo() >= (1LL << 31) || x->d.cells() >= (1LL << 31)) x->fused_ok = 0;
@@ -548,9 +550,13 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
   // meteo.f90:100 setvdrydep (tempe(:,:,1), unscaled rho(:,:,1))
   launch_setvdrydep(d, g.nc, x->diam, x->zlayer, x->ldu, x->rl, x->znt, x->ustar, x->tempe, x->rho,
                     x->vdep, s);
-  // meteo.f90:108-145 scaling, corvver, setdivu
+  // meteo.f90:108-135 scaling and corvver, :140 addradialwind, :145 setdivu
   launch_meteo_scale(d, g.coord_sys, g.dX1, g.dX2, x->dz, x->Hm1, x->topg, x->vx, x->vy, x->vz,
-                     x->rho, x->rkhor, x->rkh1, x->divu, s);
+                     x->rho, x->rkhor, x->rkh1, nullptr, s);
+  if (x->gc_on) {
+    if (int r = f3d::gc_addradialwind(x)) return r;
+  }
+  launch_setdivu(d, g.dX1, g.dX2, x->dz, x->Hm1, x->vx, x->vy, x->vz, x->divu, s);
   // meteo.f90:149 finddt
   CK(cudaMemsetAsync(small_dtcn(x), 0, sizeof(unsigned long long), s));
   launch_finddt(d, g.nc, g.dX1, g.dX2, x->dz, x->vx, x->vy, x->vz, x->vset, x->rkh1, x->rkhor,
@@ -636,6 +642,10 @@ int f3d_source(f3d_ctx* x, int nsou, const int* isrc, const int* jsrc, const int
                   cudaMemcpyDeviceToHost));
   for (int s = 0; s < nsou; ++s)
     for (int ic = 0; ic < nc; ++ic) ht[(size_t)s + (size_t)nsou * ic] *= hm[s];
+  double mfr = 0.0;  // SUM of the scaled tmrat in element order (addradialwind.f90:61)
+  for (int ic = 0; ic < nc; ++ic)
+    for (int s = 0; s < nsou; ++s) mfr = mfr + ht[(size_t)s + (size_t)nsou * ic];
+  x->mfr_scaled = mfr;
   if (nsou > x->src_cap) {
     int cap = nsou;
     int rc = dalloc(x, &x->isrc, cap);
@@ -1071,22 +1081,29 @@ void ctx_advance(f3d_ctx* x) {  // Fall3d.f90:112-114
 int ctx_log(f3d_ctx* x, f3d_log_record* log, int log_cap, int* nlog) {
   // endstep.f90:51: mass budget every 10 minutes of simulated time
   if (x->iiter == 1 || std::fmod(x->time, 600.0) <= x->dt) {
-    if (log && nlog && *nlog < log_cap) {
-      double b[4];
+    const bool rec = log && nlog && *nlog < log_cap;
+    if (rec || x->gc_on) {
+      double b[4], outmass = 0.0;
       int r2 = f3d_budget(x, &b[0], &b[1], &b[2], &b[3]);
+      if (!r2) r2 = f3d_get_state(x, nullptr, nullptr, nullptr, nullptr, nullptr, &outmass, nullptr);
       if (r2) return r2;
-      f3d_log_record& r = log[(*nlog)++];
-      r.iiter = x->iiter;
-      r.time = x->time;
-      r.dt = x->dt;
-      r.dtc = x->dtc;
-      r.massvol = b[0];
-      r.massdep = b[1];
-      r.massdry = b[2];
-      r.masswet = b[3];
-      r2 = f3d_get_state(x, nullptr, nullptr, nullptr, nullptr, nullptr, &r.outmass, nullptr);
-      if (r2) return r2;
-      r.erumass = x->erumass;
+      if (rec) {
+        f3d_log_record& r = log[(*nlog)++];
+        r.iiter = x->iiter;
+        r.time = x->time;
+        r.dt = x->dt;
+        r.dtc = x->dtc;
+        r.massvol = b[0];
+        r.massdep = b[1];
+        r.massdry = b[2];
+        r.masswet = b[3];
+        r.outmass = outmass;
+        r.erumass = x->erumass;
+      }
+      // endstep.f90:71: after writim
+      if (x->gc_on) {
+        if (int r3 = gc_divcorr(x, b[0], b[1], outmass)) return r3;
+      }
     }
   }
   return F3D_OK;

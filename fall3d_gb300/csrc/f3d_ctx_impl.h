@@ -19,6 +19,12 @@ struct f3d_ctx {
   double *dz = nullptr, *zlayer = nullptr, *Hm1 = nullptr, *topg = nullptr;
   double *diam = nullptr, *rhop = nullptr, *psi = nullptr, *sphe = nullptr;
   std::vector<double> h_diam, h_rhop;  // host copies (output class selections)
+  std::vector<double> h_zlayer;        // host copy (gravity current levels)
+  double hm11 = 1.0;                   // Hm1(1,1)
+  // gravity current (f3d_set_gravity_current)
+  f3d_gravity_current gc{};
+  int gc_on = 0;
+  double mfr_scaled = 0.0;  // sum of the Hm1-scaled source rates (addradialwind.f90:61)
   // met and coefficients (binary64)
   double *vx = nullptr, *vy = nullptr, *vz = nullptr, *tempe = nullptr, *vptemp = nullptr;
   double *rho = nullptr, *rkhor = nullptr, *rkh1 = nullptr, *rkver = nullptr, *divu = nullptr;
@@ -87,4 +93,8 @@ int ctx_log(f3d_ctx* x, f3d_log_record* log, int log_cap, int* nlog);
 // arguments of the fused precision-form step for the context's state
 FusedArgs ctx_fused_args(f3d_ctx* x);
 inline double* ctx_outmass(f3d_ctx* x) { return x->small; }
+// gravity current (f3d_gravity.cu): addradialwind on the scaled winds of
+// a meteo update, divcorr with the budget of a log step
+int gc_addradialwind(f3d_ctx* x);
+int gc_divcorr(f3d_ctx* x, double massvol, double massdep, double outmass);
 }  // namespace f3d

@@ -149,6 +149,10 @@ void launch_meteo_scale(Dims d, int coord_sys, double dX1, double dX2, const dou
                         const double* Hm1, const double* topg, double* vx, double* vy,
                         double* vz, double* rho, const double* rkhor, double* rkh1,
                         double* divu, cudaStream_t s);
+// Sources/setdivu.f90: divu of the scaled velocities
+void launch_setdivu(Dims d, double dX1, double dX2, const double* dz, const double* Hm1,
+                    const double* vx, const double* vy, const double* vz, double* divu,
+                    cudaStream_t s);
 void launch_reamet_fix(Dims d, int wetdep, double* vz, double* prate, cudaStream_t s);
 
 // setvset with the cd chain.  Work buffers come from setvset_scratch_bytes.

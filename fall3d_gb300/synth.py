@@ -361,9 +361,25 @@ def make_scenario(name="cfg0", seed=0, **over) -> Scenario:
                 safety_factor=p["safety"], vset_factor=1.0, dz=g["dz"], zlayer=zl,
                 Hm1=g["Hm1"], topg=topg, diam=cls["diam"], rhop=cls["rhop"], psi=np.asarray(psi, float),
                 sphe=cls["sphe"])
-    info = dict(params=p, classes=cls["names"], fc=cls["fc"], vent=(iv + 1, jv + 1))
+    info = dict(params=p, classes=cls["names"], fc=cls["fc"], vent=(iv + 1, jv + 1),
+                origin=(float(g["xs"][0]), float(g["ys"][0])),
+                vent_xy=(float(g["xs"][iv]), float(g["ys"][jv])),
+                zs=[float(zl[k]) for k in ks])
     return Scenario(name=name, seed=seed, grid=grid, met=met, src=src, beg_time=0.0,
                     end_time=float(run_s), info=info)
+
+
+def gravity_current(scen: Scenario, c_flow_rate=430.0, lambda_grav=0.2, k_entrain=0.1,
+                    brunt_vaisala=0.02) -> dict:
+    """Parameters of the GRAVITY_CURRENT block (Sources/readat.f90:150-213)
+    for a scenario: the centre on the vent, the grid origin (reagrd.f90:152)
+    and the top of the source column (maxval(zs), the source points'
+    heights)."""
+    return dict(c_flow_rate=c_flow_rate, lambda_grav=lambda_grav, k_entrain=k_entrain,
+                brunt_vaisala=brunt_vaisala, center_x=scen.info["vent_xy"][0],
+                center_y=scen.info["vent_xy"][1], xorigr=scen.info["origin"][0],
+                yorigr=scen.info["origin"][1], h_tot=max(scen.info["zs"]) if scen.info["zs"] else 0.0,
+                beg_time=scen.beg_time)
 
 
 def ensemble_member(seed: int, run_h: float = 12.0, max_snapshots=None, met_dt_h: float = 1.0) -> Scenario:

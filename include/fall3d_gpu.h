@@ -429,6 +429,23 @@ int f3d_output(f3d_ctx* ctx, int var, int index, int asl, void* dst,
 int f3d_output_fl(f3d_ctx* ctx, double flight_level, const double* p,
                   void* dst, int dst_type);
 
+/* Gravity current of the umbrella cloud (Costa and Macedonio;
+ * GRAVITY_CURRENT = YES, Sources/readat.f90:150-213).  While it is on, every
+ * f3d_meteo adds the radial wind of Sources/addradialwind.f90 to the scaled
+ * vx, vy after corvver and before setdivu and finddt (meteo.f90:140), and
+ * every mass-budget log step of f3d_run applies Sources/divcorr.f90 after
+ * the budget (endstep.f90:71).  NULL switches it off.  Not available in a
+ * batch (f3d_batch_add rejects such a context). */
+typedef struct f3d_gravity_current {
+  double c_flow_rate, lambda_grav, k_entrain, brunt_vaisala; /* readat.f90:169-205 */
+  double center_x, center_y; /* radial_wind_lon/lat (LON-LAT) or radial_wind_x/y
+                                (UTM): the vent (readat.f90:209-212)          */
+  double xorigr, yorigr;     /* grid origin (Sources/reagrd.f90:152-153)      */
+  double h_tot;              /* maxval(zs): the highest source point, m       */
+  double beg_time;           /* the run's start (time of the eruption onset)  */
+} f3d_gravity_current;
+int f3d_set_gravity_current(f3d_ctx* ctx, const f3d_gravity_current* gc);
+
 /* Sources/Fall3d.f90:73-121: the time loop from beg_time to end_time
  * (at most max_steps steps if max_steps > 0), reading meteorology and
  * sources when their intervals end, logging the mass budget at the steps

@@ -908,6 +908,21 @@ void orc_setvdrydep(int nx, int ny, int nc, const double* diam,
 
 /* ----------------------------------------------- scaling, corvver, divu */
 /* Sources/meteo.f90:108-123, Sources/corvver.f90:21-34, setdivu.f90:16-30 */
+/* Sources/setdivu.f90 */
+static void orc_setdivu(int nx, int ny, int nz, double dX1, double dX2, const double* dz,
+                        const double* Hm1, const double* vx, const double* vy, const double* vz,
+                        double* divu) {
+  Dims d{nx, ny, nz};
+  for (int i = 1; i <= nx; ++i)
+    for (int j = 1; j <= ny; ++j)
+      for (int k = 1; k <= nz; ++k) {
+        const double vi = vx[d.M(i, j, k)], vi_1 = vx[d.M(std::max(1, i - 1), j, k)];
+        const double vj = vy[d.M(i, j, k)], vj_1 = vy[d.M(i, std::max(1, j - 1), k)];
+        const double vk = vz[d.M(i, j, k)], vk_1 = vz[d.M(i, j, std::max(1, k - 1))];
+        divu[d.M(i, j, k)] = (vi - vi_1) / (Hm1[d.P(i, j)] * dX1) + (vj - vj_1) / dX2 + (vk - vk_1) / dz[k];
+      }
+}
+
 void orc_meteo_scale(int nx, int ny, int nz, int coord_sys, double dX1,
                      double dX2, const double* dz, const double* Hm1,
                      const double* topg, double* vx, double* vy, double* vz,
@@ -936,16 +951,7 @@ void orc_meteo_scale(int nx, int ny, int nz, int coord_sys, double dX1,
         }
       }
   }
-  if (divu) {
-    for (int i = 1; i <= nx; ++i)
-      for (int j = 1; j <= ny; ++j)
-        for (int k = 1; k <= nz; ++k) {
-          const double vi = vx[d.M(i, j, k)], vi_1 = vx[d.M(std::max(1, i - 1), j, k)];
-          const double vj = vy[d.M(i, j, k)], vj_1 = vy[d.M(i, std::max(1, j - 1), k)];
-          const double vk = vz[d.M(i, j, k)], vk_1 = vz[d.M(i, j, std::max(1, k - 1))];
-          divu[d.M(i, j, k)] = (vi - vi_1) / (Hm1[d.P(i, j)] * dX1) + (vj - vj_1) / dX2 + (vk - vk_1) / dz[k];
-        }
-  }
+  if (divu) orc_setdivu(nx, ny, nz, dX1, dX2, dz, Hm1, vx, vy, vz, divu);
 }
 
 /* --------------------------------------------------------- output fields */
@@ -1213,6 +1219,9 @@ struct orc_ctx {
   // f3d_run loop state (Fall3d.f90:73-78)
   int run_started = 0, meteotime = 1, sourcetime = 1;
   double meteo_time = 0.0, source_time = 0.0;
+  // gravity current (readat.f90:150-213)
+  int gc_on = 0;
+  f3d_gravity_current gc{};
 };
 
 orc_ctx* orc_ctx_create(const f3d_grid* g, int nthreads) {
@@ -1251,6 +1260,103 @@ orc_ctx* orc_ctx_create(const f3d_grid* g, int nthreads) {
 
 void orc_ctx_destroy(orc_ctx* x) { delete x; }
 
+/* gfortran MAX/MIN of two reals (see the header) */
+static double orc_fmin2(double a, double b) { return (b < a || std::isnan(a)) ? b : a; }
+
+/* Sources/addradialwind.f90:46-166 on the scaled winds of the context */
+static void orc_addradialwind(orc_ctx* x) {
+  const f3d_gravity_current& gc = x->gc;
+  const int nx = x->nx, ny = x->ny, nz = x->nz;
+  Dims d{nx, ny, nz};
+  const double pi = 3.14159265358979323846;
+  const double min_radius =
+      (double)1.5f * std::sqrt(x->Hm1[0] * x->dX1 * x->Hm1[0] * x->dX1 + x->dX2 * x->dX2);
+  const double wind_center_x = gc.center_x, wind_center_y = gc.center_y;
+  const double time_eruption = x->time - gc.beg_time;
+  double mass_flow_rate = 0.0;  /* sum(tmrat(1:nsou,1:nc)) in element order */
+  for (int ic = 0; ic < x->nc; ++ic)
+    for (int is = 0; is < x->nsou; ++is) mass_flow_rate = mass_flow_rate + x->tmrat[(size_t)is + (size_t)x->nsou * ic];
+  if (mass_flow_rate <= (double)0.1f) return;
+  const double vol_flow_rate = gc.c_flow_rate * std::sqrt(gc.k_entrain) * std::pow(mass_flow_rate, 0.75) /
+                               std::pow(gc.brunt_vaisala, 0.625);
+  const double c_gravr = 3.0 * gc.lambda_grav * gc.brunt_vaisala * vol_flow_rate / (2.0 * pi);
+  double radius_grav = std::pow(c_gravr * (time_eruption * time_eruption), 0.33333);
+  radius_grav = fmax2(radius_grav, min_radius);
+  const double c_gravu = std::sqrt(2.0 * gc.lambda_grav * gc.brunt_vaisala * vol_flow_rate / (3.0 * pi));
+  const double c_grav_factor = 0.75 * c_gravu * std::sqrt(radius_grav);
+  const double th_grav = c_gravu / (std::sqrt(radius_grav) * gc.lambda_grav * gc.brunt_vaisala);
+  const double h_tot = gc.h_tot;
+  const double h_umbr = h_tot / 1.32;
+  const double hmin = fmax2(h_umbr - 0.5 * th_grav, 0.5 * h_tot);
+  const double hmax = orc_fmin2(h_umbr + 0.5 * th_grav, h_tot);
+  int i_wind = (int)((wind_center_x - gc.xorigr) / x->dx);
+  int j_wind = (int)((wind_center_y - gc.yorigr) / x->dy);
+  i_wind = std::max(1, i_wind);
+  j_wind = std::max(1, j_wind);
+  int k_wind = 1;
+  double store = x->zlayer[nz - 1];
+  for (int k = 1; k <= nz; ++k) {
+    const double dist = std::fabs(x->zlayer[k - 1] - h_umbr);
+    if (dist <= store) { k_wind = k; store = dist; }
+  }
+  const double wx = x->vx[d.M(i_wind, j_wind, k_wind)], wy = x->vy[d.M(i_wind, j_wind, k_wind)];
+  const double v_wind = std::sqrt(wx * wx + wy * wy);
+  const double max_radius = 1.7777 * c_gravr / fmax2(v_wind * v_wind, 0.1);
+  int kmin = 1;
+  store = x->zlayer[nz - 1];
+  for (int k = 1; k <= nz; ++k) {
+    const double dist = std::fabs(x->zlayer[k - 1] - hmin);
+    if (dist <= store) { kmin = k; store = dist; }
+  }
+  int kmax = nz;
+  store = x->zlayer[nz - 1];
+  for (int k = 1; k <= nz; ++k) {
+    const double dist = std::fabs(x->zlayer[k - 1] - hmax);
+    if (dist <= store) { kmax = k; store = dist; }
+  }
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      const double h = x->Hm1[d.P(i, j)];
+      const double deltax = x->dX1 * h * ((gc.xorigr + i * x->dx) - wind_center_x) / x->dx;
+      const double deltay = x->dX2 * ((gc.yorigr + j * x->dy) - wind_center_y) / x->dy;
+      const double radius = std::sqrt(deltax * deltax + deltay * deltay);
+      if (std::fabs(radius) <= min_radius) continue;
+      if (std::fabs(radius) > max_radius) continue;
+      const double rvel = c_grav_factor / radius * (1.0 + radius * radius / (3.0 * (radius_grav * radius_grav)));
+      for (int k = kmin; k <= kmax; ++k) {
+        x->vx[d.M(i, j, k)] = x->vx[d.M(i, j, k)] + rvel * deltax / radius / h;
+        x->vy[d.M(i, j, k)] = x->vy[d.M(i, j, k)] + rvel * deltay / radius;
+      }
+    }
+}
+
+/* Sources/divcorr.f90:21-38 with the budget of the log step */
+static void orc_divcorr(orc_ctx* x, double massvol, double massdep) {
+  const double compmass = massvol + massdep + x->outmass;
+  const double eps = 0.005, eps1 = 10.0 * eps;
+  const double corrdiv = fmax2(orc_fmin2((x->erumass - compmass) / (x->erumass), eps1), -eps1);
+  Dims d{x->nx, x->ny, x->nz};
+  for (int k = 1; k <= x->nz; ++k)
+    for (int j = 1; j <= x->ny; ++j)
+      for (int i = 1; i <= x->nx; ++i) {
+        const double dive = x->divu[d.M(i, j, k)];
+        if (std::fabs(dive * x->dt) >= eps)
+          for (int ic = 1; ic <= x->nc; ++ic) {
+            double& c = x->c[(size_t)(ic - 1) * d.halo() + d.C(i, j, k)];
+            c = c * (1.0 + corrdiv);
+          }
+      }
+}
+
+void orc_set_gravity_current(orc_ctx* x, const f3d_gravity_current* gc) {
+  if (gc) {
+    x->gc = *gc;
+    x->gc_on = 1;
+  } else {
+    x->gc_on = 0;
+  }
+}
+
 /* Sources/meteo.f90:19-149 for one snapshot (reamet.f90:146,153 included). */
 int orc_meteo(orc_ctx* x, const double* u, const double* v, const double* w,
               const double* t, const double* tp, const double* rho,
@@ -1285,7 +1391,10 @@ int orc_meteo(orc_ctx* x, const double* u, const double* v, const double* w,
                  x->znt.data(), x->ustar.data(), x->tempe.data(), x->rho.data(), x->vdep.data());
   orc_meteo_scale(nx, ny, nz, x->coord, x->dX1, x->dX2, x->dz.data(), x->Hm1.data(), x->topg.data(),
                   x->vx.data(), x->vy.data(), x->vz.data(), x->rho.data(), x->rkhor.data(),
-                  x->rkh1.data(), x->divu.data());
+                  x->rkh1.data(), nullptr);
+  if (x->gc_on) orc_addradialwind(x);  // meteo.f90:140
+  orc_setdivu(nx, ny, nz, x->dX1, x->dX2, x->dz.data(), x->Hm1.data(), x->vx.data(), x->vy.data(),
+              x->vz.data(), x->divu.data());
   orc_finddt(nx, ny, nz, x->nc, x->dX1, x->dX2, x->dz.data(), x->vx.data(), x->vy.data(),
              x->vz.data(), x->vset.data(), x->rkh1.data(), x->rkhor.data(), x->rkver.data(),
              x->safety, &x->dt, &x->dtc);
@@ -1491,13 +1600,17 @@ int orc_run(orc_ctx* x, const f3d_met_series* met, const f3d_src_series* src,
     ++steps;
     // endstep.f90:51: log every 10 minutes of simulated time
     if (x->iiter == 1 || std::fmod(x->time, 600.0) <= x->dt) {
-      if (log && nlog && *nlog < log_cap) {
+      const bool rec = log && nlog && *nlog < log_cap;
+      if (rec || x->gc_on) {
         double b[4];
         orc_budget(x, b);
-        f3d_log_record& r = log[(*nlog)++];
-        r.iiter = x->iiter; r.time = x->time; r.dt = x->dt; r.dtc = x->dtc;
-        r.massvol = b[0]; r.massdep = b[1]; r.massdry = b[2]; r.masswet = b[3];
-        r.outmass = x->outmass; r.erumass = x->erumass;
+        if (rec) {
+          f3d_log_record& r = log[(*nlog)++];
+          r.iiter = x->iiter; r.time = x->time; r.dt = x->dt; r.dtc = x->dtc;
+          r.massvol = b[0]; r.massdep = b[1]; r.massdry = b[2]; r.masswet = b[3];
+          r.outmass = x->outmass; r.erumass = x->erumass;
+        }
+        if (x->gc_on) orc_divcorr(x, b[0], b[1]);  /* endstep.f90:71 */
       }
     }
     if (x->time >= end_time) go_on = false;

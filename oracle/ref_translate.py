@@ -48,15 +48,16 @@ UNIT_FILES = ["setbcc.f90", "advctzc.f90", "advctx.f90", "advcty.f90", "diffz.f9
               "diffy.f90", "wetdep.f90", "accum.f90", "cmass2d.f90", "cmass3d.f90", "finddt.f90",
               "kappa3.f90", "setvset.f90", "setpsi.f90", "setvdrydep.f90", "corvver.f90",
               "setdivu.f90", "setsrc.f90", "sizloop.f90", "meteo.f90", "source.f90", "endstep.f90",
-              "setcut.f90", "ter2asl.f90"]
+              "setcut.f90", "ter2asl.f90", "addradialwind.f90", "divcorr.f90"]
 # units from those files that are translated (others in the files are skipped)
 WANTED = {"setbcc", "advctzc", "advctx", "advcty", "diffz", "diffx", "diffy", "wetdep", "accum",
           "cmass2d", "cmass3d", "finddt", "kappa3", "setvset", "vsettl", "setpsi", "get_gama",
           "setvdrydep", "corvver", "setdivu", "setsrc", "sizloop", "meteo", "source", "getc0",
-          "getmem1", "getmem2", "outmem2", "setcut_fl", "standard_atm", "ter2asl"}
+          "getmem1", "getmem2", "outmem2", "setcut_fl", "standard_atm", "ter2asl",
+          "addradialwind", "divcorr"}
 NOOP_CALLS = {"bcast", "parallel_sum", "exchange_1layer", "exchange_2layer", "collect_cz",
               "collect_c", "collect_cload", "addtime", "wriwar", "flush", "reamet", "reasrc",
-              "addradialwind", "settemplume", "agrsrc", "cpu_time"}
+              "settemplume", "agrsrc", "cpu_time"}
 SKIP_STMTS = ("write", "format", "print", "open", "close", "read", "rewind", "inquire")
 
 # module scalars supplied by the serial runtime (Sources/Parallel.F90 and
@@ -695,7 +696,9 @@ class Gen:
     def intrinsic(self, name, args, elem):
         if name == "sum":
             return self.reduce_sum(args[0])
-        if name in ("maxval", "minval", "size"):
+        if name in ("maxval", "minval"):
+            return self.reduce_ext(args[0], name == "maxval")
+        if name == "size":
             return "0", "int"
         vals = [self.e(a, elem) for a in args if a[0] != "kw"]
         texts = [v[0] for v in vals]
@@ -769,6 +772,30 @@ class Gen:
         for d in reversed(range(len(lo_hi))):
             loops += f"for (long long {vars_[d]} = 0; {vars_[d]} < ({lo_hi[d][1]}); {vars_[d]}++) "
         lines.append(loops + "{ " + " ".join(inner) + f" {acc} = {acc} + {body}; }}")
+        self.pre.extend(lines)
+        return acc, ty
+
+    def reduce_ext(self, arr, is_max):
+        """MAXVAL / MINVAL (whole array or section) of a real array: the
+        largest (smallest) element, NaN elements skipped; -HUGE (+HUGE) for
+        an empty one, as gfortran returns."""
+        lo_hi = self.section_extents(arr)
+        acc = self.newtmp()
+        ty = self.elem_type(arr)
+        huge = "DBL_MAX" if ty == "double" else "FLT_MAX"
+        lines = [f"{ty} {acc} = {'-' if is_max else ''}{huge};"]
+        vars_ = [self.newtmp() for _ in lo_hi]
+        elem = {"vars": vars_, "used": False}
+        save_pre = self.pre
+        self.pre = []
+        body, _ = self.e(arr, elem)
+        inner = self.pre
+        self.pre = save_pre
+        loops = ""
+        for d in reversed(range(len(lo_hi))):
+            loops += f"for (long long {vars_[d]} = 0; {vars_[d]} < ({lo_hi[d][1]}); {vars_[d]}++) "
+        op = ">" if is_max else "<"
+        lines.append(loops + "{ " + " ".join(inner) + f" if (({body}) {op} {acc}) {acc} = {body}; }}")
         self.pre.extend(lines)
         return acc, ty
 
@@ -1219,6 +1246,7 @@ def eval_int(text, params):
 
 RUNTIME_C = r"""
 #include <math.h>
+#include <float.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>

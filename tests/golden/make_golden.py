@@ -46,7 +46,10 @@ CASES = [
      dict(modkv=2, modkh=1, modv=3, coord=1, spacing=4000.0, rmol=-1.0 / 300.0), None),
     ("tiny_dellino_ganser_two_updates", "tiny", 5, dict(modv=4, run_h=1.5, met_dt_h=0.5), None),
     ("cfg0_first_60_steps", "cfg0", 0, {}, 60),
+    ("small_gravity_current", "small", 6, dict(M0=1e7, u10=4.0, vy0=1.0, run_h=0.75), None),
 ]
+# cases run with GRAVITY_CURRENT = YES (parameters of synth.gravity_current)
+GRAVITY = {"small_gravity_current"}
 # large cases keep every SAMPLE-th value of the 3-D/4-D fields
 SAMPLE = {"cfg0_first_60_steps": 37}
 
@@ -94,8 +97,9 @@ class RefLib:
         f(*args)
 
 
-def run_reference(scen, max_steps=None):
-    """The Fall3d.f90 loop on the translated reference; returns a dict."""
+def run_reference(scen, max_steps=None, gc=None):
+    """The Fall3d.f90 loop on the translated reference; returns a dict.
+    gc: GRAVITY_CURRENT parameters (synth.gravity_current) or None."""
     R = RefLib()
     g, m, sr = scen.grid, scen.met, scen.src
     nx, ny, nz, nc = g["nx"], g["ny"], g["nz"], g["nc"]
@@ -111,6 +115,17 @@ def run_reference(scen, max_steps=None):
                  ("dt", 1.0), ("outmass", 0.0), ("erumass", 0.0)):
         R.d(k).value = float(v)
     R.setstr("coord_sys", "LON-LAT" if g["coord_sys"] == 0 else "UTM", 10)
+    if gc:  # readat.f90:150-213, reagrd.f90:152-153
+        R.i("gravity_current").value = 1
+        for k in ("c_flow_rate", "lambda_grav", "k_entrain", "brunt_vaisala"):
+            R.d(k).value = gc[k]
+        for k in ("radial_wind_lon", "radial_wind_x"):
+            R.d(k).value = gc["center_x"]
+        for k in ("radial_wind_lat", "radial_wind_y"):
+            R.d(k).value = gc["center_y"]
+        R.d("xorigr").value = gc["xorigr"]
+        R.d("yorigr").value = gc["yorigr"]
+        R.d("beg_time").value = gc["beg_time"]
     names = (C.c_char * 26 * 50).in_dll(R.lib, "m_classname")
     for ic in range(50):
         C.memmove(names[ic], b" " * 25 + b"\0", 26)
@@ -152,6 +167,8 @@ def run_reference(scen, max_steps=None):
             R.arr("jsrc", n, C.c_int)[:] = sr["jsrc"][off:off + n]
             R.arr("ksrc", n, C.c_int)[:] = sr["ksrc"][off:off + n]
             R.arr("tmrat", n * nc)[:] = sr["tmrat"][off * nc:(off + n) * nc]
+            if gc:  # the source points' heights (get_source_coordinates)
+                R.arr("zs", n)[:] = np.full(n, gc["h_tot"]) if iint else scen.info["zs"][:n]
         R.call("source")
 
     beg, end = scen.beg_time, scen.end_time
@@ -217,6 +234,10 @@ def run_reference(scen, max_steps=None):
                          ("massdry", out[2].value), ("masswet", out[3].value),
                          ("outmass", R.d("outmass").value), ("erumass", R.d("erumass").value)):
                 log[k].append(v)
+            if gc:  # endstep.f90:71, after writim
+                R.d("massvol").value = out[0].value
+                R.d("massdep").value = out[1].value
+                R.call("divcorr")
         if time >= end or (max_steps and steps >= max_steps):
             break
     res = {"c": R.arr("c", hb * nc).copy().reshape(nc, nz + 2, ny + 2, nx + 2),
@@ -283,13 +304,20 @@ def cuts():
 
 
 def main():
-    cuts()
+    """All fixtures; --cuts only output_cuts.npz; --case NAME only that case
+    (its cases.json entry replaced)."""
+    if "--case" not in sys.argv:
+        cuts()
     if "--cuts" in sys.argv:
         return
-    meta = {}
+    only = sys.argv[sys.argv.index("--case") + 1] if "--case" in sys.argv else None
+    meta = json.load(open(os.path.join(HERE, "cases.json"))) if only else {}
     for name, workload, seed, over, max_steps in CASES:
+        if only and name != only:
+            continue
         s = scenario(workload, seed, over)
-        r = run_reference(s, max_steps)
+        gc = synth.gravity_current(s) if name in GRAVITY else None
+        r = run_reference(s, max_steps, gc)
         path = os.path.join(HERE, f"{name}.npz")
         st = SAMPLE.get(name)
         if st:
@@ -300,6 +328,8 @@ def main():
         np.savez_compressed(path, **{k: np.asarray(v) for k, v in r.items()})
         meta[name] = {"workload": workload, "seed": seed, "overrides": over, "max_steps": max_steps,
                       "steps": int(r["iiter"])}
+        if gc:
+            meta[name]["gravity_current"] = gc
         print(f"{name}: {r['iiter']} steps, {os.path.getsize(path) / 1024:.0f} KB")
     with open(os.path.join(HERE, "cases.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)

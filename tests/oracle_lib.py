@@ -81,6 +81,7 @@ def load():
         "orc_download_iters": [VP, IP],
         "orc_outputs_ctx": [VP, DP, DP, DP],
         "orc_run_reset": [VP],
+        "orc_set_gravity_current": [VP, VP],
         "orc_run": [VP, VP, VP, D, D, I, VP, I, IP],
     }
     ret = {"orc_get_gama": I, "orc_vsettl": I, "orc_setvset": I, "orc_setsrc": I,
@@ -173,6 +174,13 @@ class OracleCtx:
 
     def __del__(self):
         self.close()
+
+    def set_gravity_current(self, params=None):
+        if params is None:
+            self.lib.orc_set_gravity_current(self.h, None)
+        else:
+            self._gc = _abi.make_gravity_current(params)
+            self.lib.orc_set_gravity_current(self.h, C.addressof(self._gc))
 
     def meteo(self, it=0):
         m = self.s.met

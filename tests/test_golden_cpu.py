@@ -33,6 +33,8 @@ def test_oracle_matches_reference_golden(name):
     stride = int(g["sample_stride"]) if "sample_stride" in g else 1
     s = _scenario(meta)
     o = O.OracleCtx(s, nthreads=4)
+    if "gravity_current" in meta:
+        o.set_gravity_current(meta["gravity_current"])
     log = o.run(max_steps=meta["max_steps"] or 0)
     st = o.state()
     assert st["iiter"] == int(g["iiter"]) == meta["steps"]
@@ -54,6 +56,8 @@ def test_oracle_coefficients_match_reference_golden(name):
     stride = int(g["sample_stride"]) if "sample_stride" in g else 1
     s = _scenario(meta)
     o = O.OracleCtx(s)
+    if "gravity_current" in meta:
+        o.set_gravity_current(meta["gravity_current"])
     o.source(0)
     o.meteo(0)
     co = o.coeffs()
