@@ -30,7 +30,7 @@ PREC_FP64, PREC_FP32 = 64, 32
 OPT_FUSED, OPT_TILE, OPT_GRAPH = 1, 2, 3
 # output variables of printres_nc.f90 (f3d_output)
 (OUT_LOAD, OUT_WET, OUT_THICK, OUT_COL_MASS, OUT_PM_COL, OUT_C_GRND, OUT_PM_GRND, OUT_AOT05,
- OUT_CON) = range(1, 10)
+ OUT_CON, OUT_WIND, OUT_MAGGR) = range(1, 12)
 
 
 class F3DError(RuntimeError):
@@ -102,6 +102,10 @@ def load(build_if_missing: bool = False):
         "f3d_output": [VP, I, I, I, VP, I],
         "f3d_output_fl": [VP, D, VP, VP, I],
         "f3d_set_gravity_current": [VP, VP],
+        "f3d_set_aggregation": [VP, VP],
+        "f3d_aggregation_met": [VP, VP, VP],
+        "f3d_aggregation_plume": [VP, I, VP, VP, VP, VP, VP],
+        "f3d_download_maggr": [VP, VP],
         "f3d_run": [VP, VP, VP, D, D, I, VP, I, IP],
         "f3d_run_reset": [VP],
         "f3d_sync": [VP],
@@ -450,10 +454,28 @@ class Context:
             st = _abi.make_gravity_current(params)
             _check(self.lib.f3d_set_gravity_current(self.h, C.addressof(st)))
 
+    def set_aggregation(self, agg=None):
+        """Aggregation in transport with the inputs of synth.aggregation_inputs
+        (Df, ndtagr, fc; the QV/P snapshots and plume lists are passed by
+        run()); None switches it off."""
+        self._agg = agg
+        if agg is None:
+            _check(self.lib.f3d_set_aggregation(self.h, None))
+            return
+        self._agg_fc = np.ascontiguousarray(agg["fc"], dtype=np.float64)
+        st = _abi.F3DAggregation(Df=float(agg["Df"]), ndtagr=int(agg["ndtagr"]),
+                                 fc=_abi.dptr(self._agg_fc))
+        _check(self.lib.f3d_set_aggregation(self.h, C.addressof(st)))
+
+    def maggr(self):
+        m = np.zeros((self.nz, self.ny, self.nx))
+        _check(self.lib.f3d_download_maggr(self.h, m.ctypes.data))
+        return m
+
     def output(self, var, index=0, asl=False, binary32=False):
         """One output variable of printres_nc.f90 (OUT_*): (ny, nx), or
         (nz, ny, nx) for OUT_CON; binary32 as the netCDF file holds it."""
-        shape = (self.nz, self.ny, self.nx) if var == OUT_CON else (self.ny, self.nx)
+        shape = (self.nz, self.ny, self.nx) if var in (OUT_CON, OUT_WIND, OUT_MAGGR) else (self.ny, self.nx)
         a = np.zeros(shape, np.float32 if binary32 else np.float64)
         _check(self.lib.f3d_output(self.h, int(var), int(index), int(bool(asl)), a.ctypes.data,
                                    1 if binary32 else 0))
@@ -476,8 +498,9 @@ class Context:
     # -- the Fall3d.f90 time loop -------------------------------------------
     def run(self, beg_time=None, end_time=None, max_steps=0, log_cap=4096, met=None, src=None):
         """Sources/Fall3d.f90:73-121 on the device; returns the mass-budget log."""
-        met = met or _abi.make_met(self.s.met)
-        src = src or _abi.make_src(self.s.src)
+        agg = getattr(self, "_agg", None)
+        met = met or _abi.make_met(self.s.met, agg)
+        src = src or _abi.make_src(self.s.src, agg)
         recs = (_abi.F3DLogRecord * log_cap)()
         n = C.c_int()
         _check(self.lib.f3d_run(self.h, C.addressof(met.struct), C.addressof(src.struct),

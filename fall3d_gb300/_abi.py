@@ -33,7 +33,7 @@ class F3DMetSeries(C.Structure):
         ("u", c_double_p), ("v", c_double_p), ("w", c_double_p), ("t", c_double_p),
         ("tp", c_double_p), ("rho", c_double_p),
         ("ust", c_double_p), ("pblh", c_double_p), ("rmol", c_double_p), ("znt", c_double_p),
-        ("prate", c_double_p), ("ldu", c_double_p),
+        ("prate", c_double_p), ("ldu", c_double_p), ("qv", c_double_p), ("p", c_double_p),
     ]
 
 
@@ -41,6 +41,8 @@ class F3DSrcSeries(C.Structure):
     _fields_ = [
         ("nint", C.c_int), ("t1", c_int_p), ("t2", c_int_p), ("nsou", c_int_p),
         ("isrc", c_int_p), ("jsrc", c_int_p), ("ksrc", c_int_p), ("tmrat", c_double_p),
+        ("nplume", c_int_p), ("pix", c_int_p), ("piy", c_int_p), ("piz", c_int_p),
+        ("ptemp", c_double_p), ("pwater", c_double_p),
     ]
 
 
@@ -50,6 +52,12 @@ class F3DGravityCurrent(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("c_flow_rate", "lambda_grav", "k_entrain", "brunt_vaisala",
                                           "center_x", "center_y", "xorigr", "yorigr", "h_tot",
                                           "beg_time")]
+
+
+class F3DAggregation(C.Structure):
+    """f3d_aggregation (include/fall3d_gpu.h)."""
+
+    _fields_ = [("Df", C.c_double), ("ndtagr", C.c_int), ("fc", c_double_p)]
 
 
 def make_gravity_current(p: dict) -> F3DGravityCurrent:
@@ -115,21 +123,39 @@ def make_grid(g: dict, precision: int = 64) -> Pinned:
     return Pinned(s, keep)
 
 
-def make_met(m: dict) -> Pinned:
+def make_met(m: dict, agg: dict = None) -> Pinned:
+    """f3d_met_series of a met dict; agg (synth.aggregation_inputs) adds the
+    QV and P snapshots of the aggregation model."""
     keep = {k: _f64(m[k]) for k in ("u", "v", "w", "t", "tp", "rho", "ust", "pblh", "rmol", "znt",
                                      "prate", "ldu")}
     keep["times"] = _i32(m["times"])
+    extra = {}
+    if agg is not None:
+        keep["qv"], keep["p"] = _f64(agg["qv"]), _f64(agg["p"])
+        extra = dict(qv=dptr(keep["qv"]), p=dptr(keep["p"]))
     s = F3DMetSeries(nt=len(keep["times"]), times=iptr(keep["times"]), time_lag=float(m["time_lag"]),
                      **{k: dptr(keep[k]) for k in ("u", "v", "w", "t", "tp", "rho", "ust", "pblh",
-                                                   "rmol", "znt", "prate", "ldu")})
+                                                   "rmol", "znt", "prate", "ldu")}, **extra)
     return Pinned(s, keep)
 
 
-def make_src(sr: dict) -> Pinned:
+def make_src(sr: dict, agg: dict = None) -> Pinned:
+    """f3d_src_series of a source dict; agg (synth.aggregation_inputs) adds
+    the plume temperature lists of the intervals."""
     keep = {k: _i32(sr[k]) for k in ("t1", "t2", "nsou", "isrc", "jsrc", "ksrc")}
     keep["tmrat"] = _f64(sr["tmrat"])
+    extra = {}
+    if agg is not None:
+        pl = agg["plume"]
+        keep["nplume"] = _i32([len(q["ix"]) for q in pl])
+        for k, f in (("pix", "ix"), ("piy", "iy"), ("piz", "iz")):
+            keep[k] = _i32(np.concatenate([np.asarray(q[f]) for q in pl]) if pl else [])
+        keep["ptemp"] = _f64(np.concatenate([np.asarray(q["t"]) for q in pl]) if pl else [])
+        keep["pwater"] = _f64(np.concatenate([np.asarray(q["w"]) for q in pl]) if pl else [])
+        extra = dict(nplume=iptr(keep["nplume"]), pix=iptr(keep["pix"]), piy=iptr(keep["piy"]),
+                     piz=iptr(keep["piz"]), ptemp=dptr(keep["ptemp"]), pwater=dptr(keep["pwater"]))
     s = F3DSrcSeries(nint=len(keep["t1"]), tmrat=dptr(keep["tmrat"]),
-                     **{k: iptr(keep[k]) for k in ("t1", "t2", "nsou", "isrc", "jsrc", "ksrc")})
+                     **{k: iptr(keep[k]) for k in ("t1", "t2", "nsou", "isrc", "jsrc", "ksrc")}, **extra)
     return Pinned(s, keep)
 
 

@@ -35,6 +35,7 @@ UNITS = {
     "f3d_serve.cu": ["-Xcompiler", "-fvisibility=default"],
     "f3d_output.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
     "f3d_gravity.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
+    "f3d_aggregation.cu": ["--fmad=false", "-Xcompiler", "-fvisibility=default"],
 }
 
 

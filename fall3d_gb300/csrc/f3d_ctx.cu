@@ -59,6 +59,30 @@ int dalloc(f3d_ctx* x, T** p, size_t n) {
   return F3D_OK;
 }
 
+}  // namespace
+
+namespace f3d {
+int ctx_alloc(f3d_ctx* x, void** p, size_t bytes) {
+  unsigned char* q = nullptr;
+  const int rc = dalloc(x, &q, bytes);
+  *p = q;
+  return rc;
+}
+
+void refresh_fp32_class(f3d_ctx* x, int ic) {
+  const Dims d = x->d;
+  const size_t s3 = (size_t)d.cells();
+  cudaStream_t s = x->stream;
+  launch_d2f(x->vset32 + ic * s3, x->vset + ic * s3, (long long)s3, s);
+  launch_vk32((long long)s3, 1, x->vz32, x->vset32 + ic * s3, x->vk32 + ic * s3, s);
+  const float* vs = x->vk32 + ic * s3;
+  float* vd = x->vkh + (size_t)ic * (size_t)d.halo();
+  launch_to_halo(d, 1, &vs, &vd, s);
+}
+}  // namespace f3d
+
+namespace {
+
 int is_dev(const void* p) {
   if (!p) return 0;
   cudaPointerAttributes a;
@@ -604,6 +628,7 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
     CK(cudaGetLastError());
   }
   x->have_met = 1;
+  if (x->agr_on) x->agr_due = 1;  // Fall3d.f90:94-96
   return F3D_OK;
 }
 
@@ -667,12 +692,17 @@ int f3d_source(f3d_ctx* x, int nsou, const int* isrc, const int* jsrc, const int
                        x->stream));
     CK(cudaStreamSynchronize(x->stream));  // host vectors go out of scope
   }
+  if (x->agr_on) x->agr_due = 1;  // Fall3d.f90:84-86
   return F3D_OK;
 }
 
 int f3d_step(f3d_ctx* x) {
   if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
   if (!x->have_met) return f3d::ctx_error(F3D_ERR_STATE, "f3d_step before f3d_meteo");
+  if (x->agr_on && x->agr_due) {  // Fall3d.f90:101-110: agrpar after this step's updates
+    if (int rc = f3d::agg_agrpar(x)) return rc;
+    x->agr_due = 0;
+  }
   f3d::ctx_advance(x);
   const Dims d = x->d;
   // setsrc.f90:20-35
@@ -685,6 +715,9 @@ int f3d_step(f3d_ctx* x) {
     ProfScope ps(x, "setsrc");
     launch_setsrc<double>(x->c64, d.halo(), d, x->g.nc, x->nsou, x->isrc, x->jsrc, x->ksrc, x->slink,
                           x->tmrat, x->dz, x->zlayer, x->Hm1, x->g.dX1, x->g.dX2, x->dt, x->stream);
+  }
+  if (x->agr_on) {  // setsrc.f90:37-76
+    if (int rc = f3d::agg_setsrc(x)) return rc;
   }
   if (x->prec == F3D_PREC_FP32 && x->opt_fused && x->fused_ok)
     sizloop_fused(x);
@@ -1041,6 +1074,13 @@ int ctx_run_prepare(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series*
       const int rc = f3d_source(x, src->nsou[found], src->isrc + off_found, src->jsrc + off_found,
                                 src->ksrc + off_found, src->tmrat + roff_found);
       if (rc) return rc;
+      if (x->agr_on && src->nplume) {  // settemplume at the end of source (source.f90:82)
+        size_t po = 0;
+        for (int it = 0; it < found; ++it) po += (size_t)src->nplume[it];
+        const int r2 = f3d_aggregation_plume(x, src->nplume[found], src->pix + po, src->piy + po, src->piz + po,
+                                             src->ptemp + po, src->pwater ? src->pwater + po : nullptr);
+        if (r2) return r2;
+      }
       x->source_time = (double)src->t2[found];
     }
     if (x->source_time >= end_time) x->sourcetime = 0;
@@ -1061,6 +1101,9 @@ int ctx_run_prepare(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series*
           endsec = met->times[it + 1];
         }
       const size_t o3 = (size_t)itime * s3, o2 = (size_t)itime * pl;
+      if (x->agr_on && met->qv && met->p) {
+        if (int r2 = f3d_aggregation_met(x, met->qv + o3, met->p + o3)) return r2;
+      }
       const int rc = f3d_meteo(x, met->u + o3, met->v + o3, met->w + o3, met->t + o3, met->tp + o3,
                                met->rho + o3, met->ust + o2, met->pblh + o2, met->rmol + o2,
                                met->znt + o2, met->prate ? met->prate + o2 : nullptr, met->ldu);

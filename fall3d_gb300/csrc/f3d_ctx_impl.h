@@ -25,6 +25,13 @@ struct f3d_ctx {
   f3d_gravity_current gc{};
   int gc_on = 0;
   double mfr_scaled = 0.0;  // sum of the Hm1-scaled source rates (addradialwind.f90:61)
+  // aggregation in transport (f3d_set_aggregation)
+  int agr_on = 0, agr_iaggr = 0, agr_ndtagr = 1, agr_ipass = 0, agr_due = 0;
+  double agr_Df = 3.0;
+  std::vector<double> agr_fc;  // fc(1:np)
+  double *agr_fc_dev = nullptr, *agr_cls = nullptr;
+  double *agr_al = nullptr, *agr_ab = nullptr, *agr_as = nullptr, *agr_ad = nullptr;  // Alagr..Adagr
+  double *agr_maggr = nullptr, *agr_tplume = nullptr, *agr_qv = nullptr, *agr_p = nullptr;
   // met and coefficients (binary64)
   double *vx = nullptr, *vy = nullptr, *vz = nullptr, *tempe = nullptr, *vptemp = nullptr;
   double *rho = nullptr, *rkhor = nullptr, *rkh1 = nullptr, *rkver = nullptr, *divu = nullptr;
@@ -97,4 +104,13 @@ inline double* ctx_outmass(f3d_ctx* x) { return x->small; }
 // a meteo update, divcorr with the budget of a log step
 int gc_addradialwind(f3d_ctx* x);
 int gc_divcorr(f3d_ctx* x, double massvol, double massdep, double outmass);
+// aggregation (f3d_aggregation.cu): agrpar after the updates of a step,
+// agrsrc after its point sources
+int agg_agrpar(f3d_ctx* x);
+int agg_setsrc(f3d_ctx* x);
+// a zero-filled device allocation owned by the context
+int ctx_alloc(f3d_ctx* x, void** p, size_t bytes);
+// the binary32 copies of class ic's settling velocity (vset32, vk32 and
+// its halo-layout copy) after vset changed on the device
+void refresh_fp32_class(f3d_ctx* x, int ic);
 }  // namespace f3d

@@ -172,6 +172,40 @@ __global__ void k_out_con(const T* c, Dims d, const int* cls, int ncls, const do
   }
 }
 
+// a binary64 3-D field (x fastest) times Hm1 or not, with `asl` moved to
+// heights above sea level by ter2asl: the gravity-current winds
+// (printres_nc.f90:603-644: vx*Hm1, vy*Hm1) and Maggr (:673-690)
+__global__ void k_out_field(const double* f, int times_hm1, Dims d, const double* Hm1,
+                            const double* zlayer, const double* topg, int asl, double* out) {
+  const long long p = blockIdx.x * (long long)OB + threadIdx.x;
+  const long long pl = d.plane();
+  if (p >= pl) return;
+  const double h = Hm1[p];
+  auto val = [&](int k) {
+    const double v = f[(long long)(k - 1) * pl + p];
+    return times_hm1 ? v * h : v;
+  };
+  if (!asl) {
+    for (int k = 1; k <= d.nz; ++k) out[(long long)(k - 1) * pl + p] = val(k);
+    return;
+  }
+  const double zo = fmax2(0.0, topg[p]);
+  for (int k = 1; k <= d.nz; ++k) {
+    const double zasl = zlayer[k - 1];
+    double v = 0.0;
+    if (!(zasl < zo + zlayer[0])) {
+      for (int kk = 1; kk <= d.nz - 1; ++kk) {
+        if (zasl >= zo + zlayer[kk - 1] && zasl <= zo + zlayer[kk]) {
+          const double s = (zo + zlayer[kk] - zasl) / (zlayer[kk] - zlayer[kk - 1]);
+          v = s * val(kk) + (1.0 - s) * val(kk + 1);
+          break;
+        }
+      }
+    }
+    out[(long long)(k - 1) * pl + p] = v;
+  }
+}
+
 __global__ void k_out_to_f32(const double* a, long long n, float* b) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x)
@@ -321,6 +355,14 @@ int f3d_output(f3d_ctx* x, int var, int index, int asl, void* dst, int dst_type)
         cls.push_back(index - 1);
       n = d.cells();
       break;
+    case F3D_OUT_WIND:
+      if (index != 1 && index != 2) return f3d::ctx_error(F3D_ERR_ARG, "wind component must be 1 (u) or 2 (v)");
+      n = d.cells();
+      break;
+    case F3D_OUT_MAGGR:
+      if (!x->agr_on) return f3d::ctx_error(F3D_ERR_STATE, "aggregation is off");
+      n = d.cells();
+      break;
     default:
       return f3d::ctx_error(F3D_ERR_ARG, "unknown output variable");
   }
@@ -371,6 +413,11 @@ int f3d_output(f3d_ctx* x, int var, int index, int asl, void* dst, int dst_type)
         k_out_aot<float><<<blocks(pl), OB, 0, s>>>(x->c32, d, dcls, dq, dr, ncls, x->dz, x->Hm1, res);
       else
         k_out_aot<double><<<blocks(pl), OB, 0, s>>>(x->c64, d, dcls, dq, dr, ncls, x->dz, x->Hm1, res);
+      break;
+    case F3D_OUT_WIND:
+    case F3D_OUT_MAGGR:
+      k_out_field<<<blocks(pl), OB, 0, s>>>(var == F3D_OUT_MAGGR ? x->agr_maggr : (index == 1 ? x->vx : x->vy),
+                                            var == F3D_OUT_WIND, d, x->Hm1, x->zlayer, x->topg, asl, res);
       break;
     case F3D_OUT_CON:
       if (f32)

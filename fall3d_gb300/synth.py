@@ -382,6 +382,70 @@ def gravity_current(scen: Scenario, c_flow_rate=430.0, lambda_grav=0.2, k_entrai
                 beg_time=scen.beg_time)
 
 
+def add_gas_class(scen: Scenario, rate_fraction=0.05) -> Scenario:
+    """Appends one gas species (class np+1, the first gas, which the
+    aggregation model reads as magmatic water, agrsrc.f90:262-266) emitted
+    with the source at ``rate_fraction`` of each source point's particle
+    rate."""
+    g = scen.grid
+    nc, ns = g["nc"], int(np.sum(scen.src["nsou"]))
+    g["np"] = g.get("np", nc)
+    for k, v in (("diam", 1e-6), ("rhop", 1.0), ("sphe", 1.0), ("psi", 1.0)):
+        g[k] = np.append(np.asarray(g[k], float), v)
+    tm = np.asarray(scen.src["tmrat"], float)
+    rows = []  # per interval: (nsou_i, nc) column major
+    off = 0
+    for n in scen.src["nsou"]:
+        n = int(n)
+        blk = tm[off * nc:(off + n) * nc].reshape(nc, n) if n else np.zeros((nc, 0))
+        gas = np.array([float(f"{v:.9e}") for v in rate_fraction * blk.sum(axis=0)])
+        rows.append(np.vstack([blk, gas[None, :]]).reshape(-1))
+        off += n
+    scen.src["tmrat"] = np.concatenate(rows) if rows else tm
+    g["nc"] = nc + 1
+    scen.info["fc"] = np.append(np.asarray(scen.info["fc"], float), 0.0)
+    assert off == ns
+    return scen
+
+
+def aggregation_inputs(scen: Scenario, Df=2.8, ndtagr=2, rh_band=(2000.0, 5000.0)) -> dict:
+    """Inputs of the aggregation model for a scenario (AGGREGATION block of
+    readat.f90:350-440, the DBS variables QV and P, and the plume
+    temperature file read by settemplume, source.f90:89-149):
+
+    * fc: the .grn mass fractions; Df, ndtagr;
+    * qv, p (per met snapshot): ISA pressure at the levels' heights above sea
+      level and a specific humidity at 120% of saturation (over water, the
+      formula of agrsrc.f90:402) in the height band rh_band, 30% elsewhere;
+    * plume (per source interval): the source column's cells with
+      temperatures from 500 K at the vent down to 230 K at the top (vapour,
+      water and ice phases) and a water rate."""
+    g = scen.grid
+    nx, ny, nz = g["nx"], g["ny"], g["nz"]
+    zl = np.asarray(g["zlayer"])
+    zabs = zl[:, None, None] + np.asarray(g["topg"])[None]
+    T, P, _ = standard_atmosphere(zabs)
+    ew = 100.0 * 6.112 * np.exp(17.67 * (T - 273.16) / (T - 273.16 + 243.5))
+    ws = 0.622 * ew / np.maximum(P - ew, 1.0)
+    rh = np.where((zl[:, None, None] >= rh_band[0]) & (zl[:, None, None] <= rh_band[1]), 1.2, 0.3)
+    w = rh * ws
+    qv = _f32(w / (1.0 + w))
+    nt = len(scen.met["times"])
+    iv, jv = scen.info["vent"]
+    plume = []
+    for n in scen.src["nsou"]:
+        if int(n) == 0:
+            plume.append(dict(ix=np.zeros(0, np.int32), iy=np.zeros(0, np.int32), iz=np.zeros(0, np.int32),
+                              t=np.zeros(0), w=np.zeros(0)))
+            continue
+        ks = np.array([int(k) for k in scen.src["ksrc"][:int(n)]], np.int32)
+        frac = (ks - ks.min()) / max(1, ks.max() - ks.min())
+        plume.append(dict(ix=np.full(len(ks), iv, np.int32), iy=np.full(len(ks), jv, np.int32), iz=ks,
+                          t=_f32(500.0 - 270.0 * frac), w=_f32(1e3 * (1.0 - frac))))
+    return dict(Df=float(Df), ndtagr=int(ndtagr), fc=np.asarray(scen.info["fc"][:g["np"]], float),
+                qv=np.repeat(qv[None], nt, axis=0), p=np.repeat(_f32(P)[None], nt, axis=0), plume=plume)
+
+
 def ensemble_member(seed: int, run_h: float = 12.0, max_snapshots=None, met_dt_h: float = 1.0) -> Scenario:
     """One member of the batched ensemble: nx, ny ~ U[64,320], nz ~ U[20,60],
     spacing 0.02-0.05 deg, 4-20 classes over phi -2..6, column 3-20 km, MER

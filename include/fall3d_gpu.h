@@ -302,6 +302,8 @@ typedef struct f3d_met_series {
   const double *u, *v, *w, *t, *tp, *rho;          /* nt*nx*ny*nz          */
   const double *ust, *pblh, *rmol, *znt, *prate;   /* nt*nx*ny (PRATE mm/s) */
   const double* ldu;     /* nx*ny land use, time independent              */
+  const double *qv, *p;  /* nt*nx*ny*nz QV and P: read only by the
+                            aggregation model (may be NULL otherwise)     */
 } f3d_met_series;
 
 /* Source intervals as in the .src file (libMaster/get_source_*.f90): the
@@ -312,6 +314,13 @@ typedef struct f3d_src_series {
   const int *t1, *t2, *nsou;
   const int *isrc, *jsrc, *ksrc;
   const double* tmrat;
+  /* plume temperature file of the aggregation model (settemplume,
+   * source.f90:89-149): nplume(i) cells per interval, 1-based indices,
+   * temperature (K) and water rate (kg/s), concatenated over intervals;
+   * NULL nplume when aggregation is off */
+  const int* nplume;
+  const int *pix, *piy, *piz;
+  const double *ptemp, *pwater;
 } f3d_src_series;
 
 /* One line of the mass-budget log (Sources/writim.f90:18-52). */
@@ -389,7 +398,8 @@ int f3d_outputs(f3d_ctx* ctx, double* load, double* col_mass,
  * in binary64 in the reference's order of operations and written to dst
  * (host or device memory) as binary64 or, like the reference's NF90_FLOAT
  * netCDF variables (printres_nc.f90:805-841), as binary32.  2-D variables
- * are (nx,ny), x fastest; F3D_OUT_CON is (nx,ny,nz).  `index` selects:
+ * are (nx,ny), x fastest; F3D_OUT_CON, _WIND and _MAGGR are (nx,ny,nz).
+ * `index` selects:
  *   F3D_OUT_LOAD      deposit load kg/m2, cload(:,:,index)/Hm1 with
  *                     index 0 = all particles, 1..np one class (:105-146)
  *   F3D_OUT_WET       wet deposit kg/m2, cwet(:,:,index)/Hm1 (:148-189)
@@ -407,6 +417,10 @@ int f3d_outputs(f3d_ctx* ctx, double* load, double* col_mass,
  *                     moves it from terrain-following levels to heights
  *                     above sea level (Sources/ter2asl.f90:1-55, used when
  *                     terrain_following is false)
+ *   F3D_OUT_WIND      (nx,ny,nz) wind written with the gravity current,
+ *                     index 1 = vx*Hm1, 2 = vy*Hm1 (:603-644); asl as above
+ *   F3D_OUT_MAGGR     (nx,ny,nz) accumulated aggregate mass, kg
+ *                     (:673-690; aggregation on); asl as above
  * The deposit variables first form cload = cdry + cwet and the class sums
  * (endstep.f90:35,60). */
 #define F3D_OUT_LOAD      1
@@ -418,6 +432,8 @@ int f3d_outputs(f3d_ctx* ctx, double* load, double* col_mass,
 #define F3D_OUT_PM_GRND   7
 #define F3D_OUT_AOT05     8
 #define F3D_OUT_CON       9
+#define F3D_OUT_WIND     10
+#define F3D_OUT_MAGGR    11
 #define F3D_OUT_BINARY64  0
 #define F3D_OUT_BINARY32  1
 int f3d_output(f3d_ctx* ctx, int var, int index, int asl, void* dst,
@@ -445,6 +461,32 @@ typedef struct f3d_gravity_current {
   double beg_time;           /* the run's start (time of the eruption onset)  */
 } f3d_gravity_current;
 int f3d_set_gravity_current(f3d_ctx* ctx, const f3d_gravity_current* gc);
+
+/* Aggregation in transport (Costa et al. 2010; AGGREGATION_IN_TRANSPORT
+ * = yes, Sources/readat.f90:350-440), for a grid whose class np is the
+ * aggregate (grid.aggregate).  While it is on, the first f3d_step after
+ * an f3d_meteo or f3d_source runs agrpar (Sources/agrsrc.f90:95-319;
+ * Fall3d.f90:101-110) and every step adds the aggregation source of
+ * agrsrc (:1-91) every ndtagr steps after the point sources
+ * (setsrc.f90:37-76), accumulating Maggr.  The classes iaggr..np-1 that
+ * aggregate are those finer than the aggregate (readat.f90:400-409).
+ * QV and P of the snapshot (f3d_aggregation_met, before f3d_meteo) and
+ * the plume temperatures of the source interval (f3d_aggregation_plume,
+ * after f3d_source; the reference's settemplume) are inputs; f3d_run
+ * takes them from the series (qv/p of f3d_met_series, the plume lists of
+ * f3d_src_series).  NULL switches it off.  Not available in a batch. */
+typedef struct f3d_aggregation {
+  double Df;          /* FRACTAL_EXPONENT (readat.f90:411-421, default 3) */
+  int ndtagr;         /* N_DT_AGGREGATION (readat.f90:423-433, default 1) */
+  const double* fc;   /* fc(1:np): mass fractions of the grn file (host) */
+} f3d_aggregation;
+int f3d_set_aggregation(f3d_ctx* ctx, const f3d_aggregation* ag);
+int f3d_aggregation_met(f3d_ctx* ctx, const double* qv, const double* p);
+int f3d_aggregation_plume(f3d_ctx* ctx, int n, const int* ix, const int* iy,
+                          const int* iz, const double* temp,
+                          const double* water);
+/* Maggr(nx,ny,nz): accumulated mass of aggregates, kg (setsrc.f90:62-76) */
+int f3d_download_maggr(f3d_ctx* ctx, double* maggr);
 
 /* Sources/Fall3d.f90:73-121: the time loop from beg_time to end_time
  * (at most max_steps steps if max_steps > 0), reading meteorology and

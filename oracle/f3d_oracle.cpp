@@ -1222,6 +1222,10 @@ struct orc_ctx {
   // gravity current (readat.f90:150-213)
   int gc_on = 0;
   f3d_gravity_current gc{};
+  // aggregation in transport (readat.f90:350-440, agrsrc.f90)
+  int agg_on = 0, iaggr = 0, ndtagr = 1, agr_ipass = 0, agr_due = 0;
+  double Df = 3.0;
+  std::vector<double> fc, qv, pres, tplume, wplume, Alagr, Abagr, Asagr, Adagr, Maggr;
 };
 
 orc_ctx* orc_ctx_create(const f3d_grid* g, int nthreads) {
@@ -1348,6 +1352,245 @@ static void orc_divcorr(orc_ctx* x, double massvol, double massdep) {
       }
 }
 
+/* --------------------------------------------------------- aggregation */
+/* agrsrc.f90:393-440 (water_phase): 0 vapour, 1 water, 2 ice */
+static int orc_water_phase(double qv, double P, double T, double wcloud) {
+  double w = qv / (1.0 - qv);
+  w = w + wcloud;
+  const double e = P * w / (w + 0.622);
+  double ew = 6.112 * std::exp(17.67 * (T - 273.16) / (T - 273.16 + 243.5));
+  ew = 100.0 * ew;
+  double ei = -(9.09718 * (273.16 / T - 1.0)) - 3.56654 * std::log10(273.16 / T) +
+              0.876793 * (1.0 - T / 273.16) + std::log10(6.1071);
+  ei = 100.0 * std::pow(10.0, ei);
+  if (e > ew) return T > (double)255.f ? 1 : 2;
+  return e > ei ? 2 : 0;
+}
+
+/* agrsrc.f90:446-531 (get_gamas) on the scaled winds */
+static double orc_get_gamas(const orc_ctx* x, int i, int j, int k) {
+  Dims d{x->nx, x->ny, x->nz};
+  const int nx = x->nx, ny = x->ny, nz = x->nz;
+  const double* vx = x->vx.data();
+  const double* vy = x->vy.data();
+  const double* vz = x->vz.data();
+  const double dXX = x->Hm1[d.P(i, j)] * x->dX1;
+  double dudx, dvdx, dwdx, dudy, dvdy, dwdy, dudz, dvdz, dwdz;
+  auto V = [&](const double* f, int a, int b, int c) { return f[d.M(a, b, c)]; };
+  if (i == 1) {
+    dudx = (V(vx, 2, j, k) - V(vx, 1, j, k)) / dXX;
+    dvdx = (V(vy, 2, j, k) - V(vy, 1, j, k)) / dXX;
+    dwdx = (V(vz, 2, j, k) - V(vz, 1, j, k)) / dXX;
+  } else if (i == nx) {
+    dudx = (V(vx, nx, j, k) - V(vx, nx - 1, j, k)) / dXX;
+    dvdx = (V(vy, nx, j, k) - V(vy, nx - 1, j, k)) / dXX;
+    dwdx = (V(vz, nx, j, k) - V(vz, nx - 1, j, k)) / dXX;
+  } else {
+    dudx = (V(vx, i + 1, j, k) - V(vx, i - 1, j, k)) / (2.0 * dXX);
+    dvdx = (V(vy, i + 1, j, k) - V(vy, i - 1, j, k)) / (2.0 * dXX);
+    dwdx = (V(vz, i + 1, j, k) - V(vz, i - 1, j, k)) / (2.0 * dXX);
+  }
+  if (j == 1) {
+    dudy = (V(vx, i, 2, k) - V(vx, i, 1, k)) / x->dX2;
+    dvdy = (V(vy, i, 2, k) - V(vy, i, 1, k)) / x->dX2;
+    dwdy = (V(vz, i, 2, k) - V(vz, i, 1, k)) / x->dX2;
+  } else if (j == ny) {
+    dudy = (V(vx, i, ny, k) - V(vx, i, ny - 1, k)) / x->dX2;
+    dvdy = (V(vy, i, ny, k) - V(vy, i, ny - 1, k)) / x->dX2;
+    dwdy = (V(vz, i, ny, k) - V(vz, i, ny - 1, k)) / x->dX2;
+  } else {
+    dudy = (V(vx, i, j + 1, k) - V(vx, i, j - 1, k)) / (2.0 * x->dX2);
+    dvdy = (V(vy, i, j + 1, k) - V(vy, i, j - 1, k)) / (2.0 * x->dX2);
+    dwdy = (V(vz, i, j + 1, k) - V(vz, i, j - 1, k)) / (2.0 * x->dX2);
+  }
+  const double* dz = x->dz.data();
+  if (k == 1) {
+    dudz = (V(vx, i, j, 2) - V(vx, i, j, 1)) / dz[1];
+    dvdz = (V(vy, i, j, 2) - V(vy, i, j, 1)) / dz[1];
+    dwdz = (V(vz, i, j, 2) - V(vz, i, j, 1)) / dz[1];
+  } else if (k == nz) {
+    dudz = (V(vx, i, j, nz) - V(vx, i, j, nz - 1)) / dz[nz - 1];
+    dvdz = (V(vy, i, j, nz) - V(vy, i, j, nz - 1)) / dz[nz - 1];
+    dwdz = (V(vz, i, j, nz) - V(vz, i, j, nz - 1)) / dz[nz - 1];
+  } else {
+    dudz = (V(vx, i, j, k + 1) - V(vx, i, j, k - 1)) / (dz[k - 1] + dz[k]);
+    dvdz = (V(vy, i, j, k + 1) - V(vy, i, j, k - 1)) / (dz[k - 1] + dz[k]);
+    dwdz = (V(vz, i, j, k + 1) - V(vz, i, j, k - 1)) / (dz[k - 1] + dz[k]);
+  }
+  const double half = (double)0.5f;
+  const double S11 = dudx, S12 = half * (dvdx + dudy), S13 = half * (dwdx + dudz);
+  const double S21 = S12, S22 = dvdy, S23 = half * (dwdy + dvdz);
+  const double S31 = S13, S32 = S23, S33 = dwdz;
+  const double epsilon = S11 * S11 + S12 * S12 + S13 * S13 + S21 * S21 + S22 * S22 + S23 * S23 +
+                         S31 * S31 + S32 * S32 + S33 * S33;
+  return std::sqrt((double)(1.3f * 2.0f) * epsilon);
+}
+
+/* agrsrc.f90:95-319 (agrpar), called after a source or meteo update */
+static void orc_agrpar(orc_ctx* x) {
+  const int nx = x->nx, ny = x->ny, nz = x->nz, np = x->np, ng = x->nc - x->np;
+  Dims d{nx, ny, nz};
+  const size_t s3 = d.cells();
+  const double pi = 3.14159265358979323846;
+  const double g = 9.81, kb = 1.38e-23, visc0 = 1.827e-5, Tair0 = (double)291.15f;
+  const double Stcr = 1.3, qq = 0.8;
+  const double psi3 = 6.0 / pi;
+  const double psi4 = psi3 * std::pow(6.0 / pi, 1.0 / 3.0);
+  const double* fc = x->fc.data();  /* fc(1:np) at fc[0..np-1] */
+  double sumfc = 0.0;
+  for (int ic = x->iaggr; ic <= np - 1; ++ic) sumfc = sumfc + fc[ic - 1];
+  double sumff = 0.0;
+  for (int ic = x->iaggr; ic <= np - 1; ++ic)
+    for (int jc = x->iaggr; jc <= np - 1; ++jc) sumff = sumff + fc[ic - 1] * fc[jc - 1];
+  double rhopmean = 0.0;
+  for (int ic = x->iaggr; ic <= np - 1; ++ic) rhopmean = rhopmean + fc[ic - 1] * x->rhop[ic - 1];
+  rhopmean = rhopmean / sumfc;
+  for (int iz = 1; iz <= nz; ++iz)
+    for (int iy = 1; iy <= ny; ++iy)
+      for (int ix = 1; ix <= nx; ++ix) {
+        const size_t m = d.M(ix, iy, iz);
+        const double tp = x->tplume[m];
+        const double T = tp > 0.0 ? tp : x->tempe[m];
+        const double rhoa = x->rho[m];
+        const double visc = visc0 * ((Tair0 + 120.0) / (T + 120.0)) * std::pow(T / Tair0, 1.5);
+        const double viscl = 2.414e-5 * std::pow(10.0, 247.7 / (T - 140.0));
+        int phase;  /* 0 vapour (or the plume's truncated 'vapou'), 1 water, 2 ice */
+        if (tp > 0.0) {
+          phase = T < 255 ? 2 : (T < 373 ? 1 : 0);
+        } else {
+          double wcloud = ng > 0 ? x->c[(size_t)np * d.halo() + d.C(ix, iy, iz)] / x->Hm1[d.P(ix, iy)]
+                                 : (double)0.f;
+          wcloud = wcloud / rhoa;
+          phase = orc_water_phase(x->qv[m], x->pres[m], T, wcloud);
+        }
+        x->Abagr[m] = -(4.0 * kb * T / (3.0 * visc));
+        const double gamas = orc_get_gamas(x, ix, iy, iz);
+        x->Asagr[m] = -(2.0 * gamas * psi3 / 3.0);
+        x->Adagr[m] = -(pi * (rhopmean - rhoa) * g * psi4 / (48.0 * visc));
+        double al = 0.0;
+        if (phase == 2) {
+          al = 0.09;
+        } else if (phase == 1) {
+          for (int ic = x->iaggr; ic <= np - 1; ++ic)
+            for (int jc = x->iaggr; jc <= np - 1; ++jc) {
+              const double di = x->diam[ic - 1], dj = x->diam[jc - 1];
+              const double vij = std::fabs(x->vset[(size_t)(ic - 1) * s3 + m] - x->vset[(size_t)(jc - 1) * s3 + m]) -
+                                 x->Abagr[m] / (2.0 * pi * di * dj) - x->Asagr[m] * di * dj / (4.0 * pi);
+              const double w = fc[ic - 1] * fc[jc - 1] / sumff;
+              const double Stij = 8.0 * rhopmean * vij * di * dj / (9.0 * viscl * (di + dj));
+              double alfa = 1.0 + std::pow(Stij / Stcr, qq);
+              alfa = 1.0 / alfa;
+              al = al + w * alfa;
+            }
+        }
+        x->Alagr[m] = al;
+      }
+  /* agrsrc.f90:295-301: the settling velocity of class iaggr */
+  for (size_t m = 0; m < s3; ++m)
+    x->vset[(size_t)(x->iaggr - 1) * s3 + m] = x->vset_factor * x->vset[(size_t)(x->iaggr - 1) * s3 + m];
+}
+
+/* agrsrc.f90:1-91 (agrsrc) and setsrc.f90:37-76: the aggregation source of
+ * one aggregation step added to c, and Maggr */
+static void orc_agrsrc(orc_ctx* x) {
+  const int nx = x->nx, ny = x->ny, nz = x->nz, np = x->np, iaggr = x->iaggr;
+  Dims d{nx, ny, nz};
+  const double pi = 3.14159265358979323846;
+  const double ka = 1.0, expb = 2.0, exps = 2.0 - (3.0 / x->Df), expd = 2.0 - (4.0 / x->Df);
+  std::vector<double> Ni(np + 1, 0.0), d3(np + 1, 0.0), tarat(np + 1, 0.0);
+  double sumNi = 0.0;
+  for (int ic = iaggr; ic <= np - 1; ++ic) {
+    const double di = x->diam[ic - 1];
+    d3[ic] = pi * x->rhop[ic - 1] * di * di * di;
+    Ni[ic] = ka * std::pow(x->diam[np - 1] / di, x->Df);
+    sumNi = sumNi + Ni[ic];
+  }
+  const double fac = (double)x->ndtagr * x->dt;
+  for (int iz = 1; iz <= nz; ++iz) {
+    const double dzeta = 0.5 * (x->dz[iz - 1] + x->dz[iz]);
+    for (int iy = 1; iy <= ny; ++iy)
+      for (int ix = 1; ix <= nx; ++ix) {
+        const size_t q = d.C(ix, iy, iz), m = d.M(ix, iy, iz);
+        const double h = x->Hm1[d.P(ix, iy)];
+        double ntot = 0.0, fi = 0.0;
+        for (int ic = iaggr; ic <= np - 1; ++ic) {
+          const double c = x->c[(size_t)(ic - 1) * d.halo() + q];
+          fi = fi + c / x->rhop[ic - 1];
+          ntot = ntot + 6.0 * c / d3[ic];
+        }
+        ntot = ntot / h;
+        fi = fi / h;
+        double dntot = x->Abagr[m] * std::pow(ntot, expb) +
+                       x->Asagr[m] * std::pow(ntot, exps) * std::pow(fi, 3.0 / x->Df) +
+                       x->Adagr[m] * std::pow(ntot, expd) * std::pow(fi, 4.0 / x->Df);
+        dntot = x->Alagr[m] * dntot;
+        tarat[np] = 0.0;
+        for (int ic = iaggr; ic <= np - 1; ++ic) {
+          const double c = x->c[(size_t)(ic - 1) * d.halo() + q];
+          const double dnj = dntot * Ni[ic] / sumNi;
+          tarat[ic] = dnj * d3[ic] / 6.0;
+          if (c + x->dt * tarat[ic] < 0.0) tarat[ic] = -c / x->dt;
+          tarat[np] = tarat[np] - tarat[ic];
+        }
+        for (int ic = iaggr; ic <= np; ++ic) {
+          double& c = x->c[(size_t)(ic - 1) * d.halo() + q];
+          c = c + fac * tarat[ic];
+        }
+        x->Maggr[m] = x->Maggr[m] + fac * tarat[np] * h * x->dX1 * x->dX2 * dzeta;
+      }
+  }
+}
+
+/* the aggregation model switched on: Df, ndtagr and the .grn fractions
+ * fc(1:np); iaggr as readat.f90:400-409 */
+int orc_set_aggregation(orc_ctx* x, double Df, int ndtagr, const double* fc) {
+  if (!fc) {
+    x->agg_on = 0;
+    return 0;
+  }
+  const int np = x->np;
+  if (np < 2 || ndtagr < 1) return 1;
+  int iaggr = 0;
+  for (int ic = np - 1; ic >= 1; --ic)
+    if (x->diam[np - 1] > x->diam[ic - 1]) iaggr = ic;
+  if (iaggr == 0) iaggr = np - 1;
+  x->iaggr = iaggr;
+  x->Df = Df;
+  x->ndtagr = ndtagr;
+  x->fc.assign(fc, fc + np);
+  const size_t s3 = (size_t)x->nx * x->ny * x->nz;
+  for (auto* v : {&x->qv, &x->pres, &x->tplume, &x->wplume, &x->Alagr, &x->Abagr, &x->Asagr, &x->Adagr,
+                  &x->Maggr})
+    v->assign(s3, 0.0);
+  x->agg_on = 1;
+  x->agr_ipass = 0;
+  return 0;
+}
+
+/* QV and P (nx,ny,nz) of the DBS snapshot of the next meteo update */
+void orc_aggregation_met(orc_ctx* x, const double* qv, const double* p) {
+  const size_t s3 = (size_t)x->nx * x->ny * x->nz;
+  std::copy(qv, qv + s3, x->qv.begin());
+  std::copy(p, p + s3, x->pres.begin());
+}
+
+/* settemplume (source.f90:89-149): plume temperature and water rate of
+ * the current source interval at n cells (1-based indices) */
+void orc_aggregation_plume(orc_ctx* x, int n, const int* ix, const int* iy, const int* iz,
+                           const double* t, const double* w) {
+  Dims d{x->nx, x->ny, x->nz};
+  std::fill(x->tplume.begin(), x->tplume.end(), 0.0);
+  std::fill(x->wplume.begin(), x->wplume.end(), 0.0);
+  for (int q = 0; q < n; ++q) {
+    x->tplume[d.M(ix[q], iy[q], iz[q])] = t[q];
+    x->wplume[d.M(ix[q], iy[q], iz[q])] = w[q];
+  }
+}
+
+void orc_download_maggr(orc_ctx* x, double* maggr) {
+  if (x->agg_on) std::copy(x->Maggr.begin(), x->Maggr.end(), maggr);
+}
+
 void orc_set_gravity_current(orc_ctx* x, const f3d_gravity_current* gc) {
   if (gc) {
     x->gc = *gc;
@@ -1399,6 +1642,7 @@ int orc_meteo(orc_ctx* x, const double* u, const double* v, const double* w,
              x->vz.data(), x->vset.data(), x->rkh1.data(), x->rkhor.data(), x->rkver.data(),
              x->safety, &x->dt, &x->dtc);
   x->have_met = 1;
+  if (x->agg_on) x->agr_due = 1;  /* Fall3d.f90:94-96 */
   return 0;
 }
 
@@ -1423,6 +1667,7 @@ int orc_source(orc_ctx* x, int nsou, const int* isrc, const int* jsrc,
     const double h = x->Hm1[(size_t)(isrc[is] - 1) + (size_t)x->nx * (jsrc[is] - 1)];
     for (int ic = 0; ic < nc; ++ic) x->tmrat[(size_t)is + (size_t)nsou * ic] *= h;
   }
+  if (x->agg_on) x->agr_due = 1;  /* Fall3d.f90:84-86 */
   return 0;
 }
 
@@ -1470,6 +1715,10 @@ static void orc_sizloop(orc_ctx* x) {
 /* Sources/Fall3d.f90:112-117 */
 int orc_step(orc_ctx* x) {
   if (!x->have_met) return 4;
+  if (x->agg_on && x->agr_due) {  /* Fall3d.f90:101-110, after the updates */
+    orc_agrpar(x);
+    x->agr_due = 0;
+  }
   x->time = x->time + x->dt;
   x->iiter = x->iiter + 1;
   x->erumass = x->erumass + x->flowrate * x->dt;
@@ -1477,6 +1726,10 @@ int orc_step(orc_ctx* x) {
                       x->ksrc.data(), x->tmrat.data(), x->dz.data(), x->zlayer.data(), x->Hm1.data(),
                       x->dX1, x->dX2, x->dt);
   if (rc) return rc;
+  if (x->agg_on) {  /* setsrc.f90:37-76 */
+    x->agr_ipass = x->agr_ipass + 1;
+    if (x->agr_ipass % x->ndtagr == 0) orc_agrsrc(x);
+  }
   orc_sizloop(x);
   return 0;
 }
@@ -1573,6 +1826,12 @@ int orc_run(orc_ctx* x, const f3d_met_series* met, const f3d_src_series* src,
         const int rc = orc_source(x, src->nsou[found], src->isrc + off_found, src->jsrc + off_found,
                                   src->ksrc + off_found, src->tmrat + roff);
         if (rc) return rc;
+        if (x->agg_on && src->nplume) {  /* settemplume at the end of source (source.f90:82) */
+          size_t po = 0;
+          for (int it = 0; it < found; ++it) po += (size_t)src->nplume[it];
+          orc_aggregation_plume(x, src->nplume[found], src->pix + po, src->piy + po, src->piz + po,
+                                src->ptemp + po, src->pwater + po);
+        }
         x->source_time = (double)src->t2[found];
       }
       if (x->source_time >= end_time) x->sourcetime = 0;
@@ -1587,6 +1846,7 @@ int orc_run(orc_ctx* x, const f3d_met_series* met, const f3d_src_series* src,
         for (int it = 0; it < nt - 1; ++it)
           if (ts >= met->times[it] && ts < met->times[it + 1]) { itime = it; endsec = met->times[it + 1]; }
         const size_t o3 = (size_t)itime * s3, o2 = (size_t)itime * pl;
+        if (x->agg_on && met->qv && met->p) orc_aggregation_met(x, met->qv + o3, met->p + o3);
         const int rc = orc_meteo(x, met->u + o3, met->v + o3, met->w + o3, met->t + o3, met->tp + o3,
                                  met->rho + o3, met->ust + o2, met->pblh + o2, met->rmol + o2,
                                  met->znt + o2, met->prate ? met->prate + o2 : nullptr, met->ldu);

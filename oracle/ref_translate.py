@@ -48,16 +48,17 @@ UNIT_FILES = ["setbcc.f90", "advctzc.f90", "advctx.f90", "advcty.f90", "diffz.f9
               "diffy.f90", "wetdep.f90", "accum.f90", "cmass2d.f90", "cmass3d.f90", "finddt.f90",
               "kappa3.f90", "setvset.f90", "setpsi.f90", "setvdrydep.f90", "corvver.f90",
               "setdivu.f90", "setsrc.f90", "sizloop.f90", "meteo.f90", "source.f90", "endstep.f90",
-              "setcut.f90", "ter2asl.f90", "addradialwind.f90", "divcorr.f90"]
+              "setcut.f90", "ter2asl.f90", "addradialwind.f90", "divcorr.f90",
+              "agrsrc.f90"]
 # units from those files that are translated (others in the files are skipped)
 WANTED = {"setbcc", "advctzc", "advctx", "advcty", "diffz", "diffx", "diffy", "wetdep", "accum",
           "cmass2d", "cmass3d", "finddt", "kappa3", "setvset", "vsettl", "setpsi", "get_gama",
           "setvdrydep", "corvver", "setdivu", "setsrc", "sizloop", "meteo", "source", "getc0",
           "getmem1", "getmem2", "outmem2", "setcut_fl", "standard_atm", "ter2asl",
-          "addradialwind", "divcorr"}
+          "addradialwind", "divcorr", "agrsrc", "agrpar", "water_phase", "get_gamas"}
 NOOP_CALLS = {"bcast", "parallel_sum", "exchange_1layer", "exchange_2layer", "collect_cz",
               "collect_c", "collect_cload", "addtime", "wriwar", "flush", "reamet", "reasrc",
-              "settemplume", "agrsrc", "cpu_time"}
+              "settemplume", "cpu_time"}
 SKIP_STMTS = ("write", "format", "print", "open", "close", "read", "rewind", "inquire")
 
 # module scalars supplied by the serial runtime (Sources/Parallel.F90 and
@@ -778,7 +779,10 @@ class Gen:
     def reduce_ext(self, arr, is_max):
         """MAXVAL / MINVAL (whole array or section) of a real array: the
         largest (smallest) element, NaN elements skipped; -HUGE (+HUGE) for
-        an empty one, as gfortran returns."""
+        an empty one, as gfortran returns.  MAXVAL(-a) is -MINVAL(a)."""
+        if arr[0] == "neg":
+            inner, ty = self.reduce_ext(arr[1], not is_max)
+            return f"(-{inner})", ty
         lo_hi = self.section_extents(arr)
         acc = self.newtmp()
         ty = self.elem_type(arr)

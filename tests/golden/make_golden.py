@@ -47,9 +47,14 @@ CASES = [
     ("tiny_dellino_ganser_two_updates", "tiny", 5, dict(modv=4, run_h=1.5, met_dt_h=0.5), None),
     ("cfg0_first_60_steps", "cfg0", 0, {}, 60),
     ("small_gravity_current", "small", 6, dict(M0=1e7, u10=4.0, vy0=1.0, run_h=0.75), None),
+    ("small_aggregation", "small", 9, dict(nc=7, phimin=3.0, phimax=8.0, aggregate=[0.2, 1000.0, 0.2],
+                                           M0=1e7, run_h=0.75), None),
 ]
 # cases run with GRAVITY_CURRENT = YES (parameters of synth.gravity_current)
 GRAVITY = {"small_gravity_current"}
+# cases run with aggregation in transport: a gas class appended
+# (synth.add_gas_class) and the inputs of synth.aggregation_inputs
+AGGREGATION = {"small_aggregation"}
 # large cases keep every SAMPLE-th value of the 3-D/4-D fields
 SAMPLE = {"cfg0_first_60_steps": 37}
 
@@ -97,16 +102,27 @@ class RefLib:
         f(*args)
 
 
-def run_reference(scen, max_steps=None, gc=None):
+def iaggr_of(diam, np_):
+    """Index of the first aggregating class (readat.f90:400-409): the lowest
+    class finer than the aggregate class np, else np-1."""
+    iaggr = 0
+    for ic in range(np_ - 1, 0, -1):
+        if diam[np_ - 1] > diam[ic - 1]:
+            iaggr = ic
+    return iaggr if iaggr else np_ - 1
+
+
+def run_reference(scen, max_steps=None, gc=None, agg=None):
     """The Fall3d.f90 loop on the translated reference; returns a dict.
-    gc: GRAVITY_CURRENT parameters (synth.gravity_current) or None."""
+    gc: GRAVITY_CURRENT parameters (synth.gravity_current) or None;
+    agg: aggregation inputs (synth.aggregation_inputs) or None."""
     R = RefLib()
     g, m, sr = scen.grid, scen.met, scen.src
     nx, ny, nz, nc = g["nx"], g["ny"], g["nz"], g["nc"]
-    for k, v in (("nx", nx), ("ny", ny), ("nz", nz), ("nc", nc), ("np", g["np"]), ("ng", 0),
+    for k, v in (("nx", nx), ("ny", ny), ("nz", nz), ("nc", nc), ("np", g["np"]), ("ng", nc - g["np"]),
                  ("modkv", g["modkv"]), ("modkh", g["modkh"]), ("modv", g["modv"]), ("lmeth", 1),
                  ("nz_loc", nz), ("nc_loc", nc), ("iz_loc", 1), ("ic_loc", 1), ("iiter", 0),
-                 ("wetdeposition", g["wetdep"]), ("aggregation", 0), ("gravity_current", 0),
+                 ("wetdeposition", g["wetdep"]), ("aggregation", 1 if agg else 0), ("gravity_current", 0),
                  ("meteotime", 1), ("sourcetime", 1)):
         R.i(k).value = int(v)
     for k, v in (("dx1", g["dX1"]), ("dx2", g["dX2"]), ("dx", g["dx"]), ("dy", g["dy"]),
@@ -131,6 +147,13 @@ def run_reference(scen, max_steps=None, gc=None):
         C.memmove(names[ic], b" " * 25 + b"\0", 26)
     for k in ("diam", "rhop", "psi", "sphe"):
         R.fixed(k, 50)[:nc] = g[k]
+    if g.get("aggregate"):  # classname(np) == 'aggregate' (setvset.f90:48)
+        C.memmove(names[g["np"] - 1], b"aggregate".ljust(25) + b"\0", 26)
+    if agg:  # readat_aggr (readat.f90:350-440)
+        R.i("iaggr").value = iaggr_of(list(g["diam"]), g["np"])
+        R.d("df").value = agg["Df"]
+        R.i("ndtagr").value = agg["ndtagr"]
+        R.fixed("fc", 50)[:g["np"]] = agg["fc"]
     R.call("getmem1")
     pl, s3 = nx * ny, nx * ny * nz
     R.arr("hm1", pl)[:] = np.asarray(g["Hm1"]).ravel()
@@ -150,6 +173,9 @@ def run_reference(scen, max_steps=None, gc=None):
             pr[:] = m["prate"][it].ravel()
             pr[:] = pr * 3600.0  # reamet.f90:146
         R.arr("vz", s3)[:pl] = 0.0  # reamet.f90:153
+        if agg:  # the DBS variables QV and P
+            R.arr("qv", s3)[:] = agg["qv"][it].ravel()
+            R.arr("p", s3)[:] = agg["p"][it].ravel()
         R.call("meteo")
 
     state = {"src_alloc": False}
@@ -170,6 +196,15 @@ def run_reference(scen, max_steps=None, gc=None):
             if gc:  # the source points' heights (get_source_coordinates)
                 R.arr("zs", n)[:] = np.full(n, gc["h_tot"]) if iint else scen.info["zs"][:n]
         R.call("source")
+        if agg:  # settemplume (source.f90:89-149) from the plume file
+            tp, wp = R.arr("tplume", s3), R.arr("wplume", s3)
+            tp[:] = 0.0
+            wp[:] = 0.0
+            pl_ = agg["plume"][iint]
+            for q in range(len(pl_["ix"])):
+                cell = (pl_["ix"][q] - 1) + nx * (pl_["iy"][q] - 1) + nx * ny * (pl_["iz"][q] - 1)
+                tp[cell] = pl_["t"][q]
+                wp[cell] = pl_["w"][q]
 
     beg, end = scen.beg_time, scen.end_time
     R.d("time").value = beg
@@ -182,11 +217,13 @@ def run_reference(scen, max_steps=None, gc=None):
     hb = (nx + 2) * (ny + 2) * (nz + 2)
     while True:
         time = R.d("time").value
+        aggregationtime = False
         if source_time <= time:
             if sourcetime:
                 ts = int(time)
                 it = next(i for i in range(len(sr["t1"])) if sr["t1"][i] <= ts < sr["t2"][i])
                 source(it)
+                aggregationtime = bool(agg)
                 source_time = float(sr["t2"][it])
             if source_time >= end:
                 sourcetime = False
@@ -199,6 +236,7 @@ def run_reference(scen, max_steps=None, gc=None):
                     if times[i] <= ts < times[i + 1]:
                         itime, endsec = i, times[i + 1]
                 meteo(itime)
+                aggregationtime = bool(agg)
                 meteo_time = float(endsec) - m["time_lag"]
                 if coeffs is None:
                     coeffs = {k: R.arr(k, s3).copy() for k in ("vx", "vy", "vz", "rho", "rkhor", "rkh1",
@@ -208,6 +246,8 @@ def run_reference(scen, max_steps=None, gc=None):
                     coeffs["dt"] = R.d("dt").value
             if meteo_time >= end:
                 meteotime = False
+        if aggregationtime:  # Fall3d.f90:101-110
+            R.call("agrpar")
         dt = R.d("dt").value
         R.d("time").value = R.d("time").value + dt  # Fall3d.f90:112-114
         R.i("iiter").value = R.i("iiter").value + 1
@@ -246,6 +286,8 @@ def run_reference(scen, max_steps=None, gc=None):
            "iiter": R.i("iiter").value, "time": R.d("time").value, "dt": R.d("dt").value,
            "erumass": R.d("erumass").value, "outmass": R.d("outmass").value,
            "flowrate": R.d("flowrate").value}
+    if agg:
+        res["maggr"] = R.arr("maggr", s3).copy().reshape(nz, ny, nx)
     for k, v in log.items():
         res["log_" + k] = np.array(v)
     for k, v in coeffs.items():
@@ -317,7 +359,11 @@ def main():
             continue
         s = scenario(workload, seed, over)
         gc = synth.gravity_current(s) if name in GRAVITY else None
-        r = run_reference(s, max_steps, gc)
+        agg = None
+        if name in AGGREGATION:
+            synth.add_gas_class(s)
+            agg = synth.aggregation_inputs(s)
+        r = run_reference(s, max_steps, gc, agg)
         path = os.path.join(HERE, f"{name}.npz")
         st = SAMPLE.get(name)
         if st:
@@ -330,6 +376,8 @@ def main():
                       "steps": int(r["iiter"])}
         if gc:
             meta[name]["gravity_current"] = gc
+        if agg:
+            meta[name]["aggregation"] = True
         print(f"{name}: {r['iiter']} steps, {os.path.getsize(path) / 1024:.0f} KB")
     with open(os.path.join(HERE, "cases.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)

@@ -82,11 +82,15 @@ def load():
         "orc_outputs_ctx": [VP, DP, DP, DP],
         "orc_run_reset": [VP],
         "orc_set_gravity_current": [VP, VP],
+        "orc_set_aggregation": [VP, D, I, DP],
+        "orc_aggregation_met": [VP, DP, DP],
+        "orc_aggregation_plume": [VP, I, IP, IP, IP, DP, DP],
+        "orc_download_maggr": [VP, DP],
         "orc_run": [VP, VP, VP, D, D, I, VP, I, IP],
     }
     ret = {"orc_get_gama": I, "orc_vsettl": I, "orc_setvset": I, "orc_setsrc": I,
            "orc_ctx_create": VP, "orc_meteo": I, "orc_source": I, "orc_step": I, "orc_run": I,
-           "orc_pm_classes": I, "orc_standard_pressure": D}
+           "orc_pm_classes": I, "orc_standard_pressure": D, "orc_set_aggregation": I}
     for name, args in sig.items():
         f = getattr(lib, name)
         f.argtypes = args
@@ -249,9 +253,24 @@ class OracleCtx:
     def upload_state(self, c=None, cdry=None, cwet=None, erumass=0.0, outmass=0.0, cd=1.0):
         self.lib.orc_upload_state(self.h, p(c), p(cdry), p(cwet), erumass, outmass, cd)
 
+    def set_aggregation(self, agg=None):
+        """Aggregation in transport with synth.aggregation_inputs (None: off)."""
+        self._agg = agg
+        if agg is None:
+            self.lib.orc_set_aggregation(self.h, 3.0, 1, None)
+            return
+        self._fc = np.ascontiguousarray(agg["fc"], dtype=np.float64)
+        assert self.lib.orc_set_aggregation(self.h, float(agg["Df"]), int(agg["ndtagr"]), p(self._fc)) == 0
+
+    def maggr(self):
+        m = np.zeros((self.nz, self.ny, self.nx))
+        self.lib.orc_download_maggr(self.h, p(m))
+        return m
+
     def run(self, beg_time=None, end_time=None, max_steps=0, log_cap=4096):
-        met = _abi.make_met(self.s.met)
-        src = _abi.make_src(self.s.src)
+        agg = getattr(self, "_agg", None)
+        met = _abi.make_met(self.s.met, agg)
+        src = _abi.make_src(self.s.src, agg)
         recs = (_abi.F3DLogRecord * log_cap)()
         n = C.c_int()
         rc = self.lib.orc_run(self.h, C.cast(met.ref(), VP), C.cast(src.ref(), VP),

@@ -20,6 +20,8 @@ CASES = json.load(open(os.path.join(HERE, "cases.json")))
 
 def _scenario(meta):
     s = synth.make_scenario(meta["workload"], seed=meta["seed"], **meta["overrides"])
+    if meta.get("aggregation"):
+        synth.add_gas_class(s)
     if s.grid["wetdep"]:
         band = np.linspace(0.0, 4.0, s.grid["nx"])[None, :] / 3600.0
         s.met["prate"][:] = np.asarray(band, np.float32).astype(np.float64)
@@ -35,6 +37,8 @@ def test_oracle_matches_reference_golden(name):
     o = O.OracleCtx(s, nthreads=4)
     if "gravity_current" in meta:
         o.set_gravity_current(meta["gravity_current"])
+    if meta.get("aggregation"):
+        o.set_aggregation(synth.aggregation_inputs(s))
     log = o.run(max_steps=meta["max_steps"] or 0)
     st = o.state()
     assert st["iiter"] == int(g["iiter"]) == meta["steps"]
@@ -42,6 +46,8 @@ def test_oracle_matches_reference_golden(name):
     assert_same_bits(f["c"].ravel()[::stride], g["c"].ravel(), "c")
     assert_same_bits(f["cdry"].ravel(), g["cdry"].ravel(), "cdry")
     assert_same_bits(f["cwet"].ravel(), g["cwet"].ravel(), "cwet")
+    if "maggr" in g:
+        assert_same_bits(o.maggr(), g["maggr"], "maggr")
     for k in ("time", "dt", "erumass", "outmass", "flowrate"):
         assert_same_bits(np.array([st[k]]), np.array([float(g[k])]), k)
     for k in ("iiter", "time", "dt", "dtc", "massvol", "massdep", "massdry", "masswet", "outmass",

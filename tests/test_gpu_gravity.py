@@ -106,3 +106,25 @@ def test_gravity_current_rejected_in_batch():
         b.add(g)
     b.close()
     g.set_gravity_current(None)
+
+
+def test_wind_output_with_gravity_current():
+    """The gravity-current wind variables of printres_nc.f90:603-644:
+    vx*Hm1 and vy*Hm1 on the levels, and moved to heights above sea level
+    by ter2asl (the oracle's ter2asl, pinned to the reference's)."""
+    s = _scen()
+    g = F.Context(s, F.PREC_FP64)
+    g.set_gravity_current(synth.gravity_current(s))
+    g.source(0)
+    g.meteo(0)
+    co = g.coeffs()
+    hm = np.asarray(s.grid["Hm1"])
+    lib = O.load()
+    nz, ny, nx = co["vx"].shape
+    for index, key in ((1, "vx"), (2, "vy")):
+        want = co[key] * hm[None]
+        assert_same_bits(g.output(F.OUT_WIND, index), want, key)
+        asl = np.ascontiguousarray(want.copy())
+        lib.orc_ter2asl(O.p(asl), O.p(np.ascontiguousarray(s.grid["topg"], dtype=np.float64)),
+                        O.p(np.ascontiguousarray(s.grid["zlayer"], dtype=np.float64)), nx, ny, nz)
+        assert_same_bits(g.output(F.OUT_WIND, index, asl=True), asl, key + " asl")
