@@ -103,6 +103,7 @@ def load(build_if_missing: bool = False):
         "f3d_output_fl": [VP, D, VP, VP, I],
         "f3d_set_gravity_current": [VP, VP],
         "f3d_set_aggregation": [VP, VP],
+        "f3d_track_points": [VP, I, VP, VP, D, D, VP],
         "f3d_aggregation_met": [VP, VP, VP],
         "f3d_aggregation_plume": [VP, I, VP, VP, VP, VP, VP],
         "f3d_download_maggr": [VP, VP],
@@ -480,6 +481,16 @@ class Context:
         _check(self.lib.f3d_output(self.h, int(var), int(index), int(bool(asl)), a.ctypes.data,
                                    1 if binary32 else 0))
         return a
+
+    def track_points(self, xpts, ypts, xo, yo):
+        """Tracking-point values (f3d_track_points) at points (x, y) of the
+        grid's coordinates with origin (xo, yo): (npts, 7 + 3*nz + 1 + np)."""
+        xp = np.ascontiguousarray(xpts, dtype=np.float64)
+        yp = np.ascontiguousarray(ypts, dtype=np.float64)
+        out = np.zeros((len(xp), 7 + 3 * self.nz + 1 + self.s.grid.get("np", self.nc)))
+        _check(self.lib.f3d_track_points(self.h, len(xp), xp.ctypes.data, yp.ctypes.data, float(xo), float(yo),
+                                         out.ctypes.data))
+        return out
 
     def output_fl(self, flight_level, p, binary32=False):
         """Particle concentration at a flight level (hundreds of feet), with

@@ -206,6 +206,98 @@ __global__ void k_out_field(const double* f, int times_hm1, Dims d, const double
   }
 }
 
+// Tracking points (Sources/writps.f90, writps_air.f90): one thread per
+// point, bilinear weights of the cell (ip, jp) at (s, t) in (-1,1)^2.
+// out per point: [0..6] load, thickness, ground concentration, PM05, PM10,
+// PM20, column mass (writps.f90:64-148); then nz concentrations, nz
+// extinctions, nz number concentrations and the AOD (writps_air.f90:
+// 64-109); then np class loads (writps.f90:215-222, writps_end).
+struct TrackClass {
+  double diam, rhop;
+  int aer;         // an aerosol class of get_AOT_prop's range
+  double q, r;     // Qeff(ieff), reff(ieff)
+};
+template <class T>
+__global__ void k_track(const T* c, const double* cload, Dims d, int np, const int* ip, const int* jp,
+                        const double* sp, const double* tp, int npts, const TrackClass* cls,
+                        const double* dz, const double* Hm1, double* out) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= npts) return;
+  const int nz = d.nz;
+  const long long pl = d.plane(), hb = d.halo();
+  const int stride = 7 + 3 * nz + 1 + np;
+  double* o = out + (long long)n * stride;
+  const int i = ip[n], j = jp[n];
+  const double s = sp[n], t = tp[n], st = s * t;
+  const double v1 = (1.0 - t - s + st) * 0.25, v2 = (1.0 - t + s - st) * 0.25;
+  const double v3 = (1.0 + t + s + st) * 0.25, v4 = (1.0 + t - s - st) * 0.25;
+  const long long p1 = d.P(i, j), p2 = d.P(i + 1, j), p3 = d.P(i + 1, j + 1), p4 = d.P(i, j + 1);
+  const double h1 = Hm1[p1], h2 = Hm1[p2], h3 = Hm1[p3], h4 = Hm1[p4];
+  auto pl4 = [&](const double* f) {  // v1*(f1/h1) + ... of a 2-D field
+    return v1 * (f[p1] / h1) + v2 * (f[p2] / h2) + v3 * (f[p3] / h3) + v4 * (f[p4] / h4);
+  };
+  auto c4 = [&](int ic, int k) {  // the same of c(:,:,k,ic)
+    const T* cc = c + (long long)(ic - 1) * hb;
+    return v1 * ((double)cc[d.C(i, j, k)] / h1) + v2 * ((double)cc[d.C(i + 1, j, k)] / h2) +
+           v3 * ((double)cc[d.C(i + 1, j + 1, k)] / h3) + v4 * ((double)cc[d.C(i, j + 1, k)] / h4);
+  };
+  o[0] = pl4(cload);
+  double thick = 0.0;
+  for (int ic = 1; ic <= np; ++ic) {
+    const double* f = cload + (long long)ic * pl;
+    const double rp = cls[ic - 1].rhop;
+    thick = thick + v1 * (f[p1] / h1 / rp) + v2 * (f[p2] / h2 / rp) + v3 * (f[p3] / h3 / rp) + v4 * (f[p4] / h4 / rp);
+  }
+  o[1] = 1e2 * thick;
+  auto acc4 = [&](double a, int ic, int k) {  // a + v1*(c1/h1) + ... term by term
+    const T* cc = c + (long long)(ic - 1) * hb;
+    return a + v1 * ((double)cc[d.C(i, j, k)] / h1) + v2 * ((double)cc[d.C(i + 1, j, k)] / h2) +
+           v3 * ((double)cc[d.C(i + 1, j + 1, k)] / h3) + v4 * ((double)cc[d.C(i, j + 1, k)] / h4);
+  };
+  double cg = 0.0, pm5 = 0.0, pm10 = 0.0, pm20 = 0.0;
+  for (int ic = 1; ic <= np; ++ic) cg = acc4(cg, ic, 1);
+  for (int ic = 1; ic <= np; ++ic)
+    if (cls[ic - 1].diam <= 5e-6) pm5 = acc4(pm5, ic, 1);
+  for (int ic = 1; ic <= np; ++ic)
+    if (cls[ic - 1].diam <= 1e-5) pm10 = acc4(pm10, ic, 1);
+  for (int ic = 1; ic <= np; ++ic)
+    if (cls[ic - 1].diam <= 2e-5) pm20 = acc4(pm20, ic, 1);
+  o[2] = cg * 1e3;
+  o[3] = pm5 * 1e3;
+  o[4] = pm10 * 1e3;
+  o[5] = pm20 * 1e3;
+  double cummc = 0.0;
+  for (int ic = 1; ic <= np; ++ic)
+    for (int k = 1; k <= nz - 1; ++k) {
+      const double cp1 = c4(ic, k), cp2 = c4(ic, k + 1);
+      cummc = cummc + dz[k] * 0.5 * (cp1 + cp2);
+    }
+  o[6] = 1e3 * cummc;
+  double* cz = o + 7;
+  double* ext = cz + nz;
+  double* nco = ext + nz;
+  double aod = 0.0;
+  const double pi = 3.14159265358979323846;
+  for (int k = 1; k <= nz; ++k) {
+    double a = 0.0, e = 0.0, q = 0.0;
+    for (int ic = 1; ic <= np; ++ic) {
+      const double cc = c4(ic, k);
+      a = a + cc;
+      const TrackClass& k1 = cls[ic - 1];
+      if (k1.aer) {
+        e = e + (cc * 0.75 * k1.q) / (k1.rhop * k1.r);
+        aod = aod + (dz[k] * cc * 0.75 * k1.q) / (k1.rhop * k1.r);
+      }
+      if (0.5 * k1.diam <= 32e-6) q = q + (6.0 * cc) / (k1.rhop * pi * k1.diam * k1.diam * k1.diam);
+    }
+    cz[k - 1] = a * 1e3;
+    ext[k - 1] = e * 1e6;
+    nco[k - 1] = q * 1e-6;
+  }
+  o[7 + 3 * nz] = aod;
+  for (int ic = 1; ic <= np; ++ic) o[8 + 3 * nz + ic - 1] = pl4(cload + (long long)ic * pl);
+}
+
 __global__ void k_out_to_f32(const double* a, long long n, float* b) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x)
@@ -430,6 +522,91 @@ int f3d_output(f3d_ctx* x, int var, int index, int asl, void* dst, int dst_type)
   }
   count_launch();
   return finish(x, res, n, dst, dst_type, sc);
+}
+
+int f3d_track_points(f3d_ctx* x, int npts, const double* xpts, const double* ypts, double xo, double yo,
+                     double* out) {
+  if (!x || (npts > 0 && (!xpts || !ypts || !out))) return f3d::ctx_error(F3D_ERR_ARG, "NULL argument");
+  if (npts <= 0) return F3D_OK;
+  const Dims d = x->d;
+  const int np = x->g.np, nz = d.nz;
+  // get_pts_st (Sources/reaout.f90:180-224): the cell and (s,t) of each point
+  std::vector<int> ip(npts), jp(npts);
+  std::vector<double> sp(npts), tp(npts);
+  const double dxo = x->g.dx, dyo = x->g.dy;
+  for (int n = 0; n < npts; ++n) {
+    bool found = false;
+    for (int ix = 1; ix <= d.nx - 1; ++ix) {
+      const double xx = xo + (ix - 1) * dxo;
+      if (xpts[n] >= xx && xpts[n] <= xx + dxo) {
+        ip[n] = ix;
+        sp[n] = (xpts[n] - xx) / dxo;
+        sp[n] = 2.0 * sp[n] - 1.0;
+        found = true;
+      }
+    }
+    if (!found) return f3d::ctx_error(F3D_ERR_RANGE, "get_pts_st: value not found");
+    found = false;
+    for (int iy = 1; iy <= d.ny - 1; ++iy) {
+      const double yy = yo + (iy - 1) * dyo;
+      if (ypts[n] >= yy && ypts[n] <= yy + dyo) {
+        jp[n] = iy;
+        tp[n] = (ypts[n] - yy) / dyo;
+        tp[n] = 2.0 * tp[n] - 1.0;
+        found = true;
+      }
+    }
+    if (!found) return f3d::ctx_error(F3D_ERR_RANGE, "get_pts_st: value not found");
+  }
+  std::vector<TrackClass> cls(np > 0 ? np : 1);
+  double reff[20];
+  for (int b = 0; b < 20; ++b) reff[b] = kReffUm[b] * 1e-6;
+  for (int ic = 0; ic < np; ++ic) {
+    TrackClass& k = cls[ic];
+    k.diam = x->h_diam[ic];
+    k.rhop = x->h_rhop[ic];
+    k.aer = 0;
+    k.q = k.r = 0.0;
+    const double rad = (double)0.5f * k.diam;
+    if (rad >= reff[0] && rad <= reff[19]) {
+      int ieff = 0;
+      for (int b = 0; b < 19; ++b)
+        if (rad >= reff[b] && rad <= reff[b + 1]) ieff = b + 1;
+      k.aer = 1;
+      k.q = kQeff[ieff];
+      k.r = reff[ieff];
+    }
+  }
+  const int stride = 7 + 3 * nz + 1 + np;
+  cudaStream_t s = x->stream;
+  Scratch sc;
+  sc.s = s;
+  const size_t bo = sizeof(double) * (size_t)npts * stride;
+  const size_t bi = (sizeof(int) * 2 + sizeof(double) * 2) * (size_t)npts;
+  OK(cudaMallocAsync(&sc.p, bo + bi + sizeof(TrackClass) * cls.size() + 256, s));
+  unsigned char* b = reinterpret_cast<unsigned char*>(sc.p);
+  double* res = reinterpret_cast<double*>(b);
+  double* dsp = reinterpret_cast<double*>(b + bo);
+  double* dtp = dsp + npts;
+  int* dip = reinterpret_cast<int*>(dtp + npts);
+  int* djp = dip + npts;
+  TrackClass* dcls = reinterpret_cast<TrackClass*>(b + ((bo + bi + 15) & ~size_t(15)));
+  OK(cudaMemcpyAsync(dsp, sp.data(), sizeof(double) * npts, cudaMemcpyHostToDevice, s));
+  OK(cudaMemcpyAsync(dtp, tp.data(), sizeof(double) * npts, cudaMemcpyHostToDevice, s));
+  OK(cudaMemcpyAsync(dip, ip.data(), sizeof(int) * npts, cudaMemcpyHostToDevice, s));
+  OK(cudaMemcpyAsync(djp, jp.data(), sizeof(int) * npts, cudaMemcpyHostToDevice, s));
+  OK(cudaMemcpyAsync(dcls, cls.data(), sizeof(TrackClass) * cls.size(), cudaMemcpyHostToDevice, s));
+  launch_getc0(x->cdry, x->cwet, x->cload, d, x->g.nc, np, s);
+  const unsigned nb = (unsigned)((npts + 63) / 64);
+  if (x->prec == F3D_PREC_FP32)
+    k_track<float><<<nb, 64, 0, s>>>(x->c32, x->cload, d, np, dip, djp, dsp, dtp, npts, dcls, x->dz, x->Hm1, res);
+  else
+    k_track<double><<<nb, 64, 0, s>>>(x->c64, x->cload, d, np, dip, djp, dsp, dtp, npts, dcls, x->dz, x->Hm1, res);
+  count_launch();
+  OK(cudaMemcpyAsync(out, res, bo, cudaMemcpyDefault, s));
+  OK(cudaGetLastError());
+  OK(cudaStreamSynchronize(s));
+  return F3D_OK;
 }
 
 int f3d_output_fl(f3d_ctx* x, double flight_level, const double* p, void* dst, int dst_type) {

@@ -438,6 +438,17 @@ int f3d_outputs(f3d_ctx* ctx, double* load, double* col_mass,
 #define F3D_OUT_BINARY32  1
 int f3d_output(f3d_ctx* ctx, int var, int index, int asl, void* dst,
                int dst_type);
+/* Tracking points (Sources/writps.f90, writps_air.f90, the point location
+ * of Sources/reaout.f90:180-224): for each of npts points (x, y in the
+ * grid's coordinates, origin xo, yo), bilinear in the cell that holds it,
+ * out receives 7 + 3*nz + 1 + np binary64 values per point: deposit load
+ * (kg/m2), thickness (cm), ground concentration, PM05, PM10, PM20 (g/m3),
+ * column mass (g/m2); nz concentrations (g/m3), nz aerosol extinctions
+ * (1/Mm), nz number concentrations (1/cm3) and the AOD; np class loads
+ * (the final deposit of writps_end).  Forms cload = cdry + cwet first. */
+int f3d_track_points(f3d_ctx* ctx, int npts, const double* xpts,
+                     const double* ypts, double xo, double yo, double* out);
+
 /* Particle concentration g/m3 at a flight level (hundreds of feet) of the
  * ICAO standard atmosphere (printres_nc.f90:542-573, Sources/setcut.f90):
  * interpolated in the pressure p(nx,ny,nz) of the model levels (Pa, the

@@ -1183,6 +1183,113 @@ void orc_out_con(const double* c, int nx, int ny, int nz, int np, int ic, const 
   if (asl) orc_ter2asl(out, topg, zlayer, nx, ny, nz);
 }
 
+/* Tracking points: Sources/reaout.f90:180-224 (get_pts_st), writps.f90:
+ * 64-148, writps_air.f90:64-109, writps.f90:205-222 (writps_end); cload
+ * is (nx,ny,0:nc) after getc0.  out per point: 7 + 3*nz + 1 + np values. */
+int orc_track_points(const double* c, const double* cload, int nx, int ny, int nz, int np,
+                     const double* diam, const double* rhop, const double* dz, const double* Hm1,
+                     double dxo, double dyo, double xo, double yo, int npts, const double* xpts,
+                     const double* ypts, double* out) {
+  Dims d{nx, ny, nz};
+  const size_t pl = d.plane();
+  double reff[20], qeff[20];
+  orc_aot_prop(reff, qeff);
+  const double pi = 3.14159265358979323846;
+  const int stride = 7 + 3 * nz + 1 + np;
+  for (int n = 0; n < npts; ++n) {
+    int ip = 0, jp = 0;
+    double sp = 0.0, tp = 0.0;
+    bool found = false;
+    for (int ix = 1; ix <= nx - 1; ++ix) {
+      const double x = xo + (ix - 1) * dxo;
+      if (xpts[n] >= x && xpts[n] <= x + dxo) {
+        ip = ix;
+        sp = (xpts[n] - x) / dxo;
+        sp = 2.0 * sp - 1.0;
+        found = true;
+      }
+    }
+    if (!found) return 6;
+    found = false;
+    for (int iy = 1; iy <= ny - 1; ++iy) {
+      const double y = yo + (iy - 1) * dyo;
+      if (ypts[n] >= y && ypts[n] <= y + dyo) {
+        jp = iy;
+        tp = (ypts[n] - y) / dyo;
+        tp = 2.0 * tp - 1.0;
+        found = true;
+      }
+    }
+    if (!found) return 6;
+    const double s = sp, t = tp, st = s * t;
+    const double v1 = (1.0 - t - s + st) * 0.25, v2 = (1.0 - t + s - st) * 0.25;
+    const double v3 = (1.0 + t + s + st) * 0.25, v4 = (1.0 + t - s - st) * 0.25;
+    const size_t p1 = d.P(ip, jp), p2 = d.P(ip + 1, jp), p3 = d.P(ip + 1, jp + 1), p4 = d.P(ip, jp + 1);
+    const double h1 = Hm1[p1], h2 = Hm1[p2], h3 = Hm1[p3], h4 = Hm1[p4];
+    auto C = [&](int ic, int i, int j, int k) { return c[(size_t)(ic - 1) * d.halo() + d.C(i, j, k)]; };
+    double* o = out + (size_t)n * stride;
+    o[0] = v1 * (cload[p1] / h1) + v2 * (cload[p2] / h2) + v3 * (cload[p3] / h3) + v4 * (cload[p4] / h4);
+    double thick = 0.0;
+    for (int ic = 1; ic <= np; ++ic) {
+      const double* f = cload + (size_t)ic * pl;
+      thick = thick + v1 * (f[p1] / h1 / rhop[ic - 1]) + v2 * (f[p2] / h2 / rhop[ic - 1]) +
+              v3 * (f[p3] / h3 / rhop[ic - 1]) + v4 * (f[p4] / h4 / rhop[ic - 1]);
+    }
+    o[1] = 1e2 * thick;
+    auto acc = [&](double a, int ic, int k) {
+      return a + v1 * (C(ic, ip, jp, k) / h1) + v2 * (C(ic, ip + 1, jp, k) / h2) +
+             v3 * (C(ic, ip + 1, jp + 1, k) / h3) + v4 * (C(ic, ip, jp + 1, k) / h4);
+    };
+    double cg = 0.0, pm5 = 0.0, pm10 = 0.0, pm20 = 0.0;
+    for (int ic = 1; ic <= np; ++ic) cg = acc(cg, ic, 1);
+    for (int ic = 1; ic <= np; ++ic)
+      if (diam[ic - 1] <= 5e-6) pm5 = acc(pm5, ic, 1);
+    for (int ic = 1; ic <= np; ++ic)
+      if (diam[ic - 1] <= 1e-5) pm10 = acc(pm10, ic, 1);
+    for (int ic = 1; ic <= np; ++ic)
+      if (diam[ic - 1] <= 2e-5) pm20 = acc(pm20, ic, 1);
+    o[2] = cg * 1e3;
+    o[3] = pm5 * 1e3;
+    o[4] = pm10 * 1e3;
+    o[5] = pm20 * 1e3;
+    double cummc = 0.0;
+    for (int ic = 1; ic <= np; ++ic)
+      for (int iz = 1; iz <= nz - 1; ++iz) {
+        const double cp1 = acc(0.0, ic, iz), cp2 = acc(0.0, ic, iz + 1);
+        cummc = cummc + dz[iz] * 0.5 * (cp1 + cp2);
+      }
+    o[6] = 1e3 * cummc;
+    double aod = 0.0;
+    for (int iz = 1; iz <= nz; ++iz) {
+      double cz = 0.0, ext = 0.0, nco = 0.0;
+      for (int ic = 1; ic <= np; ++ic) {
+        const double cc = v1 * (C(ic, ip, jp, iz) / h1) + v2 * (C(ic, ip + 1, jp, iz) / h2) +
+                          v3 * (C(ic, ip + 1, jp + 1, iz) / h3) + v4 * (C(ic, ip, jp + 1, iz) / h4);
+        cz = cz + cc;
+        const double rad = (double)0.5f * diam[ic - 1];
+        if (rad >= reff[0] && rad <= reff[19]) {
+          int ieff = 0;
+          for (int jeff = 1; jeff <= 19; ++jeff)
+            if (rad >= reff[jeff - 1] && rad <= reff[jeff]) ieff = jeff + 1;
+          ext = ext + (cc * 0.75 * qeff[ieff - 1]) / (rhop[ic - 1] * reff[ieff - 1]);
+          aod = aod + (dz[iz] * cc * 0.75 * qeff[ieff - 1]) / (rhop[ic - 1] * reff[ieff - 1]);
+        }
+        if (rad <= 32e-6)
+          nco = nco + (6.0 * cc) / (rhop[ic - 1] * pi * diam[ic - 1] * diam[ic - 1] * diam[ic - 1]);
+      }
+      o[7 + iz - 1] = cz * 1e3;
+      o[7 + nz + iz - 1] = ext * 1e6;
+      o[7 + 2 * nz + iz - 1] = nco * 1e-6;
+    }
+    o[7 + 3 * nz] = aod;
+    for (int ic = 1; ic <= np; ++ic) {
+      const double* f = cload + (size_t)ic * pl;
+      o[8 + 3 * nz + ic - 1] = v1 * (f[p1] / h1) + v2 * (f[p2] / h2) + v3 * (f[p3] / h3) + v4 * (f[p4] / h4);
+    }
+  }
+  return 0;
+}
+
 /* LOAD, COL_MASS and C_GRND of the context's state (:105-123, :216-247,
  * :389-411) */
 void orc_outputs(const double* c, const double* cload, int nx, int ny, int nz,

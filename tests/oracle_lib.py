@@ -86,11 +86,12 @@ def load():
         "orc_aggregation_met": [VP, DP, DP],
         "orc_aggregation_plume": [VP, I, IP, IP, IP, DP, DP],
         "orc_download_maggr": [VP, DP],
+        "orc_track_points": [DP, DP, I, I, I, I, DP, DP, DP, DP, D, D, D, D, I, DP, DP, DP],
         "orc_run": [VP, VP, VP, D, D, I, VP, I, IP],
     }
     ret = {"orc_get_gama": I, "orc_vsettl": I, "orc_setvset": I, "orc_setsrc": I,
            "orc_ctx_create": VP, "orc_meteo": I, "orc_source": I, "orc_step": I, "orc_run": I,
-           "orc_pm_classes": I, "orc_standard_pressure": D, "orc_set_aggregation": I}
+           "orc_pm_classes": I, "orc_standard_pressure": D, "orc_set_aggregation": I, "orc_track_points": I}
     for name, args in sig.items():
         f = getattr(lib, name)
         f.argtypes = args
@@ -158,6 +159,29 @@ def output(grid, fields, var, index=0, asl=False, p_levels=None, flight_level=No
         lib.orc_out_fl(p(c), nx, ny, nz, np_, p(pl), float(flight_level), p(hm), p(out2))
         return out2
     raise ValueError(var)
+
+
+def track_points(grid, fields, xpts, ypts, xo, yo):
+    """The oracle's tracking-point values (orc_track_points) of a state as
+    f3d_download returns it: (npts, 7 + 3*nz + 1 + np)."""
+    lib = load()
+    nx, ny, nz, nc, np_ = grid["nx"], grid["ny"], grid["nz"], grid["nc"], grid["np"]
+    cdry = np.array(fields["cdry"], dtype=np.float64)
+    cwet = np.array(fields["cwet"], dtype=np.float64)
+    cload = np.zeros_like(cdry)
+    lib.orc_getc0(p(cdry), p(cwet), p(cload), nx, ny, nc, np_)
+    xp = np.ascontiguousarray(xpts, dtype=np.float64)
+    yp = np.ascontiguousarray(ypts, dtype=np.float64)
+    out = np.zeros((len(xp), 7 + 3 * nz + 1 + np_))
+    rc = lib.orc_track_points(p(np.ascontiguousarray(fields["c"], dtype=np.float64)), p(cload), nx, ny, nz, np_,
+                              p(np.ascontiguousarray(grid["diam"], dtype=np.float64)),
+                              p(np.ascontiguousarray(grid["rhop"], dtype=np.float64)),
+                              p(np.ascontiguousarray(grid["dz"], dtype=np.float64)),
+                              p(np.ascontiguousarray(grid["Hm1"], dtype=np.float64)),
+                              float(grid["dx"]), float(grid["dy"]), float(xo), float(yo), len(xp), p(xp), p(yp),
+                              p(out))
+    assert rc == 0, rc
+    return out
 
 
 class OracleCtx:

@@ -83,3 +83,22 @@ def test_output_rejects_bad_selectors(run):
     for var, index in ((F.OUT_LOAD, 6), (F.OUT_COL_MASS, 2), (F.OUT_PM_COL, 7), (F.OUT_CON, 7), (99, 0)):
         with pytest.raises(F.F3DError):
             g.output(var, index)
+
+
+def test_track_points_match_oracle(run):
+    """Tracking points (writps, writps_air, writps_end) at points inside
+    the grid, on a node and in the last cell: bitwise equal to the
+    oracle's restatement on the same state."""
+    s, g, f = run
+    gr = s.grid
+    xo, yo = s.info["origin"]
+    nx, ny = gr["nx"], gr["ny"]
+    xs = np.array([xo + 0.37 * gr["dx"] * (nx - 1), xo + 3 * gr["dx"], xo + (nx - 1.5) * gr["dx"]])
+    ys = np.array([yo + 0.61 * gr["dy"] * (ny - 1), yo + 5 * gr["dy"], yo + 0.5 * gr["dy"]])
+    got = g.track_points(xs, ys, xo, yo)
+    want = O.track_points(gr, f, xs, ys, xo, yo)
+    assert got.shape == want.shape
+    assert np.array_equal(got, want), np.max(np.abs(got - want))
+    assert np.max(got[:, 0]) > 0.0
+    with pytest.raises(F.F3DError):
+        g.track_points(np.array([xo - 1.0]), np.array([yo]), xo, yo)
