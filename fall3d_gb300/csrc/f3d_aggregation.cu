@@ -183,6 +183,12 @@ __global__ void k_agrsrc(T* c, Dims d, AgrSrc a, const double* cls, const double
   }
 }
 
+// settemplume: the plume temperature at the listed cells, 0 elsewhere
+__global__ void k_plume_scatter(Dims d, int n, const int* ijk, const double* t, double* tplume) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) tplume[d.M(ijk[3 * q], ijk[3 * q + 1], ijk[3 * q + 2])] = t[q];
+}
+
 unsigned grid_of(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16); }
 
 }  // namespace
@@ -235,26 +241,14 @@ int agg_setsrc(f3d_ctx* x) {
   const f3d_grid& g = x->g;
   const Dims d = x->d;
   const int np = g.np, iaggr = x->agr_iaggr;
-  // Ni and d3 of the aggregating classes (agrsrc.f90:27-32)
-  std::vector<double> cls(2 * (size_t)(np + 1), 0.0);
-  double sumNi = 0.0;
-  for (int ic = iaggr; ic <= np - 1; ++ic) {
-    const double di = x->h_diam[ic - 1];
-    cls[2 * ic + 1] = kPi * x->h_rhop[ic - 1] * di * di * di;
-    cls[2 * ic] = 1.0 * std::pow(x->h_diam[np - 1] / di, x->agr_Df);
-    sumNi = sumNi + cls[2 * ic];
-  }
   cudaStream_t s = x->stream;
-  if (cudaMemcpyAsync(x->agr_cls, cls.data(), sizeof(double) * cls.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    return ctx_error(F3D_ERR_CUDA, "aggregation class table upload failed");
   AgrSrc a;
   a.iaggr = iaggr;
   a.np = np;
   a.Df = x->agr_Df;
   a.exps = 2.0 - (3.0 / x->agr_Df);
   a.expd = 2.0 - (4.0 / x->agr_Df);
-  a.sumNi = sumNi;
+  a.sumNi = x->agr_sumNi;
   a.dt = x->dt;
   a.fac = (double)x->agr_ndtagr * x->dt;
   a.dX1 = g.dX1;
@@ -302,7 +296,19 @@ int f3d_set_aggregation(f3d_ctx* x, const f3d_aggregation* ag) {
       return rc;
   }
   x->agr_fc.assign(ag->fc, ag->fc + np);
+  // Ni and d3 of the aggregating classes (agrsrc.f90:27-32), constant
+  std::vector<double> cls(2 * (size_t)(np + 1), 0.0);
+  double sumNi = 0.0;
+  for (int ic = iaggr; ic <= np - 1; ++ic) {
+    const double di = x->h_diam[ic - 1];
+    cls[2 * ic + 1] = kPi * x->h_rhop[ic - 1] * di * di * di;
+    cls[2 * ic] = 1.0 * std::pow(x->h_diam[np - 1] / di, ag->Df);
+    sumNi = sumNi + cls[2 * ic];
+  }
+  x->agr_sumNi = sumNi;
   if (cudaMemcpyAsync(x->agr_fc_dev, x->agr_fc.data(), sizeof(double) * np, cudaMemcpyHostToDevice, x->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(x->agr_cls, cls.data(), sizeof(double) * cls.size(), cudaMemcpyHostToDevice, x->stream) !=
           cudaSuccess ||
       cudaStreamSynchronize(x->stream) != cudaSuccess)
     return ctx_error(F3D_ERR_CUDA, "aggregation upload failed");
@@ -332,15 +338,32 @@ int f3d_aggregation_plume(f3d_ctx* x, int n, const int* ix, const int* iy, const
   if (n < 0 || (n > 0 && (!ix || !iy || !iz || !temp))) return ctx_error(F3D_ERR_ARG, "invalid plume list");
   (void)water;  // wplume is read by no computation of the reference
   const Dims d = x->d;
-  std::vector<double> t((size_t)d.cells(), 0.0);
+  std::vector<int> ijk(3 * (size_t)n);
+  std::vector<double> t(temp, temp + n);
   for (int q = 0; q < n; ++q) {
     if (ix[q] < 1 || ix[q] > d.nx || iy[q] < 1 || iy[q] > d.ny || iz[q] < 1 || iz[q] > d.nz)
       return ctx_error(F3D_ERR_RANGE, "plume cell outside the grid");
-    t[d.M(ix[q], iy[q], iz[q])] = temp[q];
+    ijk[3 * q] = ix[q];
+    ijk[3 * q + 1] = iy[q];
+    ijk[3 * q + 2] = iz[q];
   }
-  if (cudaMemcpyAsync(x->agr_tplume, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, x->stream) !=
-          cudaSuccess ||
-      cudaStreamSynchronize(x->stream) != cudaSuccess)
+  cudaStream_t s = x->stream;
+  void* buf = nullptr;
+  bool ok = cudaMemsetAsync(x->agr_tplume, 0, sizeof(double) * (size_t)d.cells(), s) == cudaSuccess;
+  if (ok && n > 0) {
+    ok = cudaMallocAsync(&buf, (sizeof(int) * 3 + sizeof(double)) * (size_t)n + 8, s) == cudaSuccess;
+    int* dijk = reinterpret_cast<int*>(buf);
+    double* dt = reinterpret_cast<double*>(dijk + 3 * (size_t)n + ((3 * n) & 1));
+    ok = ok && cudaMemcpyAsync(dijk, ijk.data(), sizeof(int) * ijk.size(), cudaMemcpyHostToDevice, s) == cudaSuccess;
+    ok = ok && cudaMemcpyAsync(dt, t.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    if (ok) {
+      k_plume_scatter<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(d, n, dijk, dt, x->agr_tplume);
+      count_launch();
+    }
+    if (buf) cudaFreeAsync(buf, s);
+  }
+  // the host lists go out of scope
+  if (!ok || cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
     return ctx_error(F3D_ERR_CUDA, "plume upload failed");
   return F3D_OK;
 }

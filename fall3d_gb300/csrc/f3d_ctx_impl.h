@@ -27,7 +27,7 @@ struct f3d_ctx {
   double mfr_scaled = 0.0;  // sum of the Hm1-scaled source rates (addradialwind.f90:61)
   // aggregation in transport (f3d_set_aggregation)
   int agr_on = 0, agr_iaggr = 0, agr_ndtagr = 1, agr_ipass = 0, agr_due = 0;
-  double agr_Df = 3.0;
+  double agr_Df = 3.0, agr_sumNi = 0.0;
   std::vector<double> agr_fc;  // fc(1:np)
   double *agr_fc_dev = nullptr, *agr_cls = nullptr;
   double *agr_al = nullptr, *agr_ab = nullptr, *agr_as = nullptr, *agr_ad = nullptr;  // Alagr..Adagr
