@@ -189,6 +189,16 @@ __global__ void k_plume_scatter(Dims d, int n, const int* ijk, const double* t, 
   if (q < n) tplume[d.M(ijk[3 * q], ijk[3 * q + 1], ijk[3 * q + 2])] = t[q];
 }
 
+// vset(:,:,:,iaggr) = vset_factor*vset(:,:,:,iaggr) (agrsrc.f90:295-301)
+__global__ void k_vset_scale(double* v, long long n, double f, int times) {
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
+       m += (long long)gridDim.x * blockDim.x) {
+    double x = v[m];
+    for (int q = 0; q < times; ++q) x = f * x;
+    v[m] = x;
+  }
+}
+
 unsigned grid_of(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16); }
 
 }  // namespace
@@ -230,8 +240,23 @@ int agg_agrpar(f3d_ctx* x) {
                                                         x->diam, x->agr_fc_dev, x->vset, x->agr_al, x->agr_ab,
                                                         x->agr_as, x->agr_ad);
   count_launch();
+  x->agr_npar = x->agr_npar + 1;
   if (x->prec == F3D_PREC_FP32) refresh_fp32_class(x, iaggr - 1);
   return cudaGetLastError() == cudaSuccess ? F3D_OK : ctx_error(F3D_ERR_CUDA, "agrpar launch failed");
+}
+
+// A restored run: the coefficients of its last agrpar come from the
+// checkpoint (they depend on the state at that time); the replayed meteo
+// update only needs class iaggr's settling velocity scaled once per agrpar
+// the saved run made since its meteo update.
+int agg_restore_vset(f3d_ctx* x, int times) {
+  const long long s3 = x->d.cells();
+  k_vset_scale<<<grid_of(s3), 256, 0, x->stream>>>(x->vset + (long long)(x->agr_iaggr - 1) * s3, s3,
+                                                   x->g.vset_factor, times);
+  count_launch();
+  x->agr_npar = times;
+  if (x->prec == F3D_PREC_FP32) refresh_fp32_class(x, x->agr_iaggr - 1);
+  return cudaGetLastError() == cudaSuccess ? F3D_OK : ctx_error(F3D_ERR_CUDA, "vset scaling launch failed");
 }
 
 // setsrc.f90:37-76 after the point sources of this step

@@ -628,7 +628,10 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
     CK(cudaGetLastError());
   }
   x->have_met = 1;
-  if (x->agr_on) x->agr_due = 1;  // Fall3d.f90:94-96
+  if (x->agr_on) {  // Fall3d.f90:94-96
+    x->agr_due = 1;
+    x->agr_npar = 0;
+  }
   return F3D_OK;
 }
 
@@ -700,8 +703,10 @@ int f3d_step(f3d_ctx* x) {
   if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
   if (!x->have_met) return f3d::ctx_error(F3D_ERR_STATE, "f3d_step before f3d_meteo");
   if (x->agr_on && x->agr_due) {  // Fall3d.f90:101-110: agrpar after this step's updates
-    if (int rc = f3d::agg_agrpar(x)) return rc;
+    const int rc = x->agr_replay > 0 ? f3d::agg_restore_vset(x, x->agr_replay) : f3d::agg_agrpar(x);
+    if (rc) return rc;
     x->agr_due = 0;
+    x->agr_replay = 0;
   }
   f3d::ctx_advance(x);
   const Dims d = x->d;
@@ -859,6 +864,7 @@ struct CkptHeader {
   double time, erumass, outmass, cd_prev;
 };
 const char kCkptMagic[8] = {'F', '3', 'D', 'C', 'K', 'P', 'T', '1'};
+const long long kCkptAggr = 0x5247474146334446LL;  // the optional aggregation section
 }  // namespace
 
 int f3d_ctx_save(f3d_ctx* x, const char* path) {
@@ -878,8 +884,15 @@ int f3d_ctx_save(f3d_ctx* x, const char* path) {
   h.time = x->time;
   h.erumass = x->erumass;
   std::vector<unsigned char> c(hb * esz);
-  std::vector<double> cdry(pl2), cwet(pl2);
+  // aggregation: Maggr and the coefficients of the last agrpar
+  const size_t s3 = (size_t)d.cells();
+  std::vector<double> cdry(pl2), cwet(pl2), agf(x->agr_on ? 5 * s3 : 0);
   cudaStream_t s = x->stream;
+  if (x->agr_on) {
+    const double* src[5] = {x->agr_maggr, x->agr_al, x->agr_ab, x->agr_as, x->agr_ad};
+    for (int q = 0; q < 5; ++q)
+      CK(cudaMemcpyAsync(agf.data() + q * s3, src[q], s3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
   CK(cudaMemcpyAsync(&h.outmass, small_outmass(x), sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&h.cd_prev, small_cd_prev(x), sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(c.data(), x->prec == F3D_PREC_FP32 ? (const void*)x->c32 : (const void*)x->c64, hb * esz,
@@ -891,6 +904,11 @@ int f3d_ctx_save(f3d_ctx* x, const char* path) {
   if (!f) return f3d::ctx_error(F3D_ERR_ARG, "cannot open the checkpoint file for writing");
   bool ok = fwrite(&h, sizeof h, 1, f) == 1 && fwrite(c.data(), 1, c.size(), f) == c.size() &&
             fwrite(cdry.data(), sizeof(double), pl2, f) == pl2 && fwrite(cwet.data(), sizeof(double), pl2, f) == pl2;
+  if (ok && x->agr_on) {  // aggregation: the agrsrc step counter, agrpar calls since the meteo update,
+                          // Maggr and Alagr, Abagr, Asagr, Adagr
+    const long long agg[3] = {kCkptAggr, x->agr_ipass, x->agr_npar};
+    ok = fwrite(agg, sizeof agg, 1, f) == 1 && fwrite(agf.data(), sizeof(double), agf.size(), f) == agf.size();
+  }
   ok = (fclose(f) == 0) && ok;
   if (!ok) return f3d::ctx_error(F3D_ERR_ARG, "checkpoint write failed");
   return F3D_OK;
@@ -917,8 +935,15 @@ int f3d_ctx_restore(f3d_ctx* x, const char* path) {
   std::vector<double> cdry(pl2), cwet(pl2);
   ok = fread(c.data(), 1, c.size(), f) == c.size() && fread(cdry.data(), sizeof(double), pl2, f) == pl2 &&
        fread(cwet.data(), sizeof(double), pl2, f) == pl2;
+  long long agg[3] = {0, 0, 0};
+  const bool has_agg = ok && fread(agg, sizeof agg, 1, f) == 1 && agg[0] == kCkptAggr;
+  const size_t s3 = (size_t)d.cells();
+  std::vector<double> agf(has_agg ? 5 * s3 : 0);
+  if (has_agg) ok = fread(agf.data(), sizeof(double), agf.size(), f) == agf.size();
   fclose(f);
   if (!ok) return f3d::ctx_error(F3D_ERR_ARG, "truncated checkpoint file");
+  if (has_agg != (x->agr_on != 0))
+    return f3d::ctx_error(F3D_ERR_ARG, "aggregation is on in only one of the checkpoint and the context");
   cudaStream_t s = x->stream;
   CK(cudaMemcpyAsync(x->prec == F3D_PREC_FP32 ? (void*)x->c32 : (void*)x->c64, c.data(), hb * esz,
                      cudaMemcpyHostToDevice, s));
@@ -927,6 +952,13 @@ int f3d_ctx_restore(f3d_ctx* x, const char* path) {
   CK(cudaMemcpyAsync(small_outmass(x), &h.outmass, sizeof(double), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(small_cd(x), &h.cd_prev, sizeof(double), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(small_cd_prev(x), &h.cd_prev, sizeof(double), cudaMemcpyHostToDevice, s));
+  if (has_agg) {
+    double* dst[5] = {x->agr_maggr, x->agr_al, x->agr_ab, x->agr_as, x->agr_ad};
+    for (int q = 0; q < 5; ++q)
+      CK(cudaMemcpyAsync(dst[q], agf.data() + q * s3, s3 * sizeof(double), cudaMemcpyHostToDevice, s));
+    x->agr_ipass = (int)agg[1];
+    x->agr_replay = (int)agg[2];  // vset scalings owed after the replayed updates (0: none made yet)
+  }
   CK(cudaStreamSynchronize(s));
   x->time = h.time;
   x->iiter = h.iiter;

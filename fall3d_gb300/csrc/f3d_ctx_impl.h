@@ -27,6 +27,8 @@ struct f3d_ctx {
   double mfr_scaled = 0.0;  // sum of the Hm1-scaled source rates (addradialwind.f90:61)
   // aggregation in transport (f3d_set_aggregation)
   int agr_on = 0, agr_iaggr = 0, agr_ndtagr = 1, agr_ipass = 0, agr_due = 0;
+  int agr_npar = 0;    // agrpar calls since the last meteo update
+  int agr_replay = 0;  // agrpar calls owed by a restored run
   double agr_Df = 3.0, agr_sumNi = 0.0;
   std::vector<double> agr_fc;  // fc(1:np)
   double *agr_fc_dev = nullptr, *agr_cls = nullptr;
@@ -108,6 +110,7 @@ int gc_divcorr(f3d_ctx* x, double massvol, double massdep, double outmass);
 // agrsrc after its point sources
 int agg_agrpar(f3d_ctx* x);
 int agg_setsrc(f3d_ctx* x);
+int agg_restore_vset(f3d_ctx* x, int times);
 // a zero-filled device allocation owned by the context
 int ctx_alloc(f3d_ctx* x, void** p, size_t bytes);
 // the binary32 copies of class ic's settling velocity (vset32, vk32 and

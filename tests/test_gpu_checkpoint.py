@@ -58,3 +58,49 @@ def test_restore_rejects_other_grid(tmp_path):
         other.restore(path)
     with pytest.raises(F.F3DError):
         F.Context(s, F.PREC_FP64).restore(path)
+
+
+@pytest.mark.parametrize("prec", [F.PREC_FP64, F.PREC_FP32])
+def test_restart_with_aggregation(tmp_path, prec):
+    """Aggregation in transport: the checkpoint carries Maggr, the agrsrc step
+    counter and the agrpar calls since the meteo update (a source update in
+    between scales vset of class iaggr once more), so a run saved after the
+    source update and before the next meteo update continues bit for bit."""
+    s = synth.make_scenario("small", seed=9, nc=7, phimin=3.0, phimax=8.0, aggregate=[0.2, 1000.0, 0.2],
+                            M0=1e7, run_h=1.0, met_dt_h=0.5, erupt_h=0.25)
+    synth.add_gas_class(s)
+    agg = synth.aggregation_inputs(s)
+    ref = F.Context(s, prec)
+    ref.set_aggregation(agg)
+    log_ref = ref.run()
+    f_ref, m_ref = ref.fields(), ref.maggr()
+    times = log_ref["time"]
+    ref.close()
+    # a step between the source update (900 s) and the next meteo update
+    probe = F.Context(s, prec)
+    probe.set_aggregation(agg)
+    k = 0
+    while True:
+        k += 1
+        probe.run(max_steps=1)
+        if probe.state()["time"] > 1000.0:
+            break
+    assert probe.state()["time"] < 1800.0
+    probe.close()
+    a = F.Context(s, prec)
+    a.set_aggregation(agg)
+    a.run(max_steps=k)
+    path = tmp_path / "agg.ckpt"
+    a.save(path)
+    a.close()
+    b = F.Context(s, prec)
+    b.set_aggregation(agg)
+    b.restore(path)
+    b.run()
+    for key in ("c", "cdry", "cwet"):
+        assert_same_bits(b.fields()[key], f_ref[key], key)
+    assert_same_bits(b.maggr(), m_ref, "maggr")
+    assert len(times) > 0
+    # a context without aggregation refuses the checkpoint
+    with pytest.raises(F.F3DError):
+        F.Context(s, prec).restore(path)
