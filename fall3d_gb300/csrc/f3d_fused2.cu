@@ -128,12 +128,14 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
   const float auxvx = a.auxvx, auxvy = a.auxvy;
 
   // ------------------------------------------------ per-position state
-  // bit 2r+c: row r (gj = gy0 + warp + NW*r), column c (gi + c)
+  // bit 2r+c: row r (gj = gy0 + 2*warp + r), column c (gi + c); a warp owns
+  // two adjacent rows, so each row's y-neighbour on the other side is the
+  // same lane's other row
   unsigned kin = 0, kgx = 0, kgy = 0, inr = 0;  // inr: the pair of row r lies in the halo array
   int h0[RPW];                                  // halo offset of (gi, gj, plane 0), clamped
 #pragma unroll
   for (int r = 0; r < RPW; ++r) {
-    const int gj = gy0 + warp + NW * r;
+    const int gj = gy0 + 2 * warp + r;
     const bool yin = gj >= 1 && gj <= ny;
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
@@ -154,7 +156,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     o_0[r] = o_p1[r] = vk0[r] = w1k[r] = w2km[r] = w2k[r] = gtop[r] = make_float2(0.0f, 0.0f);
     ra[r] = rb[r] = rc[r] = fprev[r] = gprev[r] = pb[r] = make_float2(0.0f, 0.0f);
   }
-  const unsigned sbase = (unsigned)__cvta_generic_to_shared(stage) + 4u * (unsigned)(warp * HX + 2 * lane);
+  const unsigned sbase = (unsigned)__cvta_generic_to_shared(stage) + 4u * (unsigned)(2 * warp * HX + 2 * lane);
 
   // the staged inputs of iteration t into buffer t&1 (fields as in
   // f3d_fused.cu); positions outside the halo array copy nothing (zero fill)
@@ -172,7 +174,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
                okl = g1 && t >= 2;
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
-      const unsigned dst = sb + 4u * (unsigned)(NW * r * HX);
+      const unsigned dst = sb + 4u * (unsigned)(r * HX);
       const int ht = h0[r] + t * cs;  // this row's offset at plane t
       const bool v0 = !EDGE || (inr >> (2 * r) & 1u), v1 = !EDGE || (inr >> (2 * r + 1) & 1u);
       auto cp = [&](int field, const float* base, int off) {
@@ -211,7 +213,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
   // bottom ghost, first window (setbcc.f90:19-33, advctzc work(1))
 #pragma unroll
   for (int r = 0; r < RPW; ++r) {
-    const int gj = gy0 + warp + NW * r;
+    const int gj = gy0 + 2 * warp + r;
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
       if (!(kin >> (2 * r + c) & 1u)) continue;
@@ -252,8 +254,8 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     // barrier, after which no warp reads its advection fields
     const bool early = STEADY || (t >= 3 && t <= nz);
     if (early) prefetch(edge_c, t + 1, 0);
-    const float* sb = stage + (t & 1) * (NF * NP) + warp * HX + 2 * lane;  // this lane's row-0 position
-    auto at = [&](int field, int r) { return sb + field * NP + NW * r * HX; };
+    const float* sb = stage + (t & 1) * (NF * NP) + 2 * warp * HX + 2 * lane;  // this lane's row-0 position
+    auto at = [&](int field, int r) { return sb + field * NP + r * HX; };
     auto km = [&](int r, int c) { return (kin >> (2 * r + c) & 1u) != 0; };
     float2 s2[RPW];
     if (STEADY || t <= nz) {
@@ -262,7 +264,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
       // ---------------- A: setbcc ghosts + advctzc for plane t
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
-        const int gj = gy0 + warp + NW * r;
+        const int gj = gy0 + 2 * warp + r;
         float2 ghost = make_float2(0.0f, 0.0f);
         if constexpr (EDGE) {
           // x-face ghosts from the neighbouring column's original c and vx (setbcc.f90:53-66)
@@ -360,38 +362,49 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
         }
       };
       auto adv_y = [&](const float2* in, float2* out) {
-        float* P0 = P0s + warp * HX + 2 * lane;
-        float* W1 = W1s + warp * HX + 2 * lane;
-        float* W2 = W2s + warp * HX + 2 * lane;
+        float* P0 = P0s + 2 * warp * HX + 2 * lane;
+        float* W1 = W1s + 2 * warp * HX + 2 * lane;
+        float* W2 = W2s + 2 * warp * HX + 2 * lane;
 #pragma unroll
-        for (int r = 0; r < RPW; ++r) sts2(P0 + NW * r * HX, in[r]);
+        for (int r = 0; r < RPW; ++r) sts2(P0 + r * HX, in[r]);
         __syncthreads();
         // every thread is past iteration t-1: its staging buffer may be refilled
         prefetch(edge_c, t + 1, early ? 1 : 2);
+        static_assert(RPW == 2, "a warp owns a pair of adjacent rows");
         float2 w1s[RPW], w2s[RPW], vs[RPW];
+        // y-neighbours: the rows below and above this lane's pair come from
+        // the neighbouring warps, the rest from its own registers
+        vs[0] = lds2(at(F_VY, 0));
+        vs[1] = lds2(at(F_VY, 1));
+        const float2 cmv[RPW] = {lds2(P0 - HX), in[0]};
+        const float2 cpv[RPW] = {in[1], lds2(P0 + 2 * HX)};
+        const float2 vmv[RPW] = {lds2(at(F_VY, 0) - HX), vs[0]};  // vy(i, j-1)
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
-          const int gj = gy0 + warp + NW * r;
+          const int gj = gy0 + 2 * warp + r;
           const float2 c0 = in[r];
-          const float2 cm = lds2(P0 + NW * r * HX - HX), cp = lds2(P0 + NW * r * HX + HX);
-          const float2 v = lds2(at(F_VY, r)), vmr = lds2(at(F_VY, r) - HX);  // vy(i, j-1)
-          vs[r] = v;
+          const float2 cm = cmv[r], cp = cpv[r];
+          const float2 v = vs[r], vmr = vmv[r];
           if constexpr (EDGE) {  // row conditions are uniform across the warp
             line_work2(cm, c0, cp, v, gj == 1 ? v : vmr, auxvy, a.inv_dy, dt, w1s[r], w2s[r]);
             if (gj == ny + 1) w1s[r] = mul2(mul2(splat(auxvy), vmr), sub2(c0, cm));  // advcty.f90:45
           } else {
             line_work2(cm, c0, cp, v, vmr, auxvy, a.inv_dy, dt, w1s[r], w2s[r]);
           }
-          sts2(W1 + NW * r * HX, w1s[r]);
-          sts2(W2 + NW * r * HX, w2s[r]);
         }
+        sts2(W1, w1s[0]);  // the row above the pair below reads it
+        sts2(W2, w2s[0]);
+        sts2(W2 + HX, w2s[1]);
         __syncthreads();
+        const float2 w1pv[RPW] = {w1s[1], lds2(W1 + 2 * HX)};
+        const float2 w2mv[RPW] = {lds2(W2 - HX), w2s[0]};
+        const float2 w2pv[RPW] = {w2s[1], lds2(W2 + 2 * HX)};
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
-          const float2 w1p = lds2(W1 + NW * r * HX + HX);
-          float2 w2m = lds2(W2 + NW * r * HX - HX), w2p = lds2(W2 + NW * r * HX + HX);
+          const float2 w1p = w1pv[r];
+          float2 w2m = w2mv[r], w2p = w2pv[r];
           if constexpr (EDGE) {
-            const int gj = gy0 + warp + NW * r;
+            const int gj = gy0 + 2 * warp + r;
             if (gj == 1) w2m = w2s[r];
             if (gj == ny) w2p = w2s[r];
             const float2 u = line_update2(in[r], vs[r], w1s[r], w1p, w2s[r], w2m, w2p);
@@ -458,7 +471,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
           const bool ok = (inr >> (2 * r + c) & 1u) != 0;
-          const int hh = ok ? gi + c + px * (gy0 + warp + NW * r) + (nz - 1) * cs : 0;
+          const int hh = ok ? gi + c + px * (gy0 + 2 * warp + r) + (nz - 1) * cs : 0;
           cmp(la, c) = __ldg(a.lrhoh + hh);
           cmp(pa, c) = __ldg(a.pkzh + hh);
         }
@@ -504,7 +517,10 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
       }
     };
     auto dif_y = [&](const float2* in, float2* out) {
-      float* P1 = P1s + warp * HX + 2 * lane;
+      float* P1 = P1s + 2 * warp * HX + 2 * lane;
+      const float2 P0v[RPW] = {lds2(at(F_PY, 0)), lds2(at(F_PY, 1))};
+      const float2 Pmv[RPW] = {lds2(at(F_PY, 0) - HX), P0v[0]};
+      const float2 Ppv[RPW] = {P0v[1], lds2(at(F_PY, 1) + HX)};
       if constexpr (!EDGE) {
         // neighbours read c/rho: the products c*(1/rho) of diffy.f90:34-40,
         // each computed once by its owner
@@ -512,32 +528,33 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
           q[r] = mul2(in[r], lbv[r]);
-          sts2(P1 + NW * r * HX, q[r]);
+          sts2(P1 + r * HX, q[r]);
         }
         __syncthreads();
+        const float2 qm[RPW] = {lds2(P1 - HX), q[0]};
+        const float2 qp[RPW] = {q[1], lds2(P1 + 2 * HX)};
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
-          const float* PY = at(F_PY, r);
-          const float2 Pm = lds2(PY - HX), P0 = lds2(PY), Pp = lds2(PY + HX);
-          const float2 gradr =
-              mul2(mul2(splat(0.5f), add2(Pp, P0)), sub2(lds2(P1 + NW * r * HX + HX), q[r]));
-          const float2 gradl =
-              mul2(mul2(splat(0.5f), add2(P0, Pm)), sub2(q[r], lds2(P1 + NW * r * HX - HX)));
+          const float2 Pm = Pmv[r], P0 = P0v[r], Pp = Ppv[r];
+          const float2 gradr = mul2(mul2(splat(0.5f), add2(Pp, P0)), sub2(qp[r], q[r]));
+          const float2 gradl = mul2(mul2(splat(0.5f), add2(P0, Pm)), sub2(q[r], qm[r]));
           out[r] = add2(in[r], mul2(splat(a.dtdy2), sub2(gradr, gradl)));
         }
         return;
       }
 #pragma unroll
-      for (int r = 0; r < RPW; ++r) sts2(P1 + NW * r * HX, in[r]);
+      for (int r = 0; r < RPW; ++r) sts2(P1 + r * HX, in[r]);
       __syncthreads();
+      const float2 cmv[RPW] = {lds2(P1 - HX), in[0]};
+      const float2 cpv[RPW] = {in[1], lds2(P1 + 2 * HX)};
+      const float2 lmv[RPW] = {lds2(at(F_L1, 0) - HX), lbv[0]};
+      const float2 lpv[RPW] = {lbv[1], lds2(at(F_L1, 1) + HX)};
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
-        const float* L = at(F_L1, r);
-        const float* PY = at(F_PY, r);
-        const float2 cm = lds2(P1 + NW * r * HX - HX), cp = lds2(P1 + NW * r * HX + HX);
-        const float2 lm = lds2(L - HX), lp = lds2(L + HX), Pm = lds2(PY - HX), P0 = lds2(PY), Pp = lds2(PY + HX);
+        const float2 cm = cmv[r], cp = cpv[r];
+        const float2 lm = lmv[r], lp = lpv[r], Pm = Pmv[r], P0 = P0v[r], Pp = Ppv[r];
         if constexpr (EDGE) {
-          const int gj = gy0 + warp + NW * r;
+          const int gj = gy0 + 2 * warp + r;
           float2 u;
           if (gj == 1 || gj == ny) {  // uniform across the warp
 #pragma unroll
@@ -568,7 +585,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
       const bool o0 = 2 * lane >= 3 && 2 * lane < 3 + TX, o1 = 2 * lane + 1 >= 3 && 2 * lane + 1 < 3 + TX;
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
-        const int hy = warp + NW * r;
+        const int hy = 2 * warp + r;
         if (hy < 3 || hy >= 3 + TY) continue;  // uniform across the warp
         float2 res = s4[r];
         if (wet && k <= s_kzmax) {  // uniform across the block
@@ -595,7 +612,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     }
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
-      const int hy = warp + NW * r;
+      const int hy = 2 * warp + r;
       const int gj = gy0 + hy;
       const int hrow = gi + px * gj + k * cs;  // halo index of the first column
       float2 res = s4[r];
