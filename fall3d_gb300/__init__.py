@@ -83,6 +83,7 @@ def load(build_if_missing: bool = False):
                        VP, VP, VP, VP, VP],
         "f3d_setvset": [IP, IP, IP, IP, IP, IP, VP, VP, VP, VP, VP, VP, IP, DP, VP, DP],
         "f3d_setvdrydep": [IP, IP, IP, VP, VP, VP, VP, VP, VP, VP, VP, VP],
+        "f3d_dmath_eval": [I, C.c_longlong, VP, VP],
         "f3d_meteo_scale": [IP, IP, IP, IP, DP, DP, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP],
         "f3d_ctx_create": [VP, C.POINTER(VP)],
         "f3d_ctx_destroy": [VP],
@@ -311,6 +312,16 @@ def setvset(nx, ny, nz, nc, np_, modv, diam, rhop, psi, sphe, tempe, rho, aggreg
                               _addr(rhop), _addr(psi), _addr(sphe), _addr(tempe), _addr(rho),
                               _i(aggregate), _d(vset_factor), _addr(vset), C.byref(cdv)))
     return cdv.value
+
+
+def dmath_eval(op, x):
+    """The drag iteration's table-driven binary64 log (op 0) or exp (op 1)
+    of every value of the float64 array x (a diagnostic; returns a new
+    array)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    _check(load().f3d_dmath_eval(int(op), x.size, _addr(x), _addr(y)))
+    return y
 
 
 def setvdrydep(nx, ny, nc, diam, zlayer, ldu, rl, znt, ustar, tempe, rho, vdep):

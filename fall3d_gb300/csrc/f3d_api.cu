@@ -618,6 +618,17 @@ int f3d_setvset(const int* nx, const int* ny, const int* nz, const int* nc, cons
   return F3D_OK;
 }
 
+int f3d_dmath_eval(int op, long long n, const double* x, double* y) {
+  if ((op != 0 && op != 1) || n < 0) return set_error(F3D_ERR_ARG, "op must be 0 (log) or 1 (exp), n >= 0");
+  if (n > 0 && (!x || !y)) return set_error(F3D_ERR_ARG, "NULL argument");
+  Marshal m;
+  const double* dx = m.arr(x, (size_t)n, false);
+  double* dy = m.arr(y, (size_t)n, true);
+  if (m.error()) return m.error();
+  launch_dmath_eval(op, n, dx, dy, 0);
+  return m.finish();
+}
+
 int f3d_setvdrydep(const int* nx, const int* ny, const int* nc, const double* diam,
                    const double* zlayer, const double* ldu, const double* rl, const double* znt,
                    const double* ustar, const double* tempe, const double* rho, double* vdep) {

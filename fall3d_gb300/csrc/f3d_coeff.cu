@@ -15,8 +15,15 @@
 // contracts, so the warm-up reaches the exact chain value within a few to a
 // few tens of cells; any segment that fails the check is recomputed in order
 // from the verified exit of its predecessor.
+//
+// The drag iteration is binary64-pipe bound on GB300, so its Ganser form is
+// restated with one division, one reciprocal square root and a table-driven
+// log/exp per iteration (f3d_dmath.cuh) in place of the reference's four
+// divisions, square root and pow: the same iteration and stopping test on
+// values that differ from the reference's by a few ulp.
 #include <algorithm>
 
+#include "f3d_dmath.cuh"
 #include "f3d_internal.h"
 
 namespace f3d {
@@ -323,6 +330,7 @@ struct ClassConst {
   double diam, rhop, psi;
   double num;       // 4*gi*diam*rhop, the numerator of setvset.f90:104
   double rk1, rk2;  // Ganser shape factors (setvset.f90:127-128)
+  double rk12;      // rk1 * rk2
   double cd100;     // Wilson
   int ok;           // get_gama converged
 };
@@ -360,7 +368,7 @@ __global__ void k_class_consts(int np, int modv, const double* diam, const doubl
   k.rhop = rhop[ic];
   k.psi = psi[ic];
   k.num = 4.0 * gi * k.diam * k.rhop;
-  k.rk1 = k.rk2 = k.cd100 = 0.0;
+  k.rk1 = k.rk2 = k.rk12 = k.cd100 = 0.0;
   k.ok = 1;
   if (modv == 2) {
     double gama;
@@ -369,6 +377,7 @@ __global__ void k_class_consts(int np, int modv, const double* diam, const doubl
     const double dnd = 0.5 * (1.0 + gama) * pow(gama, (double)(-2.0f / 3.0f));
     k.rk1 = 1.0 / (dnd / 3.0 + 2.0 / (3.0 * sqrt(k.psi)));
     k.rk2 = pow(10.0, 1.8148 * pow(-log10(k.psi), 0.5743));
+    k.rk12 = k.rk1 * k.rk2;
   } else if (modv == 3) {
     k.cd100 = 0.24 * pow(k.psi, -0.828) + 2.0 * sqrt(1.0 - k.psi);
   }
@@ -377,10 +386,35 @@ __global__ void k_class_consts(int np, int modv, const double* diam, const doubl
 
 // Sources/setvset.f90:65-181 for one call; returns iterations (0 for the
 // closed-form Dellino model) or -1 when maxit is reached.
+//
+// Ganser (setvset.f90:117-136): with R = rey*rk1*rk2 = G*v,
+// G = rhoa*diam*rk1*rk2/visc, and v = T/sqrt(cd), T = sqrt(4*gi*diam*rhop/(3*rhoa)),
+//   cd = 24/(rey*rk1)*(1 + 0.1118*R^0.6567) + 0.4305*rk2/(1 + 3305/R)
+//      = rk2*((24*(R + 3305) + 0.4305*R^2)/(R*(R + 3305)) + 24*0.1118*R^(0.6567-1)).
 __device__ int vsettl_dev(const ClassConst& k, int model, double rhoa, double visc, double& cd,
-                          double& vset) {
+                          double& vset, const DMathTab& tab) {
   const double eps = 1e-3;
   double vold = 1e5, v = 0.0;
+  if (model == 2) {
+    const double T = sqrt(k.num / (3.0 * rhoa));
+    const double G = rhoa * k.diam * k.rk12 / visc;
+    for (int it = 1; it <= 100; ++it) {
+      v = T * rsqrt(cd);
+      const double R = G * v;
+      const double L = dm_log(tab, R);
+      const double P = dm_exp(tab, fma(0.6567, L, -L));  // R^0.6567 / R
+      const double Q = R + 3305.0;
+      const double N = fma(0.4305 * R, R, 24.0 * Q);
+      cd = k.rk2 * fma(24.0 * 0.1118, P, N / (R * Q));
+      if (it > 1 && fabs(v - vold) <= eps) {
+        vset = T * rsqrt(cd);
+        return it;
+      }
+      vold = v;
+    }
+    vset = v;
+    return -1;
+  }
   if (model == 4) {
     const double gi = 9.81, diam = k.diam;
     v = pow((diam * diam * diam * gi * (k.rhop - rhoa) * rhoa * pow(k.psi, 1.6)) / (visc * visc),
@@ -391,10 +425,7 @@ __device__ int vsettl_dev(const ClassConst& k, int model, double rhoa, double vi
   for (int it = 1; it <= 100; ++it) {
     v = sqrt(k.num / (3.0 * cd * rhoa));
     const double rey = rhoa * v * k.diam / visc;
-    if (model == 2) {
-      cd = 24.0 / (rey * k.rk1) * (1.0 + 0.1118 * pow(rey * k.rk1 * k.rk2, 0.6567)) +
-           0.4305 * k.rk2 / (1.0 + 3305.0 / (rey * k.rk1 * k.rk2));
-    } else if (model == 1) {
+    if (model == 1) {
       if (rey <= 988.947)
         cd = 24.0 / rey * (1.0 + 0.15 * pow(rey, 0.687));
       else
@@ -456,7 +487,8 @@ __global__ void k_visc(long long s3, const double* tempe, double* visc) {
 // Runs chain cells [q0, q1) from cd; writes outputs when `write`.
 __device__ void chain_run(const ChainGeom& g, long long q0, long long q1, int modv,
                           const ClassConst* cc, const double* viscs, const double* rho,
-                          double* vset, int* iters, double& cd, bool write, int& nonconv) {
+                          double* vset, int* iters, double& cd, bool write, int& nonconv,
+                          const DMathTab& tab) {
   const long long s3 = g.d.cells();
   for (long long q = q0; q < q1; ++q) {
     int ic;
@@ -464,7 +496,7 @@ __device__ void chain_run(const ChainGeom& g, long long q0, long long q1, int mo
     chain_cell(g, q, ic, m);
     const double visc = viscs[m];
     double v;
-    const int it = vsettl_dev(cc[ic], modv, rho[m], visc, cd, v);
+    const int it = vsettl_dev(cc[ic], modv, rho[m], visc, cd, v, tab);
     if (write) {
       vset[(long long)ic * s3 + m] = v;
       if (iters) iters[(long long)ic * s3 + m] = it;
@@ -477,6 +509,9 @@ __global__ void k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, co
                                  const double* rho, double* vset, int* iters,
                                  const double* cd_state, double* entry, double* exitv,
                                  int* nonconv) {
+  __shared__ DMathTab tab;
+  dmath_tab_init(tab);
+  __syncthreads();
   const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (s >= g.nseg) return;
   const long long q0 = s * g.S, q1 = min(g.L, q0 + g.S);
@@ -486,10 +521,10 @@ __global__ void k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, co
     cd = *cd_state;
   } else {
     cd = 1.0;
-    chain_run(g, max(0LL, q0 - g.W), q0, modv, cc, visc, rho, vset, iters, cd, false, dummy);
+    chain_run(g, max(0LL, q0 - g.W), q0, modv, cc, visc, rho, vset, iters, cd, false, dummy, tab);
   }
   entry[s] = cd;
-  chain_run(g, q0, q1, modv, cc, visc, rho, vset, iters, cd, true, nc_flag);
+  chain_run(g, q0, q1, modv, cc, visc, rho, vset, iters, cd, true, nc_flag, tab);
   exitv[s] = cd;
   nonconv[s] = nc_flag;
 }
@@ -512,6 +547,9 @@ __global__ void k_chain_fix(ChainGeom g, int modv, const ClassConst* cc, const d
                             const double* rho, double* vset, int* iters, double* entry,
                             double* exitv, int* nonconv, int* bad, const int* nbad, int cap,
                             double* cd_state) {
+  __shared__ DMathTab tab;
+  dmath_tab_init(tab);
+  __syncthreads();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int nb = *nbad;
   if (nb > 0) {
@@ -536,7 +574,7 @@ __global__ void k_chain_fix(ChainGeom g, int modv, const ClassConst* cc, const d
         int nc_flag = 0;
         entry[s] = cd;
         const long long q0 = s * g.S, q1 = min(g.L, q0 + g.S);
-        chain_run(g, q0, q1, modv, cc, visc, rho, vset, iters, cd, true, nc_flag);
+        chain_run(g, q0, q1, modv, cc, visc, rho, vset, iters, cd, true, nc_flag, tab);
         exitv[s] = cd;
         nonconv[s] = nc_flag;
         ++s;  // the successor must be re-checked
@@ -557,6 +595,21 @@ __global__ void k_chain_fix(ChainGeom g, int modv, const ClassConst* cc, const d
 __global__ void k_chain_status(ChainGeom g, const int* nonconv, int* status) {
   const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (s < g.nseg && nonconv[s]) atomicOr(status, 1);
+}
+
+__global__ void k_dmath_eval(int op, long long n, const double* x, double* y) {
+  __shared__ DMathTab tab;
+  dmath_tab_init(tab);
+  __syncthreads();
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    y[q] = op == 0 ? dm_log(tab, x[q]) : dm_exp(tab, x[q]);
+}
+
+void launch_dmath_eval(int op, long long n, const double* x, double* y, cudaStream_t s) {
+  if (n <= 0) return;
+  k_dmath_eval<<<(unsigned)std::min<long long>((n + 255) / 256, 152LL * 8), 256, 0, s>>>(op, n, x, y);
+  count_launch();
 }
 
 // setvset.f90:48-60: the aggregate loop touches class np+1 (a gas class with

@@ -163,6 +163,8 @@ void launch_setvset(Dims d, int nc, int np, int modv, const double* diam, const 
                     const double* psi, const double* sphe, const double* tempe,
                     const double* rho, int aggregate, double vset_factor, double* vset,
                     int* iters, double* cd_state, void* scratch, int* status, cudaStream_t s);
+// The drag iteration's table-driven log (op 0) and exp (op 1) on n values.
+void launch_dmath_eval(int op, long long n, const double* x, double* y, cudaStream_t s);
 
 // Conversions for the FP32 form.
 void launch_d2f(float* dst, const double* src, long long n, cudaStream_t s);

@@ -6,11 +6,13 @@ that profiler captures of the step kernels run.
                                         [--time]
 
 With --time, the steps after the first are timed per kernel with CUDA
-events and printed as milliseconds per launch.
+events and printed as milliseconds per launch, then two meteo updates are
+timed on the host clock.
 """
 from __future__ import annotations
 
 import argparse
+import time
 
 import fall3d_gb300 as F
 from fall3d_gb300 import synth
@@ -43,6 +45,11 @@ def main():
         g.sync()
         for name, (n, ms) in sorted(g.profile_read().items(), key=lambda kv: -kv[1][1]):
             print(f"  {name:12s} {n:4d} launches {ms / max(n, 1):9.4f} ms/launch")
+        for snap in (1, 0):  # a meteo update: upload, coefficient chain, settling velocities
+            t0 = time.perf_counter()
+            g.meteo(snap)
+            g.sync()
+            print(f"  meteo update {time.perf_counter() - t0:9.4f} s (host clock, upload included)")
     else:
         g.step(args.steps)
     g.sync()

@@ -242,6 +242,11 @@ int f3d_setvset(const int* nx, const int* ny, const int* nz, const int* nc,
                 const double* tempe, const double* rho, const int* aggregate,
                 const double* vset_factor, double* vset, double* cd);
 
+/* Diagnostic: the binary64 log (op 0) or exp (op 1) that setvset's Ganser
+ * drag iteration uses in place of pow (a table-driven restatement, within a
+ * few ulp), on n host or device values.  No reference counterpart. */
+int f3d_dmath_eval(int op, long long n, const double* x, double* y);
+
 /* Sources/setvdrydep.f90:1 setvdrydep (module state made explicit). */
 int f3d_setvdrydep(const int* nx, const int* ny, const int* nc,
                    const double* diam, const double* zlayer,
