@@ -276,7 +276,7 @@ int f3d_diffx(double* c, const int* nx, const int* ny, const int* nz, const int*
   const double* drk = m.arr(rkhor, (size_t)d.cells(), false);
   const double* drho = m.arr(rho, (size_t)d.cells(), false);
   if (m.error()) return m.error();
-  launch_diffx<double>(dc, 0, d, *nz_loc, *iz_loc, *dx, *dt, drk, drho, 1, 0);
+  launch_diffx<double>(dc, 0, d, *nz_loc, *iz_loc, *dx, *dt, drk, drho, nullptr, nullptr, 1, 0);
   return m.finish();
 }
 
@@ -292,7 +292,7 @@ int f3d_diffy(double* c, const int* nx, const int* ny, const int* nz, const int*
   const double* drk = m.arr(rkhor, (size_t)d.cells(), false);
   const double* drho = m.arr(rho, (size_t)d.cells(), false);
   if (m.error()) return m.error();
-  launch_diffy<double>(dc, 0, d, *nz_loc, *iz_loc, *dy, *dt, drk, drho, 1, 0);
+  launch_diffy<double>(dc, 0, d, *nz_loc, *iz_loc, *dy, *dt, drk, drho, nullptr, nullptr, 1, 0);
   return m.finish();
 }
 

@@ -28,6 +28,23 @@ F3D_HD T fabs_t(T x) { return x < T(0) ? -x : (x == T(0) ? T(0) : x); }
 __device__ __forceinline__ double absd(double x) { return fabs(x); }
 __device__ __forceinline__ float absd(float x) { return fabsf(x); }
 
+// The slope limiter of advctx.f90:34-40 (and advcty), with
+// deltar = a/dx, deltal = b/dx:
+//   sigma = 0.5*(SIGN(1,deltar)+SIGN(1,deltal))*MIN(|deltar|,|deltal|).
+// For dx > 0, x -> RN(x/dx) is monotonic and keeps the sign of x (zeros and
+// underflows included), so SIGN(1,RN(a/dx)) = SIGN(1,a) and
+// MIN(|RN(a/dx)|,|RN(b/dx)|) = RN(m/dx) with m = MIN(|a|,|b|) under the same
+// MIN rule (NaN operands included): one division instead of two, the same
+// bits.  Other dx take the reference's two divisions.
+template <class T>
+__device__ __forceinline__ T minmod_div(T a, T b, T dx) {
+  if (!(dx > T(0))) {
+    const T dr = a / dx, dl = b / dx;
+    return T(0.5) * (sign1(dr) + sign1(dl)) * fmin2(absd(dr), absd(dl));
+  }
+  return T(0.5) * (sign1(a) + sign1(b)) * (fmin2(absd(a), absd(b)) / dx);
+}
+
 // Grid geometry of one scenario (interior nx, ny, nz; halo arrays are
 // (nx+2)(ny+2)(nz+2), x fastest).
 struct Dims {

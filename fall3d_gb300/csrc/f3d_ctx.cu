@@ -113,6 +113,7 @@ long long footprint_bytes(const f3d_grid* g) {
     b += 4LL * (11 * s3 + s3 * nc + pl * nc + nz + 1) + 8LL * pl + nc;
   } else {
     b += 8LL * halo * nc;
+    b += 8LL * 3 * s3;  // 1/rho, rkh1*rho, rkhor*rho
   }
   b += (long long)f3d::reduce_scratch_bytes(2LL * nc * (nx + ny) * nz + nc * pl, 4);
   b += (long long)f3d::setvset_scratch_bytes(Dims{g->nx, g->ny, g->nz}, g->np);
@@ -186,6 +187,9 @@ struct Fields<double> {
   static const double* vset(f3d_ctx* x) { return x->vset; }
   static const double* vdep(f3d_ctx* x) { return x->vdep; }
   static const double* dz(f3d_ctx* x) { return x->dz; }
+  static const double* lrho(f3d_ctx* x) { return x->lrho64; }
+  static const double* pkx(f3d_ctx* x) { return x->pkx64; }
+  static const double* pky(f3d_ctx* x) { return x->pky64; }
 };
 template <>
 struct Fields<float> {
@@ -200,6 +204,10 @@ struct Fields<float> {
   static const float* vset(f3d_ctx* x) { return x->vset32; }
   static const float* vdep(f3d_ctx* x) { return x->vdep32; }
   static const float* dz(f3d_ctx* x) { return x->dz32; }
+  // the per-routine binary32 sweeps divide in binary32 themselves
+  static const float* lrho(f3d_ctx*) { return nullptr; }
+  static const float* pkx(f3d_ctx*) { return nullptr; }
+  static const float* pky(f3d_ctx*) { return nullptr; }
 };
 
 // Sources/sizloop.f90:31-83 for all classes, class-batched sweeps.
@@ -223,11 +231,11 @@ void sizloop(f3d_ctx* x) {
   };
   auto difx = [&] {
     ProfScope ps(x, "diffx");
-    launch_diffx<T>(c, hb, d, nz, 1, dX1, dt, F::rkh1(x), F::rho(x), nc, s);
+    launch_diffx<T>(c, hb, d, nz, 1, dX1, dt, F::rkh1(x), F::rho(x), F::lrho(x), F::pkx(x), nc, s);
   };
   auto dify = [&] {
     ProfScope ps(x, "diffy");
-    launch_diffy<T>(c, hb, d, nz, 1, dX2, dt, F::rkhor(x), F::rho(x), nc, s);
+    launch_diffy<T>(c, hb, d, nz, 1, dX2, dt, F::rkhor(x), F::rho(x), F::lrho(x), F::pky(x), nc, s);
   };
   {
     ProfScope ps(x, "setbcc");
@@ -446,6 +454,11 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
   A(cwet, pl * (nc + 1));
   A(cload, pl * (nc + 1));
   A(small, 64);
+  if (x->prec == F3D_PREC_FP64) {
+    A(lrho64, s3);
+    A(pkx64, s3);
+    A(pky64, s3);
+  }
   if (x->prec == F3D_PREC_FP32) {
     A(c32, hb * nc);
     A(vx32, s3);
@@ -585,6 +598,8 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
   CK(cudaMemsetAsync(small_dtcn(x), 0, sizeof(unsigned long long), s));
   launch_finddt(d, g.nc, g.dX1, g.dX2, x->dz, x->vx, x->vy, x->vz, x->vset, x->rkh1, x->rkhor,
                 x->rkver, small_dtcn(x), s);
+  if (x->prec == F3D_PREC_FP64)
+    launch_diff_coeffs((long long)s3, x->rho, x->rkh1, x->rkhor, x->lrho64, x->pkx64, x->pky64, s);
   if (x->prec == F3D_PREC_FP32) {
     launch_d2f(x->vx32, x->vx, (long long)s3, s);
     launch_d2f(x->vy32, x->vy, (long long)s3, s);

@@ -224,9 +224,7 @@ __device__ __forceinline__ void adv_line_work(const T* cl, int q, int n, T vq, T
                                               T auxv, T& w1, T& w2) {
   const T vq_12 = T(0.5) * (vq + vq_1);
   w1 = auxv * (vq * cl[q] - vq_1 * cl[q - 1]);
-  const T deltar = (cl[q + 1] - cl[q]) / dx;
-  const T deltal = (cl[q] - cl[q - 1]) / dx;
-  const T sigma = T(0.5) * (sign1(deltar) + sign1(deltal)) * fmin2(absd(deltar), absd(deltal));
+  const T sigma = minmod_div(cl[q + 1] - cl[q], cl[q] - cl[q - 1], dx);
   const T Cri = auxv * absd(vq_12);
   w2 = dt * T(0.5) * (T(1) - Cri) * sigma * absd(vq_12);
   (void)n;
@@ -293,10 +291,7 @@ __global__ void k_advcty(T* c, long long cstride, Dims d, int iz_loc, const T* v
         const T vq_12 = T(0.5) * (vq + vq_1);
         const T cq = cl[q * TI + tx], cm = cl[(q - 1) * TI + tx], cp = cl[(q + 1) * TI + tx];
         w1[q * TI + tx] = auxv * (vq * cq - vq_1 * cm);
-        const T deltar = (cp - cq) / dy;
-        const T deltal = (cq - cm) / dy;
-        const T sigma =
-            T(0.5) * (sign1(deltar) + sign1(deltal)) * fmin2(absd(deltar), absd(deltal));
+        const T sigma = minmod_div(cp - cq, cq - cm, dy);
         const T Crj = auxv * absd(vq_12);
         w2[q * TI + tx] = dt * T(0.5) * (T(1) - Crj) * sigma * absd(vq_12);
       } else {
@@ -469,7 +464,7 @@ __device__ __forceinline__ T diff_line_cell(int q, int n, const T* cl, const T* 
 
 template <class T>
 __global__ void k_diffx(T* c, long long cstride, Dims d, int iz_loc, T dx, T dt, const T* rkh,
-                        const T* rho) {
+                        const T* rho, const T* lrp, const T* pkp) {
   extern __shared__ unsigned char smem_raw[];
   const int nx = d.nx, ny = d.ny;
   T* cl = reinterpret_cast<T*>(smem_raw);
@@ -481,9 +476,14 @@ __global__ void k_diffx(T* c, long long cstride, Dims d, int iz_loc, T dx, T dt,
   for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) {
     cl[q] = cc[q];
     if (q >= 1 && q <= nx) {
-      const T r = rho[mb + q];
-      lr[q] = T(1) / r;
-      pk[q] = rkh[mb + q] * r;
+      if (lrp) {
+        lr[q] = lrp[mb + q];
+        pk[q] = pkp[mb + q];
+      } else {
+        const T r = rho[mb + q];
+        lr[q] = T(1) / r;
+        pk[q] = rkh[mb + q] * r;
+      }
     }
   }
   __syncthreads();
@@ -494,7 +494,7 @@ __global__ void k_diffx(T* c, long long cstride, Dims d, int iz_loc, T dx, T dt,
 
 template <class T>
 __global__ void k_diffy(T* c, long long cstride, Dims d, int iz_loc, T dy, T dt, const T* rkh,
-                        const T* rho) {
+                        const T* rho, const T* lrp, const T* pkp) {
   extern __shared__ unsigned char smem_raw[];
   const int nx = d.nx, ny = d.ny, TI = blockDim.x;
   T* cl = reinterpret_cast<T*>(smem_raw);
@@ -512,9 +512,14 @@ __global__ void k_diffy(T* c, long long cstride, Dims d, int iz_loc, T dy, T dt,
   for (int q = ty; q <= ny + 1; q += TJ) {
     cl[q * TI + tx] = act ? cc[base + q * rowstride] : T(0);
     if (q >= 1 && q <= ny) {
-      const T r = act ? rho[vb + (long long)q * nx] : T(1);
-      lr[q * TI + tx] = T(1) / r;
-      pk[q * TI + tx] = act ? rkh[vb + (long long)q * nx] * r : T(0);
+      if (lrp) {
+        lr[q * TI + tx] = act ? lrp[vb + (long long)q * nx] : T(1);
+        pk[q * TI + tx] = act ? pkp[vb + (long long)q * nx] : T(0);
+      } else {
+        const T r = act ? rho[vb + (long long)q * nx] : T(1);
+        lr[q * TI + tx] = T(1) / r;
+        pk[q * TI + tx] = act ? rkh[vb + (long long)q * nx] * r : T(0);
+      }
     }
   }
   __syncthreads();
@@ -526,24 +531,44 @@ __global__ void k_diffy(T* c, long long cstride, Dims d, int iz_loc, T dy, T dt,
 
 template <class T>
 void launch_diffx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dx, T dt,
-                  const T* rkh, const T* rho, int ncls, cudaStream_t s) {
+                  const T* rkh, const T* rho, const T* lr, const T* pk, int ncls, cudaStream_t s) {
   const size_t sm = 3 * (size_t)(d.nx + 2) * sizeof(T);
   set_smem((const void*)k_diffx<T>, sm);
   const int bs = d.nx >= 256 ? 256 : 128;
-  k_diffx<T><<<dim3(d.ny * nz_loc, ncls), bs, sm, s>>>(c, cstride, d, iz_loc, dx, dt, rkh, rho);
+  k_diffx<T><<<dim3(d.ny * nz_loc, ncls), bs, sm, s>>>(c, cstride, d, iz_loc, dx, dt, rkh, rho, lr, pk);
   count_launch();
 }
 
 template <class T>
 void launch_diffy(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dy, T dt,
-                  const T* rkh, const T* rho, int ncls, cudaStream_t s) {
+                  const T* rkh, const T* rho, const T* lr, const T* pk, int ncls, cudaStream_t s) {
   const int TI = pick_ti(d.ny, sizeof(T), 3);
   const int TJ = 256 / TI;
   const size_t sm = 3 * (size_t)(d.ny + 2) * TI * sizeof(T);
   set_smem((const void*)k_diffy<T>, sm);
   const int ntile = (d.nx + TI - 1) / TI;
   k_diffy<T><<<dim3(ntile * nz_loc, ncls), dim3(TI, TJ), sm, s>>>(c, cstride, d, iz_loc, dy, dt,
-                                                                   rkh, rho);
+                                                                   rkh, rho, lr, pk);
+  count_launch();
+}
+
+// The class-independent factors of diffx/diffy for one meteo update, with
+// the sweeps' own operations (so the sweeps read the same bits).
+__global__ void k_diff_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,
+                              double* lr, double* pkx, double* pky) {
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
+       m += (long long)gridDim.x * blockDim.x) {
+    const double r = rho[m];
+    lr[m] = 1.0 / r;
+    pkx[m] = rkh1[m] * r;
+    pky[m] = rkhor[m] * r;
+  }
+}
+
+void launch_diff_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,
+                        double* lr, double* pkx, double* pky, cudaStream_t s) {
+  const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  k_diff_coeffs<<<nb, 256, 0, s>>>(n, rho, rkh1, rkhor, lr, pkx, pky);
   count_launch();
 }
 
@@ -752,10 +777,10 @@ void launch_f2d(double* dst, const float* src, long long n, cudaStream_t s) {
                                  cudaStream_t);                                                  \
   template void launch_diffz<T>(T*, long long, Dims, int, int, const T*, T, const T*, const T*,  \
                                 int, cudaStream_t);                                              \
-  template void launch_diffx<T>(T*, long long, Dims, int, int, T, T, const T*, const T*, int,    \
-                                cudaStream_t);                                                   \
-  template void launch_diffy<T>(T*, long long, Dims, int, int, T, T, const T*, const T*, int,    \
-                                cudaStream_t);                                                   \
+  template void launch_diffx<T>(T*, long long, Dims, int, int, T, T, const T*, const T*,        \
+                                const T*, const T*, int, cudaStream_t);                          \
+  template void launch_diffy<T>(T*, long long, Dims, int, int, T, T, const T*, const T*,        \
+                                const T*, const T*, int, cudaStream_t);                          \
   template void launch_wetdep<T>(T*, long long, double*, int, Dims, int, int, double,            \
                                  const double*, const double*, const double*, const double*,     \
                                  const double*, int, cudaStream_t);                              \
