@@ -260,7 +260,7 @@ int f3d_diffz(double* c, const int* nx, const int* ny, const int* nz, const int*
   const double* drk = m.arr(rkver, (size_t)d.cells(), false);
   const double* drho = m.arr(rho, (size_t)d.cells(), false);
   if (m.error()) return m.error();
-  launch_diffz<double>(dc, 0, d, *nz_loc, *iz_loc, ddz, *dt, drk, drho, 1, 0);
+  launch_diffz<double>(dc, 0, d, *nz_loc, *iz_loc, ddz, *dt, drk, drho, nullptr, 1, 0);
   return m.finish();
 }
 

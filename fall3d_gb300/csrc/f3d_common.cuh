@@ -45,6 +45,43 @@ __device__ __forceinline__ T minmod_div(T a, T b, T dx) {
   return T(0.5) * (sign1(a) + sign1(b)) * (fmin2(absd(a), absd(b)) / dx);
 }
 
+// The limiter 0.5*(SIGN(1,dr)+SIGN(1,dl))*MIN(|dr|,|dl|) (advctzc.f90:44).
+template <class T>
+__device__ __forceinline__ T minmod_ref(T dr, T dl) {
+  return T(0.5) * (sign1(dr) + sign1(dl)) * fmin2(absd(dr), absd(dl));
+}
+
+// binary64 forms of both limiters on the bit patterns.  GB300 issues
+// binary64 arithmetic at 1/64 of the binary32 rate while integer operations
+// run at full rate, so the sign and minimum logic moves to integers.  For
+// finite operands (the others take the formula):
+//  * 0.5*(s_r + s_l) is +-1 when the sign bits agree (SIGN(1,-0) = -1), and
+//    +0 when they differ, where +0 * (a finite m >= 0) = +0;
+//  * |x| of finite binary64 values orders like the integers of their bit
+//    patterns with the sign cleared, and MIN keeps the first operand on
+//    ties, which has the same bits as the second;
+//  * (+-1) * m is m with the sign bit of the first operand.
+// The results are the formula's bits.
+__device__ __forceinline__ double minmod_ref(double dr, double dl) {
+  const long long br = __double_as_longlong(dr), bl = __double_as_longlong(dl);
+  const long long mr = br & 0x7fffffffffffffffLL, ml = bl & 0x7fffffffffffffffLL;
+  if (mr >= 0x7ff0000000000000LL || ml >= 0x7ff0000000000000LL)
+    return 0.5 * (sign1(dr) + sign1(dl)) * fmin2(fabs(dr), fabs(dl));
+  if ((br ^ bl) < 0) return 0.0;
+  return __longlong_as_double((ml < mr ? ml : mr) | (br & (long long)0x8000000000000000ULL));
+}
+__device__ __forceinline__ double minmod_div(double a, double b, double dx) {
+  const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
+  const long long ma = ba & 0x7fffffffffffffffLL, mb = bb & 0x7fffffffffffffffLL;
+  if (!(dx > 0.0) || ma >= 0x7ff0000000000000LL || mb >= 0x7ff0000000000000LL) {
+    const double dr = a / dx, dl = b / dx;
+    return 0.5 * (sign1(dr) + sign1(dl)) * fmin2(fabs(dr), fabs(dl));
+  }
+  const double q = __longlong_as_double(mb < ma ? mb : ma) / dx;  // >= 0, +inf on overflow
+  if ((ba ^ bb) < 0) return isinf(q) ? 0.0 * q : 0.0;             // 0 * q
+  return __longlong_as_double(__double_as_longlong(q) | (ba & (long long)0x8000000000000000ULL));
+}
+
 // Grid geometry of one scenario (interior nx, ny, nz; halo arrays are
 // (nx+2)(ny+2)(nz+2), x fastest).
 struct Dims {

@@ -113,7 +113,7 @@ long long footprint_bytes(const f3d_grid* g) {
     b += 4LL * (11 * s3 + s3 * nc + pl * nc + nz + 1) + 8LL * pl + nc;
   } else {
     b += 8LL * halo * nc;
-    b += 8LL * 3 * s3;  // 1/rho, rkh1*rho, rkhor*rho
+    b += 8LL * 4 * s3;  // 1/rho, rkh1*rho, rkhor*rho, diffz face coefficients
   }
   b += (long long)f3d::reduce_scratch_bytes(2LL * nc * (nx + ny) * nz + nc * pl, 4);
   b += (long long)f3d::setvset_scratch_bytes(Dims{g->nx, g->ny, g->nz}, g->np);
@@ -190,6 +190,7 @@ struct Fields<double> {
   static const double* lrho(f3d_ctx* x) { return x->lrho64; }
   static const double* pkx(f3d_ctx* x) { return x->pkx64; }
   static const double* pky(f3d_ctx* x) { return x->pky64; }
+  static const double* rksz(f3d_ctx* x) { return x->rksz64; }
 };
 template <>
 struct Fields<float> {
@@ -208,6 +209,7 @@ struct Fields<float> {
   static const float* lrho(f3d_ctx*) { return nullptr; }
   static const float* pkx(f3d_ctx*) { return nullptr; }
   static const float* pky(f3d_ctx*) { return nullptr; }
+  static const float* rksz(f3d_ctx*) { return nullptr; }
 };
 
 // Sources/sizloop.f90:31-83 for all classes, class-batched sweeps.
@@ -256,7 +258,7 @@ void sizloop(f3d_ctx* x) {
   }
   {
     ProfScope ps(x, "diffz");
-    launch_diffz<T>(c, hb, d, nz, 1, F::dz(x), dt, F::rkver(x), F::rho(x), nc, s);
+    launch_diffz<T>(c, hb, d, nz, 1, F::dz(x), dt, F::rkver(x), F::rho(x), F::rksz(x), nc, s);
   }
   if (x->iiter % 2 == 0) {
     difx();
@@ -458,6 +460,7 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
     A(lrho64, s3);
     A(pkx64, s3);
     A(pky64, s3);
+    A(rksz64, s3);
   }
   if (x->prec == F3D_PREC_FP32) {
     A(c32, hb * nc);
@@ -599,7 +602,7 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
   launch_finddt(d, g.nc, g.dX1, g.dX2, x->dz, x->vx, x->vy, x->vz, x->vset, x->rkh1, x->rkhor,
                 x->rkver, small_dtcn(x), s);
   if (x->prec == F3D_PREC_FP64)
-    launch_diff_coeffs((long long)s3, x->rho, x->rkh1, x->rkhor, x->lrho64, x->pkx64, x->pky64, s);
+    launch_diff_coeffs(d, x->rho, x->rkh1, x->rkhor, x->rkver, x->lrho64, x->pkx64, x->pky64, x->rksz64, s);
   if (x->prec == F3D_PREC_FP32) {
     launch_d2f(x->vx32, x->vx, (long long)s3, s);
     launch_d2f(x->vy32, x->vy, (long long)s3, s);

@@ -53,9 +53,10 @@ struct f3d_ctx {
   // per-column wet rate, per-class wet-deposition switch
   float* c32b = nullptr;
   float *lrho32 = nullptr, *pkx32 = nullptr, *pky32 = nullptr, *pkz32 = nullptr;
-  // plain form: 1/rho, rkh1*rho, rkhor*rho of the current meteo update (the
-  // class-independent factors of diffx/diffy)
-  double *lrho64 = nullptr, *pkx64 = nullptr, *pky64 = nullptr;
+  // plain form: 1/rho, rkh1*rho, rkhor*rho and the diffz face coefficients
+  // of the current meteo update (the class-independent factors of the
+  // diffusion sweeps)
+  double *lrho64 = nullptr, *pkx64 = nullptr, *pky64 = nullptr, *rksz64 = nullptr;
   float* vk32 = nullptr;  // vz + vset per class
   // the fused met fields in the halo layout of c (two-columns-per-lane kernel)
   float *vxh = nullptr, *vyh = nullptr, *lrhoh = nullptr, *pkxh = nullptr, *pkyh = nullptr,

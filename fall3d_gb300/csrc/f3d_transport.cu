@@ -132,9 +132,7 @@ __device__ __forceinline__ void adv_z_work(T cm, T c0, T cp, T vk, T vk_1, const
                                            T& w1, T& w2) {
   const T vk_12 = T(0.5) * (vk + vk_1);
   w1 = dt * (vk * c0 - vk_1 * cm) * z.dzz;
-  const T deltar = (cp - c0) * z.dzk;
-  const T deltal = (c0 - cm) * z.dzk_1;
-  const T sigma = T(0.5) * (sign1(deltar) + sign1(deltal)) * fmin2(absd(deltar), absd(deltal));
+  const T sigma = minmod_ref((cp - c0) * z.dzk, (c0 - cm) * z.dzk_1);
   const T Crk = absd(vk_12) * dt * z.dzk_1;
   w2 = dt * T(0.5) * z.dzm1 * (T(1) - Crk) * sigma * absd(vk_12) * z.dzz;
 }
@@ -355,7 +353,7 @@ void launch_advcty(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, cons
 // expression in both, so it is computed once and carried.
 template <class T>
 __global__ void k_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* dz, T dt,
-                        const T* rkver, const T* rho) {
+                        const T* rkver, const T* rho, const T* rksz) {
   extern __shared__ unsigned char smem_raw[];
   T* l_dz = reinterpret_cast<T*>(smem_raw);  // 0..nz
   T* l_dzdz = l_dz + (d.nz + 1);             // 1..nz
@@ -377,8 +375,9 @@ __global__ void k_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc,
   const int kb = iz_loc, ke = iz_loc + nz_loc - 1;
   // Interior face flux between k and k+1 (diffz.f90:42-45):
   //   0.5*(rho(k+1)K(k+1) + rho(k)K(k)) * (c(k+1)/rho(k+1) - c(k)/rho(k)) * l_dz(k)
+  // rksz, when given, holds that face's 0.5*(...) for the meteo update
   auto face = [&](int k, T qk, T qk1, T rk, T rk1, T Kk, T Kk1) {
-    const T rks = T(0.5) * (rk1 * Kk1 + rk * Kk);
+    const T rks = rksz ? rksz[mb + (k - 1) * ms] : T(0.5) * (rk1 * Kk1 + rk * Kk);
     return rks * (qk1 - qk) * l_dz[k];
   };
   // Window of originals: c(k-1), c(k), c(k+1); rho, K at k-1, k, k+1.
@@ -425,12 +424,13 @@ __global__ void k_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc,
 
 template <class T>
 void launch_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* dz, T dt,
-                  const T* rkver, const T* rho, int ncls, cudaStream_t s) {
+                  const T* rkver, const T* rho, const T* rksz, int ncls, cudaStream_t s) {
   const int bs = 128;
   const long long cols = (long long)d.nx * d.ny;
   const size_t sm = 2 * sizeof(T) * (d.nz + 1);
   k_diffz<T><<<dim3((unsigned)((cols + bs - 1) / bs), ncls), bs, sm, s>>>(c, cstride, d, nz_loc,
-                                                                         iz_loc, dz, dt, rkver, rho);
+                                                                         iz_loc, dz, dt, rkver, rho,
+                                                                         rksz);
   count_launch();
 }
 
@@ -554,21 +554,27 @@ void launch_diffy(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dy,
 
 // The class-independent factors of diffx/diffy for one meteo update, with
 // the sweeps' own operations (so the sweeps read the same bits).
-__global__ void k_diff_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,
-                              double* lr, double* pkx, double* pky) {
+// rksz(i,j,k) = 0.5*(rho(k+1)*rkver(k+1) + rho(k)*rkver(k)), the face
+// (k, k+1) coefficient of diffz.f90:43 for k < nz.
+__global__ void k_diff_coeffs(Dims d, const double* rho, const double* rkh1, const double* rkhor,
+                              const double* rkver, double* lr, double* pkx, double* pky,
+                              double* rksz) {
+  const long long n = d.cells(), pl = d.plane(), top = n - pl;
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
        m += (long long)gridDim.x * blockDim.x) {
     const double r = rho[m];
     lr[m] = 1.0 / r;
     pkx[m] = rkh1[m] * r;
     pky[m] = rkhor[m] * r;
+    rksz[m] = m < top ? 0.5 * (rho[m + pl] * rkver[m + pl] + r * rkver[m]) : 0.0;
   }
 }
 
-void launch_diff_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,
-                        double* lr, double* pkx, double* pky, cudaStream_t s) {
-  const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
-  k_diff_coeffs<<<nb, 256, 0, s>>>(n, rho, rkh1, rkhor, lr, pkx, pky);
+void launch_diff_coeffs(Dims d, const double* rho, const double* rkh1, const double* rkhor,
+                        const double* rkver, double* lr, double* pkx, double* pky, double* rksz,
+                        cudaStream_t s) {
+  const int nb = (int)std::min<long long>((d.cells() + 255) / 256, 152LL * 16);
+  k_diff_coeffs<<<nb, 256, 0, s>>>(d, rho, rkh1, rkhor, rkver, lr, pkx, pky, rksz);
   count_launch();
 }
 
@@ -776,6 +782,7 @@ void launch_f2d(double* dst, const float* src, long long n, cudaStream_t s) {
   template void launch_advcty<T>(T*, long long, Dims, int, int, const T*, T, T, int,             \
                                  cudaStream_t);                                                  \
   template void launch_diffz<T>(T*, long long, Dims, int, int, const T*, T, const T*, const T*,  \
+                                const T*,                                                        \
                                 int, cudaStream_t);                                              \
   template void launch_diffx<T>(T*, long long, Dims, int, int, T, T, const T*, const T*,        \
                                 const T*, const T*, int, cudaStream_t);                          \
