@@ -314,10 +314,13 @@ __global__ void k_advcty(T* c, long long cstride, Dims d, int iz_loc, const T* v
 }
 
 static int pick_ti(int nline, size_t elem, int arrays) {
-  // Widest tile whose staging fits in 96 KB.
+  // Widest tile whose staging fits in 96 KB (at least 4 lines when they
+  // fit in the 227 KB a block may have).
   for (int ti = 32; ti >= 4; ti >>= 1)
     if ((size_t)arrays * (nline + 2) * ti * elem <= 96 * 1024) return ti;
-  return 4;
+  for (int ti = 4; ti > 1; ti >>= 1)
+    if ((size_t)arrays * (nline + 2) * ti * elem <= 227 * 1024) return ti;
+  return 1;
 }
 
 static void set_smem(const void* fn, size_t bytes) {
@@ -435,31 +438,73 @@ void launch_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const
 }
 
 // ------------------------------------------------------- diffx / diffy
-// Sources/diffx.f90:20-55, Sources/diffy.f90:20-55.  lr(q) = 1/rho(q) and
-// pk(q) = rkh(q)*rho(q) are staged with the line.
+// Sources/diffx.f90:20-55, Sources/diffy.f90:20-55.  A line is staged with
+// what its cells share: c (0..n+1), cl = c*(1/rho) (1..n) and the averaged
+// face coefficient fk(q) = 0.5*(pk(q+1)+pk(q)) (1..n-1), pk = rkh*rho, each
+// formed once with the reference's operations, so every cell reads the bits
+// it would have computed itself.  The end cells (non-averaged faces, ghost
+// products) fetch their own factors.
+
+// 1/rho and rkh*rho of one position: precomputed (lrp, pkp) or formed here.
 template <class T>
-__device__ __forceinline__ T diff_line_cell(int q, int n, const T* cl, const T* lr, const T* pk,
-                                            int st, T dtdx2) {
+__device__ __forceinline__ void diff_factors(const T* lrp, const T* pkp, const T* rho, const T* rkh,
+                                             long long m, T& l, T& p) {
+  if (lrp) {
+    l = lrp[m];
+    p = pkp[m];
+  } else {
+    const T r = rho[m];
+    l = T(1) / r;
+    p = rkh[m] * r;
+  }
+}
+
+template <class T>
+struct DiffSrc {  // the line's factors in global memory: position q at m1 + (q-1)*ms
+  const T *lrp, *pkp, *rho, *rkh;
+  long long m1, ms;
+  __device__ void at(int q, T& l, T& p) const { diff_factors(lrp, pkp, rho, rkh, m1 + (q - 1) * ms, l, p); }
+};
+
+template <class T>
+__device__ __forceinline__ T diff_line_cell(int q, int n, const T* cv, const T* cl, const T* fk,
+                                            const DiffSrc<T>& src, int st, T dtdx2) {
   // st: stride between consecutive line positions in the staged arrays
-  auto Cq = [&](int a) { return cl[a * st]; };
-  auto Lq = [&](int a) { return lr[a * st]; };
-  auto Pq = [&](int a) { return pk[a * st]; };
+  auto Cq = [&](int a) { return cv[a * st]; };
+  auto Q = [&](int a) { return cl[a * st]; };
   T gradr, gradl;
   if (q == 1) {
-    gradr = Pq(2) * (Cq(2) * Lq(2) - Cq(1) * Lq(1));
-    gradl = Pq(1) * (Cq(1) * Lq(1) - Cq(0) * Lq(1));
+    T l1, p1, l2, p2;
+    src.at(1, l1, p1);
+    src.at(2, l2, p2);
+    gradr = p2 * (Q(2) - Q(1));
+    gradl = p1 * (Q(1) - Cq(0) * l1);
     gradl = fmax2(T(0), gradl);
   } else if (q == n) {
-    gradr = Pq(n) * (Cq(n + 1) * Lq(n) - Cq(n) * Lq(n));
-    gradl = Pq(n - 1) * (Cq(n) * Lq(n) - Cq(n - 1) * Lq(n - 1));
+    T ln, pn, lm, pm;
+    src.at(n, ln, pn);
+    src.at(n - 1, lm, pm);
+    gradr = pn * (Cq(n + 1) * ln - Q(n));
+    gradl = pm * (Q(n) - Q(n - 1));
     gradr = fmin2(T(0), gradr);
   } else {
-    const T rksr = T(0.5) * (Pq(q + 1) + Pq(q));
-    const T rksl = T(0.5) * (Pq(q) + Pq(q - 1));
-    gradr = rksr * (Cq(q + 1) * Lq(q + 1) - Cq(q) * Lq(q));
-    gradl = rksl * (Cq(q) * Lq(q) - Cq(q - 1) * Lq(q - 1));
+    gradr = fk[q * st] * (Q(q + 1) - Q(q));
+    gradl = fk[(q - 1) * st] * (Q(q) - Q(q - 1));
   }
   return Cq(q) + dtdx2 * (gradr - gradl);
+}
+
+// Stages position q (1..n) of a line: cl(q) and, below n, fk(q).
+template <class T>
+__device__ __forceinline__ void diff_stage(int q, int n, T v, const DiffSrc<T>& src, T* clq, T* fkq) {
+  T l, p;
+  src.at(q, l, p);
+  *clq = v * l;
+  if (q < n) {
+    T l1, p1;
+    src.at(q + 1, l1, p1);
+    *fkq = T(0.5) * (p1 + p);
+  }
 }
 
 template <class T>
@@ -467,29 +512,21 @@ __global__ void k_diffx(T* c, long long cstride, Dims d, int iz_loc, T dx, T dt,
                         const T* rho, const T* lrp, const T* pkp) {
   extern __shared__ unsigned char smem_raw[];
   const int nx = d.nx, ny = d.ny;
-  T* cl = reinterpret_cast<T*>(smem_raw);
-  T* lr = cl + (nx + 2);
-  T* pk = lr + (nx + 2);
+  T* cv = reinterpret_cast<T*>(smem_raw);
+  T* cl = cv + (nx + 2);
+  T* fk = cl + (nx + 2);
   const int j = blockIdx.x % ny + 1, k = blockIdx.x / ny + iz_loc;
   T* cc = c + (long long)blockIdx.y * cstride + d.C(0, j, k);
-  const long long mb = d.M(1, j, k) - 1;
+  const DiffSrc<T> src{lrp, pkp, rho, rkh, d.M(1, j, k), 1};
   for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) {
-    cl[q] = cc[q];
-    if (q >= 1 && q <= nx) {
-      if (lrp) {
-        lr[q] = lrp[mb + q];
-        pk[q] = pkp[mb + q];
-      } else {
-        const T r = rho[mb + q];
-        lr[q] = T(1) / r;
-        pk[q] = rkh[mb + q] * r;
-      }
-    }
+    const T v = cc[q];
+    cv[q] = v;
+    if (q >= 1 && q <= nx) diff_stage(q, nx, v, src, cl + q, fk + q);
   }
   __syncthreads();
   const T dtdx2 = dt / (dx * dx);
   for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x)
-    cc[q] = diff_line_cell(q, nx, cl, lr, pk, 1, dtdx2);
+    cc[q] = diff_line_cell(q, nx, cv, cl, fk, src, 1, dtdx2);
 }
 
 template <class T>
@@ -497,9 +534,9 @@ __global__ void k_diffy(T* c, long long cstride, Dims d, int iz_loc, T dy, T dt,
                         const T* rho, const T* lrp, const T* pkp) {
   extern __shared__ unsigned char smem_raw[];
   const int nx = d.nx, ny = d.ny, TI = blockDim.x;
-  T* cl = reinterpret_cast<T*>(smem_raw);
-  T* lr = cl + (ny + 2) * TI;
-  T* pk = lr + (ny + 2) * TI;
+  T* cv = reinterpret_cast<T*>(smem_raw);  // [q][TI]
+  T* cl = cv + (ny + 2) * TI;
+  T* fk = cl + (ny + 2) * TI;
   const int ntile = (nx + TI - 1) / TI;
   const int i0 = (blockIdx.x % ntile) * TI + 1, k = blockIdx.x / ntile + iz_loc;
   const int tx = threadIdx.x, ty = threadIdx.y, TJ = blockDim.y;
@@ -508,25 +545,17 @@ __global__ void k_diffy(T* c, long long cstride, Dims d, int iz_loc, T dy, T dt,
   T* cc = c + (long long)blockIdx.y * cstride;
   const long long rowstride = nx + 2;
   const long long base = d.C(act ? i : nx, 0, k);
-  const long long vb = d.M(act ? i : nx, 1, k) - nx;
+  const DiffSrc<T> src{lrp, pkp, rho, rkh, d.M(act ? i : nx, 1, k), nx};
   for (int q = ty; q <= ny + 1; q += TJ) {
-    cl[q * TI + tx] = act ? cc[base + q * rowstride] : T(0);
-    if (q >= 1 && q <= ny) {
-      if (lrp) {
-        lr[q * TI + tx] = act ? lrp[vb + (long long)q * nx] : T(1);
-        pk[q * TI + tx] = act ? pkp[vb + (long long)q * nx] : T(0);
-      } else {
-        const T r = act ? rho[vb + (long long)q * nx] : T(1);
-        lr[q * TI + tx] = T(1) / r;
-        pk[q * TI + tx] = act ? rkh[vb + (long long)q * nx] * r : T(0);
-      }
-    }
+    const T v = act ? cc[base + q * rowstride] : T(0);
+    cv[q * TI + tx] = v;
+    if (act && q >= 1 && q <= ny) diff_stage(q, ny, v, src, cl + q * TI + tx, fk + q * TI + tx);
   }
   __syncthreads();
   if (!act) return;
   const T dtdy2 = dt / (dy * dy);
   for (int q = ty + 1; q <= ny; q += TJ)
-    cc[base + q * rowstride] = diff_line_cell(q, ny, cl + tx, lr + tx, pk + tx, TI, dtdy2);
+    cc[base + q * rowstride] = diff_line_cell(q, ny, cv + tx, cl + tx, fk + tx, src, TI, dtdy2);
 }
 
 template <class T>
