@@ -331,6 +331,8 @@ struct ClassConst {
   double num;       // 4*gi*diam*rhop, the numerator of setvset.f90:104
   double rk1, rk2;  // Ganser shape factors (setvset.f90:127-128)
   double rk12;      // rk1 * rk2
+  double sqnum;    // sqrt(num)
+  double drk12;     // diam * rk1 * rk2
   double cd100;     // Wilson
   int ok;           // get_gama converged
 };
@@ -368,7 +370,7 @@ __global__ void k_class_consts(int np, int modv, const double* diam, const doubl
   k.rhop = rhop[ic];
   k.psi = psi[ic];
   k.num = 4.0 * gi * k.diam * k.rhop;
-  k.rk1 = k.rk2 = k.rk12 = k.cd100 = 0.0;
+  k.rk1 = k.rk2 = k.rk12 = k.sqnum = k.drk12 = k.cd100 = 0.0;
   k.ok = 1;
   if (modv == 2) {
     double gama;
@@ -378,6 +380,8 @@ __global__ void k_class_consts(int np, int modv, const double* diam, const doubl
     k.rk1 = 1.0 / (dnd / 3.0 + 2.0 / (3.0 * sqrt(k.psi)));
     k.rk2 = pow(10.0, 1.8148 * pow(-log10(k.psi), 0.5743));
     k.rk12 = k.rk1 * k.rk2;
+    k.sqnum = sqrt(k.num);
+    k.drk12 = k.diam * k.rk12;
   } else if (modv == 3) {
     k.cd100 = 0.24 * pow(k.psi, -0.828) + 2.0 * sqrt(1.0 - k.psi);
   }
@@ -388,16 +392,19 @@ __global__ void k_class_consts(int np, int modv, const double* diam, const doubl
 // closed-form Dellino model) or -1 when maxit is reached.
 //
 // Ganser (setvset.f90:117-136): with R = rey*rk1*rk2 = G*v,
-// G = rhoa*diam*rk1*rk2/visc, and v = T/sqrt(cd), T = sqrt(4*gi*diam*rhop/(3*rhoa)),
+// G = (rhoa/visc)*(diam*rk1*rk2), and v = T/sqrt(cd),
+// T = sqrt(4*gi*diam*rhop)*sqrt(1/(3*rhoa)),
 //   cd = 24/(rey*rk1)*(1 + 0.1118*R^0.6567) + 0.4305*rk2/(1 + 3305/R)
 //      = rk2*((24*(R + 3305) + 0.4305*R^2)/(R*(R + 3305)) + 24*0.1118*R^(0.6567-1)).
-__device__ int vsettl_dev(const ClassConst& k, int model, double rhoa, double visc, double& cd,
-                          double& vset, const DMathTab& tab) {
+// The cell factors sqrt(1/(3*rhoa)) and rhoa/visc come from k_visc
+// (shared by all classes): cf.x, cf.y.
+__device__ int vsettl_dev(const ClassConst& k, int model, double rhoa, double visc, double2 cf,
+                          double& cd, double& vset, const DMathTab& tab) {
   const double eps = 1e-3;
   double vold = 1e5, v = 0.0;
   if (model == 2) {
-    const double T = sqrt(k.num / (3.0 * rhoa));
-    const double G = rhoa * k.diam * k.rk12 / visc;
+    const double T = k.sqnum * cf.x;
+    const double G = cf.y * k.drk12;
     for (int it = 1; it <= 100; ++it) {
       v = T * rsqrt(cd);
       const double R = G * v;
@@ -477,16 +484,20 @@ __device__ __forceinline__ double sutherland(double T) {
   return visc0 * ((Tair0 + 120.0) / (T + 120.0)) * pow(T / Tair0, 1.5);
 }
 
-// The air viscosity of every cell, shared by all classes (setvset.f90:95-97).
-__global__ void k_visc(long long s3, const double* tempe, double* visc) {
+// The air viscosity of every cell, shared by all classes (setvset.f90:95-97),
+// and the Ganser iteration's cell factors sqrt(1/(3*rho)), rho/visc.
+__global__ void k_visc(long long s3, const double* tempe, const double* rho, double* visc, double2* cf) {
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < s3;
-       m += (long long)gridDim.x * blockDim.x)
-    visc[m] = sutherland(tempe[m]);
+       m += (long long)gridDim.x * blockDim.x) {
+    const double vs = sutherland(tempe[m]), r = rho[m];
+    visc[m] = vs;
+    cf[m] = make_double2(sqrt(1.0 / (3.0 * r)), r / vs);
+  }
 }
 
 // Runs chain cells [q0, q1) from cd; writes outputs when `write`.
 __device__ void chain_run(const ChainGeom& g, long long q0, long long q1, int modv,
-                          const ClassConst* cc, const double* viscs, const double* rho,
+                          const ClassConst* cc, const double* viscs, const double2* cf, const double* rho,
                           double* vset, int* iters, double& cd, bool write, int& nonconv,
                           const DMathTab& tab) {
   const long long s3 = g.d.cells();
@@ -496,7 +507,7 @@ __device__ void chain_run(const ChainGeom& g, long long q0, long long q1, int mo
     chain_cell(g, q, ic, m);
     const double visc = viscs[m];
     double v;
-    const int it = vsettl_dev(cc[ic], modv, rho[m], visc, cd, v, tab);
+    const int it = vsettl_dev(cc[ic], modv, rho[m], visc, cf[m], cd, v, tab);
     if (write) {
       vset[(long long)ic * s3 + m] = v;
       if (iters) iters[(long long)ic * s3 + m] = it;
@@ -506,7 +517,7 @@ __device__ void chain_run(const ChainGeom& g, long long q0, long long q1, int mo
 }
 
 __global__ void k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, const double* visc,
-                                 const double* rho, double* vset, int* iters,
+                                 const double2* cf, const double* rho, double* vset, int* iters,
                                  const double* cd_state, double* entry, double* exitv,
                                  int* nonconv) {
   __shared__ DMathTab tab;
@@ -521,10 +532,10 @@ __global__ void k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, co
     cd = *cd_state;
   } else {
     cd = 1.0;
-    chain_run(g, max(0LL, q0 - g.W), q0, modv, cc, visc, rho, vset, iters, cd, false, dummy, tab);
+    chain_run(g, max(0LL, q0 - g.W), q0, modv, cc, visc, cf, rho, vset, iters, cd, false, dummy, tab);
   }
   entry[s] = cd;
-  chain_run(g, q0, q1, modv, cc, visc, rho, vset, iters, cd, true, nc_flag, tab);
+  chain_run(g, q0, q1, modv, cc, visc, cf, rho, vset, iters, cd, true, nc_flag, tab);
   exitv[s] = cd;
   nonconv[s] = nc_flag;
 }
@@ -544,7 +555,7 @@ __global__ void k_chain_check(ChainGeom g, const double* entry, const double* ex
 // stay; a recomputed segment may change its exit, so its successor is
 // re-checked until the chain agrees again.  cap overflow -> full scan.
 __global__ void k_chain_fix(ChainGeom g, int modv, const ClassConst* cc, const double* visc,
-                            const double* rho, double* vset, int* iters, double* entry,
+                            const double2* cf, const double* rho, double* vset, int* iters, double* entry,
                             double* exitv, int* nonconv, int* bad, const int* nbad, int cap,
                             double* cd_state) {
   __shared__ DMathTab tab;
@@ -574,7 +585,7 @@ __global__ void k_chain_fix(ChainGeom g, int modv, const ClassConst* cc, const d
         int nc_flag = 0;
         entry[s] = cd;
         const long long q0 = s * g.S, q1 = min(g.L, q0 + g.S);
-        chain_run(g, q0, q1, modv, cc, visc, rho, vset, iters, cd, true, nc_flag, tab);
+        chain_run(g, q0, q1, modv, cc, visc, cf, rho, vset, iters, cd, true, nc_flag, tab);
         exitv[s] = cd;
         nonconv[s] = nc_flag;
         ++s;  // the successor must be re-checked
@@ -665,7 +676,8 @@ size_t setvset_scratch_bytes(Dims d, int np) {
   size_t b = sizeof(ClassConst) * (size_t)(np + 1);
   b += 2 * sizeof(double) * (size_t)g.nseg + sizeof(int) * (size_t)g.nseg;
   b += sizeof(int) * (kBadCap + 8) + 1024;
-  b += sizeof(double) * (size_t)d.cells() + 256;  // viscosity per cell
+  b += sizeof(double) * (size_t)d.cells() + 256;      // viscosity per cell
+  b += 2 * sizeof(double) * (size_t)d.cells() + 256;  // Ganser cell factors
   return b;
 }
 
@@ -687,17 +699,18 @@ void launch_setvset(Dims d, int nc, int np, int modv, const double* diam, const 
   int* nbad = reinterpret_cast<int*>(take(sizeof(int) * 8));
   int* bad = reinterpret_cast<int*>(take(sizeof(int) * kBadCap));
   double* visc = reinterpret_cast<double*>(take(sizeof(double) * (size_t)d.cells()));
+  double2* cf = reinterpret_cast<double2*>(take(2 * sizeof(double) * (size_t)d.cells()));
   cudaMemsetAsync(nbad, 0, sizeof(int), s);
   cudaMemsetAsync(status, 0, sizeof(int), s);
   if (np > 0 && g.L > 0) {
     k_class_consts<<<(np + 31) / 32, 32, 0, s>>>(np, modv, diam, rhop, psi, sphe, cc);
     k_visc<<<(int)std::min<long long>((d.cells() + 255) / 256, 152LL * 16), 256, 0, s>>>(d.cells(), tempe,
-                                                                                         visc);
+                                                                                         rho, visc, cf);
     const int bs = 64;
     k_chain_segments<<<(unsigned)((g.nseg + bs - 1) / bs), bs, 0, s>>>(
-        g, modv, cc, visc, rho, vset, iters, cd_state, entry, exitv, nonconv);
+        g, modv, cc, visc, cf, rho, vset, iters, cd_state, entry, exitv, nonconv);
     k_chain_check<<<(unsigned)((g.nseg + 255) / 256), 256, 0, s>>>(g, entry, exitv, bad, nbad, kBadCap);
-    k_chain_fix<<<1, 32, 0, s>>>(g, modv, cc, visc, rho, vset, iters, entry, exitv, nonconv, bad,
+    k_chain_fix<<<1, 32, 0, s>>>(g, modv, cc, visc, cf, rho, vset, iters, entry, exitv, nonconv, bad,
                                  nbad, kBadCap, cd_state);
     k_chain_status<<<(unsigned)((g.nseg + 255) / 256), 256, 0, s>>>(g, nonconv, status);
     count_launch(6);

@@ -39,8 +39,9 @@ __device__ __forceinline__ void dmath_tab_init(DMathTab& t) {
 }
 
 __device__ __forceinline__ double dm_log(const DMathTab& t, double x) {
-  if (!(x >= 0x1p-1000 && x <= 0x1p1000)) return log(x);
   const long long ix = __double_as_longlong(x);
+  // 2^-1000 <= x <= 2^1000 (positive, normal, finite), as one unsigned compare
+  if ((unsigned long long)(ix - 0x0170000000000000LL) > 0x7d00000000000000ULL) return log(x);
   const int k = (int)(ix >> 52) - 1023;
   const int j = (int)((ix >> 45) & 127);
   const double z = __longlong_as_double((ix & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
@@ -58,7 +59,8 @@ __device__ __forceinline__ double dm_log(const DMathTab& t, double x) {
 }
 
 __device__ __forceinline__ double dm_exp(const DMathTab& t, double a) {
-  if (!(fabs(a) <= 700.0)) return exp(a);
+  // |a| <= 700 (NaN excluded), as one integer compare on the magnitude bits
+  if ((__double_as_longlong(a) & 0x7fffffffffffffffLL) > 0x4085e00000000000LL) return exp(a);
   const double shift = 0x1.8p52;                        // rounds a*64/ln2 to an integer
   const double kd = fma(a, 0x1.71547652b82fep+6, shift);
   const long long n = __double_as_longlong(kd) - __double_as_longlong(shift);
