@@ -533,13 +533,13 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
         __syncthreads();
         const float2 qm[RPW] = {lds2(P1 - HX), q[0]};
         const float2 qp[RPW] = {q[1], lds2(P1 + 2 * HX)};
-#pragma unroll
-        for (int r = 0; r < RPW; ++r) {
-          const float2 Pm = Pmv[r], P0 = P0v[r], Pp = Ppv[r];
-          const float2 gradr = mul2(mul2(splat(0.5f), add2(Pp, P0)), sub2(qp[r], q[r]));
-          const float2 gradl = mul2(mul2(splat(0.5f), add2(P0, Pm)), sub2(q[r], qm[r]));
-          out[r] = add2(in[r], mul2(splat(a.dtdy2), sub2(gradr, gradl)));
-        }
+        // three faces: below the pair, between its rows (gradr of row 0 and
+        // gradl of row 1, the same operations on the same values), above it
+        const float2 fb = mul2(mul2(splat(0.5f), add2(P0v[0], Pmv[0])), sub2(q[0], qm[0]));
+        const float2 fm = mul2(mul2(splat(0.5f), add2(Ppv[0], P0v[0])), sub2(qp[0], q[0]));
+        const float2 ft = mul2(mul2(splat(0.5f), add2(Ppv[1], P0v[1])), sub2(qp[1], q[1]));
+        out[0] = add2(in[0], mul2(splat(a.dtdy2), sub2(fm, fb)));
+        out[1] = add2(in[1], mul2(splat(a.dtdy2), sub2(ft, fm)));
         return;
       }
 #pragma unroll

@@ -214,102 +214,106 @@ void launch_advctzc(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, con
 }
 
 // ------------------------------------------------------ advctx / advcty
-// Sources/advctx.f90:24-56 and Sources/advcty.f90:24-55 on one staged line:
-// cl[0..n+1] concentrations, vl(q) velocity at q (1..n).  Phase 1 fills
-// w1[1..n+1], w2[1..n]; phase 2 updates.
+// Sources/advctx.f90:24-56 and Sources/advcty.f90:24-55 on staged lines.
+// A block takes one line (advctx) or a tile of lines (advcty) through every
+// class: the class-independent factors of the line are formed once,
+//   a(q) = |0.5*(v(q)+v(q-1))|,  b(q) = (dt*0.5)*(1 - auxv*a(q)),
+// so that work(q,2) = dt*0.5*(1-Cri)*sigma*|v_12| is (b(q)*sigma)*a(q),
+// the reference's product left to right; then per class the line's
+// concentrations are staged, work(q,1), work(q,2) formed and the line
+// updated.
 template <class T>
-__device__ __forceinline__ void adv_line_work(const T* cl, int q, int n, T vq, T vq_1, T dx, T dt,
-                                              T auxv, T& w1, T& w2) {
-  const T vq_12 = T(0.5) * (vq + vq_1);
-  w1 = auxv * (vq * cl[q] - vq_1 * cl[q - 1]);
-  const T sigma = minmod_div(cl[q + 1] - cl[q], cl[q] - cl[q - 1], dx);
-  const T Cri = auxv * absd(vq_12);
-  w2 = dt * T(0.5) * (T(1) - Cri) * sigma * absd(vq_12);
-  (void)n;
-}
+struct AdvLine {  // a line's staged arrays at stride st
+  T *v, *a, *b, *cl, *w1, *w2;
+};
 
 template <class T>
-__device__ __forceinline__ T adv_line_update(T cq, T vq, int q, int n, const T* w1, const T* w2) {
-  if (vq > T(0)) return cq - w1[q] - (w2[q] - w2[q > 1 ? q - 1 : 1]);
-  return cq - w1[q + 1] - (w2[q < n ? q + 1 : n] - w2[q]);
+__device__ __forceinline__ void adv_line_coef(T vq, T vq_1, T auxv, T dth, T& a, T& b) {
+  a = absd(T(0.5) * (vq + vq_1));
+  b = dth * (T(1) - auxv * a);
 }
 
-// One block per x line (j,k,class); threads stride over i.
+// work(q,1), work(q,2) of position q (1..n), or work(n+1,1) (advctx.f90:46)
 template <class T>
-__global__ void k_advctx(T* c, long long cstride, Dims d, int iz_loc, const T* vx, T dx, T dt) {
-  extern __shared__ unsigned char smem_raw[];
-  const int nx = d.nx, ny = d.ny;
-  T* cl = reinterpret_cast<T*>(smem_raw);
-  T* w1 = cl + (nx + 2);
-  T* w2 = w1 + (nx + 2);
-  const int j = blockIdx.x % ny + 1, k = blockIdx.x / ny + iz_loc;
-  T* cc = c + (long long)blockIdx.y * cstride + d.C(0, j, k);
-  const T* vl = vx + d.M(1, j, k) - 1;  // vl[i] = vx(i,j,k)
-  for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) cl[q] = cc[q];
-  __syncthreads();
-  const T auxv = dt / dx;
-  for (int q = threadIdx.x + 1; q <= nx + 1; q += blockDim.x) {
-    if (q <= nx) {
-      adv_line_work(cl, q, nx, vl[q], vl[q > 1 ? q - 1 : 1], dx, dt, auxv, w1[q], w2[q]);
-    } else {
-      w1[nx + 1] = auxv * vl[nx] * (cl[nx + 1] - cl[nx]);  // advctx.f90:46
-    }
+__device__ __forceinline__ void adv_line_work(const AdvLine<T>& L, int q, int n, int st, T dx, T auxv) {
+  auto C = [&](int i) { return L.cl[i * st]; };
+  if (q > n) {
+    L.w1[(n + 1) * st] = auxv * L.v[n * st] * (C(n + 1) - C(n));
+    return;
   }
-  __syncthreads();
-  for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x)
-    cc[q] = adv_line_update(cl[q], vl[q], q, nx, w1, w2);
+  const T vq = L.v[q * st], vq_1 = L.v[(q > 1 ? q - 1 : 1) * st];
+  L.w1[q * st] = auxv * (vq * C(q) - vq_1 * C(q - 1));
+  const T sigma = minmod_div(C(q + 1) - C(q), C(q) - C(q - 1), dx);
+  L.w2[q * st] = L.b[q * st] * sigma * L.a[q * st];
 }
 
-// One block per tile of TI adjacent y lines (i0..i0+TI-1) at one k.
 template <class T>
-__global__ void k_advcty(T* c, long long cstride, Dims d, int iz_loc, const T* vy, T dy, T dt) {
+__device__ __forceinline__ T adv_line_update(const AdvLine<T>& L, int q, int n, int st) {
+  const T cq = L.cl[q * st], vq = L.v[q * st];
+  if (vq > T(0)) return cq - L.w1[q * st] - (L.w2[q * st] - L.w2[(q > 1 ? q - 1 : 1) * st]);
+  return cq - L.w1[(q + 1) * st] - (L.w2[(q < n ? q + 1 : n) * st] - L.w2[q * st]);
+}
+
+// One block per x line (j,k) through classes 0..ncls-1; threads stride over i.
+template <class T>
+__global__ void k_advctx(T* c, long long cstride, int ncls, Dims d, int iz_loc, const T* vx, T dx, T dt) {
+  extern __shared__ unsigned char smem_raw[];
+  const int nx = d.nx, ny = d.ny, n2 = nx + 2;
+  T* base = reinterpret_cast<T*>(smem_raw);
+  const AdvLine<T> L{base, base + n2, base + 2 * n2, base + 3 * n2, base + 4 * n2, base + 5 * n2};
+  const int j = blockIdx.x % ny + 1, k = blockIdx.x / ny + iz_loc;
+  const T* vl = vx + d.M(1, j, k) - 1;  // vl[i] = vx(i,j,k)
+  const T auxv = dt / dx, dth = dt * T(0.5);
+  for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x) {
+    const T vq = vl[q];
+    L.v[q] = vq;
+    adv_line_coef(vq, vl[q > 1 ? q - 1 : 1], auxv, dth, L.a[q], L.b[q]);
+  }
+  for (int ic = 0; ic < ncls; ++ic) {
+    T* cc = c + (long long)ic * cstride + d.C(0, j, k);
+    __syncthreads();  // the coefficients are staged; the previous class is done with cl, w1, w2
+    for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) L.cl[q] = cc[q];
+    __syncthreads();
+    for (int q = threadIdx.x + 1; q <= nx + 1; q += blockDim.x) adv_line_work(L, q, nx, 1, dx, auxv);
+    __syncthreads();
+    for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x) cc[q] = adv_line_update(L, q, nx, 1);
+  }
+}
+
+// One block per tile of TI adjacent y lines (i0..i0+TI-1) at one k, through
+// classes 0..ncls-1.
+template <class T>
+__global__ void k_advcty(T* c, long long cstride, int ncls, Dims d, int iz_loc, const T* vy, T dy, T dt) {
   extern __shared__ unsigned char smem_raw[];
   const int nx = d.nx, ny = d.ny, TI = blockDim.x;
-  T* cl = reinterpret_cast<T*>(smem_raw);  // [q][TI]
-  T* w1 = cl + (ny + 2) * TI;
-  T* w2 = w1 + (ny + 2) * TI;
   const int ntile = (nx + TI - 1) / TI;
   const int i0 = (blockIdx.x % ntile) * TI + 1, k = blockIdx.x / ntile + iz_loc;
   const int tx = threadIdx.x, ty = threadIdx.y, TJ = blockDim.y;
   const int i = i0 + tx;
   const bool act = i <= nx;
-  T* cc = c + (long long)blockIdx.y * cstride;
+  const size_t n2 = (size_t)(ny + 2) * TI;
+  T* base = reinterpret_cast<T*>(smem_raw) + tx;  // [q][TI], this thread's line
+  const AdvLine<T> L{base, base + n2, base + 2 * n2, base + 3 * n2, base + 4 * n2, base + 5 * n2};
   const long long rowstride = nx + 2;
-  const long long base = d.C(act ? i : nx, 0, k);
-  for (int q = ty; q <= ny + 1; q += TJ) cl[q * TI + tx] = act ? cc[base + q * rowstride] : T(0);
-  __syncthreads();
-  const T auxv = dt / dy;
+  const long long cbase = d.C(act ? i : nx, 0, k);
   const long long vb = d.M(act ? i : nx, 1, k) - nx;  // vb + q*nx = vy(i,q,k)
-  if (act) {
-    // w arrays strided by TI: view line tx through a pointer offset.
-    for (int q = ty + 1; q <= ny + 1; q += TJ) {
-      if (q <= ny) {
-        const T vq = vy[vb + (long long)q * nx];
-        const T vq_1 = vy[vb + (long long)(q > 1 ? q - 1 : 1) * nx];
-        const T vq_12 = T(0.5) * (vq + vq_1);
-        const T cq = cl[q * TI + tx], cm = cl[(q - 1) * TI + tx], cp = cl[(q + 1) * TI + tx];
-        w1[q * TI + tx] = auxv * (vq * cq - vq_1 * cm);
-        const T sigma = minmod_div(cp - cq, cq - cm, dy);
-        const T Crj = auxv * absd(vq_12);
-        w2[q * TI + tx] = dt * T(0.5) * (T(1) - Crj) * sigma * absd(vq_12);
-      } else {
-        const T vn = vy[vb + (long long)ny * nx];
-        w1[(ny + 1) * TI + tx] = auxv * vn * (cl[(ny + 1) * TI + tx] - cl[ny * TI + tx]);  // advcty.f90:45
-      }
-    }
-  }
-  __syncthreads();
-  if (act) {
+  const T auxv = dt / dy, dth = dt * T(0.5);
+  if (act)
     for (int q = ty + 1; q <= ny; q += TJ) {
       const T vq = vy[vb + (long long)q * nx];
-      const T cq = cl[q * TI + tx];
-      T cn;
-      if (vq > T(0))
-        cn = cq - w1[q * TI + tx] - (w2[q * TI + tx] - w2[(q > 1 ? q - 1 : 1) * TI + tx]);
-      else
-        cn = cq - w1[(q + 1) * TI + tx] - (w2[(q < ny ? q + 1 : ny) * TI + tx] - w2[q * TI + tx]);
-      cc[base + q * rowstride] = cn;
+      L.v[q * TI] = vq;
+      adv_line_coef(vq, vy[vb + (long long)(q > 1 ? q - 1 : 1) * nx], auxv, dth, L.a[q * TI], L.b[q * TI]);
     }
+  for (int ic = 0; ic < ncls; ++ic) {
+    T* cc = c + (long long)ic * cstride;
+    __syncthreads();
+    for (int q = ty; q <= ny + 1; q += TJ) L.cl[q * TI] = act ? cc[cbase + q * rowstride] : T(0);
+    __syncthreads();
+    if (act)
+      for (int q = ty + 1; q <= ny + 1; q += TJ) adv_line_work(L, q, ny, TI, dy, auxv);
+    __syncthreads();
+    if (act)
+      for (int q = ty + 1; q <= ny; q += TJ) cc[cbase + q * rowstride] = adv_line_update(L, q, ny, TI);
   }
 }
 
@@ -330,22 +334,22 @@ static void set_smem(const void* fn, size_t bytes) {
 template <class T>
 void launch_advctx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vx, T dx,
                    T dt, int ncls, cudaStream_t s) {
-  const size_t sm = 3 * (size_t)(d.nx + 2) * sizeof(T);
+  const size_t sm = 6 * (size_t)(d.nx + 2) * sizeof(T);
   set_smem((const void*)k_advctx<T>, sm);
   const int bs = d.nx >= 256 ? 256 : 128;
-  k_advctx<T><<<dim3(d.ny * nz_loc, ncls), bs, sm, s>>>(c, cstride, d, iz_loc, vx, dx, dt);
+  k_advctx<T><<<dim3(d.ny * nz_loc), bs, sm, s>>>(c, cstride, ncls, d, iz_loc, vx, dx, dt);
   count_launch();
 }
 
 template <class T>
 void launch_advcty(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vy, T dy,
                    T dt, int ncls, cudaStream_t s) {
-  const int TI = pick_ti(d.ny, sizeof(T), 3);
+  const int TI = pick_ti(d.ny, sizeof(T), 6);
   const int TJ = 256 / TI;
-  const size_t sm = 3 * (size_t)(d.ny + 2) * TI * sizeof(T);
+  const size_t sm = 6 * (size_t)(d.ny + 2) * TI * sizeof(T);
   set_smem((const void*)k_advcty<T>, sm);
   const int ntile = (d.nx + TI - 1) / TI;
-  k_advcty<T><<<dim3(ntile * nz_loc, ncls), dim3(TI, TJ), sm, s>>>(c, cstride, d, iz_loc, vy, dy, dt);
+  k_advcty<T><<<dim3(ntile * nz_loc), dim3(TI, TJ), sm, s>>>(c, cstride, ncls, d, iz_loc, vy, dy, dt);
   count_launch();
 }
 
