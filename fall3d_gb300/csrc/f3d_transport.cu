@@ -498,12 +498,13 @@ __device__ __forceinline__ T diff_line_cell(int q, int n, const T* cv, const T* 
   return Cq(q) + dtdx2 * (gradr - gradl);
 }
 
-// Stages position q (1..n) of a line: cl(q) and, below n, fk(q).
+// Stages the class-independent factors of position q (1..n) of a line:
+// 1/rho(q) and, below n, fk(q).
 template <class T>
-__device__ __forceinline__ void diff_stage(int q, int n, T v, const DiffSrc<T>& src, T* clq, T* fkq) {
+__device__ __forceinline__ void diff_stage(int q, int n, const DiffSrc<T>& src, T* lq, T* fkq) {
   T l, p;
   src.at(q, l, p);
-  *clq = v * l;
+  *lq = l;
   if (q < n) {
     T l1, p1;
     src.at(q + 1, l1, p1);
@@ -511,77 +512,94 @@ __device__ __forceinline__ void diff_stage(int q, int n, T v, const DiffSrc<T>& 
   }
 }
 
+// One block per x line (j,k) through classes 0..ncls-1.
 template <class T>
-__global__ void k_diffx(T* c, long long cstride, Dims d, int iz_loc, T dx, T dt, const T* rkh,
+__global__ void k_diffx(T* c, long long cstride, int ncls, Dims d, int iz_loc, T dx, T dt, const T* rkh,
                         const T* rho, const T* lrp, const T* pkp) {
   extern __shared__ unsigned char smem_raw[];
   const int nx = d.nx, ny = d.ny;
-  T* cv = reinterpret_cast<T*>(smem_raw);
+  T* lr = reinterpret_cast<T*>(smem_raw);
+  T* fk = lr + (nx + 2);
+  T* cv = fk + (nx + 2);
   T* cl = cv + (nx + 2);
-  T* fk = cl + (nx + 2);
   const int j = blockIdx.x % ny + 1, k = blockIdx.x / ny + iz_loc;
-  T* cc = c + (long long)blockIdx.y * cstride + d.C(0, j, k);
   const DiffSrc<T> src{lrp, pkp, rho, rkh, d.M(1, j, k), 1};
-  for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) {
-    const T v = cc[q];
-    cv[q] = v;
-    if (q >= 1 && q <= nx) diff_stage(q, nx, v, src, cl + q, fk + q);
-  }
-  __syncthreads();
+  for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x) diff_stage(q, nx, src, lr + q, fk + q);
   const T dtdx2 = dt / (dx * dx);
-  for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x)
-    cc[q] = diff_line_cell(q, nx, cv, cl, fk, src, 1, dtdx2);
+  for (int ic = 0; ic < ncls; ++ic) {
+    T* cc = c + (long long)ic * cstride + d.C(0, j, k);
+    __syncthreads();  // factors staged; the previous class is done with cv, cl
+    for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) {
+      const T v = cc[q];
+      cv[q] = v;
+      if (q >= 1 && q <= nx) cl[q] = v * lr[q];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x)
+      cc[q] = diff_line_cell(q, nx, cv, cl, fk, src, 1, dtdx2);
+  }
 }
 
+// One block per tile of TI adjacent y lines at one k, through classes 0..ncls-1.
 template <class T>
-__global__ void k_diffy(T* c, long long cstride, Dims d, int iz_loc, T dy, T dt, const T* rkh,
+__global__ void k_diffy(T* c, long long cstride, int ncls, Dims d, int iz_loc, T dy, T dt, const T* rkh,
                         const T* rho, const T* lrp, const T* pkp) {
   extern __shared__ unsigned char smem_raw[];
   const int nx = d.nx, ny = d.ny, TI = blockDim.x;
-  T* cv = reinterpret_cast<T*>(smem_raw);  // [q][TI]
-  T* cl = cv + (ny + 2) * TI;
-  T* fk = cl + (ny + 2) * TI;
   const int ntile = (nx + TI - 1) / TI;
   const int i0 = (blockIdx.x % ntile) * TI + 1, k = blockIdx.x / ntile + iz_loc;
   const int tx = threadIdx.x, ty = threadIdx.y, TJ = blockDim.y;
   const int i = i0 + tx;
   const bool act = i <= nx;
-  T* cc = c + (long long)blockIdx.y * cstride;
+  const size_t n2 = (size_t)(ny + 2) * TI;
+  T* lr = reinterpret_cast<T*>(smem_raw) + tx;  // [q][TI], this thread's line
+  T* fk = lr + n2;
+  T* cv = fk + n2;
+  T* cl = cv + n2;
   const long long rowstride = nx + 2;
   const long long base = d.C(act ? i : nx, 0, k);
   const DiffSrc<T> src{lrp, pkp, rho, rkh, d.M(act ? i : nx, 1, k), nx};
-  for (int q = ty; q <= ny + 1; q += TJ) {
-    const T v = act ? cc[base + q * rowstride] : T(0);
-    cv[q * TI + tx] = v;
-    if (act && q >= 1 && q <= ny) diff_stage(q, ny, v, src, cl + q * TI + tx, fk + q * TI + tx);
-  }
-  __syncthreads();
-  if (!act) return;
+  if (act)
+    for (int q = ty + 1; q <= ny; q += TJ) diff_stage(q, ny, src, lr + q * TI, fk + q * TI);
   const T dtdy2 = dt / (dy * dy);
-  for (int q = ty + 1; q <= ny; q += TJ)
-    cc[base + q * rowstride] = diff_line_cell(q, ny, cv + tx, cl + tx, fk + tx, src, TI, dtdy2);
+  for (int ic = 0; ic < ncls; ++ic) {
+    T* cc = c + (long long)ic * cstride;
+    __syncthreads();
+    if (act)
+      for (int q = ty; q <= ny + 1; q += TJ) {
+        const T v = cc[base + q * rowstride];
+        cv[q * TI] = v;
+        if (q >= 1 && q <= ny) cl[q * TI] = v * lr[q * TI];
+      }
+    __syncthreads();
+    if (act)
+      for (int q = ty + 1; q <= ny; q += TJ)
+        cc[base + q * rowstride] = diff_line_cell(q, ny, cv, cl, fk, src, TI, dtdy2);
+  }
 }
 
 template <class T>
 void launch_diffx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dx, T dt,
                   const T* rkh, const T* rho, const T* lr, const T* pk, int ncls, cudaStream_t s) {
-  const size_t sm = 3 * (size_t)(d.nx + 2) * sizeof(T);
+  const size_t sm = 4 * (size_t)(d.nx + 2) * sizeof(T);
   set_smem((const void*)k_diffx<T>, sm);
   const int bs = d.nx >= 256 ? 256 : 128;
-  k_diffx<T><<<dim3(d.ny * nz_loc, ncls), bs, sm, s>>>(c, cstride, d, iz_loc, dx, dt, rkh, rho, lr, pk);
+  k_diffx<T><<<dim3(d.ny * nz_loc), bs, sm, s>>>(c, cstride, ncls, d, iz_loc, dx, dt, rkh, rho, lr, pk);
   count_launch();
 }
 
 template <class T>
 void launch_diffy(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dy, T dt,
                   const T* rkh, const T* rho, const T* lr, const T* pk, int ncls, cudaStream_t s) {
-  const int TI = pick_ti(d.ny, sizeof(T), 3);
+  // at most ~48 KB per block, so that several blocks share an SM
+  int TI = pick_ti(d.ny, sizeof(T), 4);
+  while (TI > 4 && 4 * (size_t)(d.ny + 2) * TI * sizeof(T) > 48 * 1024) TI >>= 1;
   const int TJ = 256 / TI;
-  const size_t sm = 3 * (size_t)(d.ny + 2) * TI * sizeof(T);
+  const size_t sm = 4 * (size_t)(d.ny + 2) * TI * sizeof(T);
   set_smem((const void*)k_diffy<T>, sm);
   const int ntile = (d.nx + TI - 1) / TI;
-  k_diffy<T><<<dim3(ntile * nz_loc, ncls), dim3(TI, TJ), sm, s>>>(c, cstride, d, iz_loc, dy, dt,
-                                                                   rkh, rho, lr, pk);
+  k_diffy<T><<<dim3(ntile * nz_loc), dim3(TI, TJ), sm, s>>>(c, cstride, ncls, d, iz_loc, dy, dt,
+                                                             rkh, rho, lr, pk);
   count_launch();
 }
 
