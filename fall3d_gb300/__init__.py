@@ -315,12 +315,20 @@ def setvset(nx, ny, nz, nc, np_, modv, diam, rhop, psi, sphe, tempe, rho, aggreg
 
 
 def dmath_eval(op, x):
-    """The drag iteration's table-driven binary64 log (op 0) or exp (op 1)
-    of every value of the float64 array x (a diagnostic; returns a new
-    array)."""
-    x = np.ascontiguousarray(x, dtype=np.float64)
-    y = np.empty_like(x)
-    _check(load().f3d_dmath_eval(int(op), x.size, _addr(x), _addr(y)))
+    """Diagnostic: the drag iteration's table-driven binary64 log (op 0) or
+    exp (op 1) of every value of the float64 array x, or (op 2) the
+    quotients a/b of the pairs x = (a0, b0, a1, b1, ...) formed from the
+    reciprocal of b as the plain form's sweeps divide.  Returns a new
+    array (one value per pair for op 2)."""
+    x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    if op == 2:
+        if x.size % 2:
+            raise ValueError("op 2 takes pairs: x must have an even number of values")
+        n = x.size // 2
+    else:
+        n = x.size
+    y = np.empty(n, dtype=np.float64)
+    _check(load().f3d_dmath_eval(int(op), n, _addr(x), _addr(y)))
     return y
 
 

@@ -260,7 +260,12 @@ int f3d_diffz(double* c, const int* nx, const int* ny, const int* nz, const int*
   const double* drk = m.arr(rkver, (size_t)d.cells(), false);
   const double* drho = m.arr(rho, (size_t)d.cells(), false);
   if (m.error()) return m.error();
-  launch_diffz<double>(dc, 0, d, *nz_loc, *iz_loc, ddz, *dt, drk, drho, nullptr, 1, 0);
+  // 1/rho, so that c/rho is formed the way the context's sweep forms it
+  TmpBuf lr;
+  if (int r = lr.alloc(sizeof(double) * (size_t)d.cells())) return r;
+  launch_recip(d.cells(), drho, reinterpret_cast<double*>(lr.p), 0);
+  launch_diffz<double>(dc, 0, d, *nz_loc, *iz_loc, ddz, *dt, drk, drho, nullptr,
+                       reinterpret_cast<const double*>(lr.p), 1, 0);
   return m.finish();
 }
 
@@ -619,10 +624,10 @@ int f3d_setvset(const int* nx, const int* ny, const int* nz, const int* nc, cons
 }
 
 int f3d_dmath_eval(int op, long long n, const double* x, double* y) {
-  if ((op != 0 && op != 1) || n < 0) return set_error(F3D_ERR_ARG, "op must be 0 (log) or 1 (exp), n >= 0");
+  if (op < 0 || op > 2 || n < 0) return set_error(F3D_ERR_ARG, "op must be 0 (log), 1 (exp) or 2 (quotient), n >= 0");
   if (n > 0 && (!x || !y)) return set_error(F3D_ERR_ARG, "NULL argument");
   Marshal m;
-  const double* dx = m.arr(x, (size_t)n, false);
+  const double* dx = m.arr(x, (size_t)n * (op == 2 ? 2 : 1), false);
   double* dy = m.arr(y, (size_t)n, true);
   if (m.error()) return m.error();
   launch_dmath_eval(op, n, dx, dy, 0);

@@ -614,7 +614,7 @@ __global__ void k_dmath_eval(int op, long long n, const double* x, double* y) {
   __syncthreads();
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x)
-    y[q] = op == 0 ? dm_log(tab, x[q]) : dm_exp(tab, x[q]);
+    y[q] = op == 0 ? dm_log(tab, x[q]) : op == 1 ? dm_exp(tab, x[q]) : div_rn_recip(x[2 * q], x[2 * q + 1], 1.0 / x[2 * q + 1]);
 }
 
 void launch_dmath_eval(int op, long long n, const double* x, double* y, cudaStream_t s) {

@@ -28,6 +28,34 @@ F3D_HD T fabs_t(T x) { return x < T(0) ? -x : (x == T(0) ? T(0) : x); }
 __device__ __forceinline__ double absd(double x) { return fabs(x); }
 __device__ __forceinline__ float absd(float x) { return fabsf(x); }
 
+// RN(a/b) from y = RN(1/b) without a division (P. Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J.
+// Res. Develop. 34(1), 1990): q0 = RN(a*y) is within 1.5 ulp of a/b;
+// q1 = RN(q0 + RN(a - b*q0)*y) is within 1 ulp; and when y is within half
+// an ulp of 1/b and q1 within one ulp of a/b, the residual a - b*q1 is
+// exact and RN(q1 + (a - b*q1)*y) = RN(a/b).  A zero a gives a*y (the
+// signed zero of a/b).  Operands outside [2^-900, 2^900] in
+// magnitude (where a residual could leave the normal range), or
+// non-finite, take the IEEE division: the result is RN(a/b) for all inputs.
+// the rare paths out of line, so that they cost the callers no registers
+static __device__ __noinline__ double div_ieee(double a, double b) { return a / b; }
+static __device__ __noinline__ double minmod_div_ieee(double a, double b, double dx) {
+  const double dr = a / dx, dl = b / dx;
+  return 0.5 * (sign1(dr) + sign1(dl)) * fmin2(fabs(dr), fabs(dl));
+}
+__device__ __forceinline__ bool div_in_range(double x) {
+  const unsigned long long m = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+  return m - 0x07b0000000000000ULL <= 0x7080000000000000ULL;  // 2^-900 <= |x| <= 2^900
+}
+__device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
+  if (!div_in_range(b)) return div_ieee(a, b);  // y may be inexact, infinite or zero
+  const double q0 = a * y;
+  if ((__double_as_longlong(a) & 0x7fffffffffffffffLL) == 0) return q0;
+  if (!(div_in_range(a) && div_in_range(q0))) return div_ieee(a, b);
+  const double q1 = fma(fma(-q0, b, a), y, q0);
+  return fma(fma(-q1, b, a), y, q1);
+}
+
 // The slope limiter of advctx.f90:34-40 (and advcty), with
 // deltar = a/dx, deltal = b/dx:
 //   sigma = 0.5*(SIGN(1,deltar)+SIGN(1,deltal))*MIN(|deltar|,|deltal|).
@@ -37,7 +65,8 @@ __device__ __forceinline__ float absd(float x) { return fabsf(x); }
 // MIN rule (NaN operands included): one division instead of two, the same
 // bits.  Other dx take the reference's two divisions.
 template <class T>
-__device__ __forceinline__ T minmod_div(T a, T b, T dx) {
+__device__ __forceinline__ T minmod_div(T a, T b, T dx, T rdx) {
+  (void)rdx;
   if (!(dx > T(0))) {
     const T dr = a / dx, dl = b / dx;
     return T(0.5) * (sign1(dr) + sign1(dl)) * fmin2(absd(dr), absd(dl));
@@ -70,14 +99,13 @@ __device__ __forceinline__ double minmod_ref(double dr, double dl) {
   if ((br ^ bl) < 0) return 0.0;
   return __longlong_as_double((ml < mr ? ml : mr) | (br & (long long)0x8000000000000000ULL));
 }
-__device__ __forceinline__ double minmod_div(double a, double b, double dx) {
+// rdx = RN(1/dx): the division by dx goes through div_rn_recip.
+__device__ __forceinline__ double minmod_div(double a, double b, double dx, double rdx) {
   const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b);
   const long long ma = ba & 0x7fffffffffffffffLL, mb = bb & 0x7fffffffffffffffLL;
-  if (!(dx > 0.0) || ma >= 0x7ff0000000000000LL || mb >= 0x7ff0000000000000LL) {
-    const double dr = a / dx, dl = b / dx;
-    return 0.5 * (sign1(dr) + sign1(dl)) * fmin2(fabs(dr), fabs(dl));
-  }
-  const double q = __longlong_as_double(mb < ma ? mb : ma) / dx;  // >= 0, +inf on overflow
+  if (!(dx > 0.0) || ma >= 0x7ff0000000000000LL || mb >= 0x7ff0000000000000LL)
+    return minmod_div_ieee(a, b, dx);
+  const double q = div_rn_recip(__longlong_as_double(mb < ma ? mb : ma), dx, rdx);  // >= 0, +inf on overflow
   if ((ba ^ bb) < 0) return isinf(q) ? 0.0 * q : 0.0;             // 0 * q
   return __longlong_as_double(__double_as_longlong(q) | (ba & (long long)0x8000000000000000ULL));
 }

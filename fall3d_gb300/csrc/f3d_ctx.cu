@@ -258,7 +258,7 @@ void sizloop(f3d_ctx* x) {
   }
   {
     ProfScope ps(x, "diffz");
-    launch_diffz<T>(c, hb, d, nz, 1, F::dz(x), dt, F::rkver(x), F::rho(x), F::rksz(x), nc, s);
+    launch_diffz<T>(c, hb, d, nz, 1, F::dz(x), dt, F::rkver(x), F::rho(x), F::rksz(x), F::lrho(x), nc, s);
   }
   if (x->iiter % 2 == 0) {
     difx();

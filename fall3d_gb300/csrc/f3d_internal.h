@@ -32,9 +32,10 @@ template <class T>
 void launch_advcty(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vy, T dy,
                    T dt, int ncls, cudaStream_t s);
 template <class T>
-// rksz: the face coefficients precomputed (launch_diff_coeffs) or NULL.
+// rksz, lrz: the face coefficients and 1/rho precomputed
+// (launch_diff_coeffs) or NULL.
 void launch_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* dz, T dt,
-                  const T* rkver, const T* rho, const T* rksz, int ncls, cudaStream_t s);
+                  const T* rkver, const T* rho, const T* rksz, const T* lrz, int ncls, cudaStream_t s);
 // lr, pk: 1/rho and rkh*rho precomputed (launch_diff_coeffs), or NULL to
 // form them from rho and rkh in the sweep.
 template <class T>
@@ -43,6 +44,7 @@ void launch_diffx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dx,
 template <class T>
 void launch_diffy(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dy, T dt,
                   const T* rkh, const T* rho, const T* lr, const T* pk, int ncls, cudaStream_t s);
+void launch_recip(long long n, const double* x, double* y, cudaStream_t s);  // y = 1/x
 void launch_diff_coeffs(Dims d, const double* rho, const double* rkh1, const double* rkhor,
                         const double* rkver, double* lr, double* pkx, double* pky, double* rksz,
                         cudaStream_t s);

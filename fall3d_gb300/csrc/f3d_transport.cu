@@ -235,7 +235,7 @@ __device__ __forceinline__ void adv_line_coef(T vq, T vq_1, T auxv, T dth, T& a,
 
 // work(q,1), work(q,2) of position q (1..n), or work(n+1,1) (advctx.f90:46)
 template <class T>
-__device__ __forceinline__ void adv_line_work(const AdvLine<T>& L, int q, int n, int st, T dx, T auxv) {
+__device__ __forceinline__ void adv_line_work(const AdvLine<T>& L, int q, int n, int st, T dx, T rdx, T auxv) {
   auto C = [&](int i) { return L.cl[i * st]; };
   if (q > n) {
     L.w1[(n + 1) * st] = auxv * L.v[n * st] * (C(n + 1) - C(n));
@@ -243,7 +243,7 @@ __device__ __forceinline__ void adv_line_work(const AdvLine<T>& L, int q, int n,
   }
   const T vq = L.v[q * st], vq_1 = L.v[(q > 1 ? q - 1 : 1) * st];
   L.w1[q * st] = auxv * (vq * C(q) - vq_1 * C(q - 1));
-  const T sigma = minmod_div(C(q + 1) - C(q), C(q) - C(q - 1), dx);
+  const T sigma = minmod_div(C(q + 1) - C(q), C(q) - C(q - 1), dx, rdx);
   L.w2[q * st] = L.b[q * st] * sigma * L.a[q * st];
 }
 
@@ -263,7 +263,7 @@ __global__ void k_advctx(T* c, long long cstride, int ncls, Dims d, int iz_loc, 
   const AdvLine<T> L{base, base + n2, base + 2 * n2, base + 3 * n2, base + 4 * n2, base + 5 * n2};
   const int j = blockIdx.x % ny + 1, k = blockIdx.x / ny + iz_loc;
   const T* vl = vx + d.M(1, j, k) - 1;  // vl[i] = vx(i,j,k)
-  const T auxv = dt / dx, dth = dt * T(0.5);
+  const T auxv = dt / dx, dth = dt * T(0.5), rdx = T(1) / dx;
   for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x) {
     const T vq = vl[q];
     L.v[q] = vq;
@@ -274,7 +274,7 @@ __global__ void k_advctx(T* c, long long cstride, int ncls, Dims d, int iz_loc, 
     __syncthreads();  // the coefficients are staged; the previous class is done with cl, w1, w2
     for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) L.cl[q] = cc[q];
     __syncthreads();
-    for (int q = threadIdx.x + 1; q <= nx + 1; q += blockDim.x) adv_line_work(L, q, nx, 1, dx, auxv);
+    for (int q = threadIdx.x + 1; q <= nx + 1; q += blockDim.x) adv_line_work(L, q, nx, 1, dx, rdx, auxv);
     __syncthreads();
     for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x) cc[q] = adv_line_update(L, q, nx, 1);
   }
@@ -297,7 +297,7 @@ __global__ void k_advcty(T* c, long long cstride, int ncls, Dims d, int iz_loc, 
   const long long rowstride = nx + 2;
   const long long cbase = d.C(act ? i : nx, 0, k);
   const long long vb = d.M(act ? i : nx, 1, k) - nx;  // vb + q*nx = vy(i,q,k)
-  const T auxv = dt / dy, dth = dt * T(0.5);
+  const T auxv = dt / dy, dth = dt * T(0.5), rdy = T(1) / dy;
   if (act)
     for (int q = ty + 1; q <= ny; q += TJ) {
       const T vq = vy[vb + (long long)q * nx];
@@ -310,7 +310,7 @@ __global__ void k_advcty(T* c, long long cstride, int ncls, Dims d, int iz_loc, 
     for (int q = ty; q <= ny + 1; q += TJ) L.cl[q * TI] = act ? cc[cbase + q * rowstride] : T(0);
     __syncthreads();
     if (act)
-      for (int q = ty + 1; q <= ny + 1; q += TJ) adv_line_work(L, q, ny, TI, dy, auxv);
+      for (int q = ty + 1; q <= ny + 1; q += TJ) adv_line_work(L, q, ny, TI, dy, rdy, auxv);
     __syncthreads();
     if (act)
       for (int q = ty + 1; q <= ny; q += TJ) cc[cbase + q * rowstride] = adv_line_update(L, q, ny, TI);
@@ -358,9 +358,21 @@ void launch_advcty(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, cons
 // flux (bottom/top non-averaged, interior averaged) are evaluated exactly as
 // written; an interior face shared by cells k and k+1 is the same
 // expression in both, so it is computed once and carried.
+// c/rho of diffz.f90: with lr = RN(1/rho) precomputed, the binary64 form
+// forms RN(c/rho) by div_rn_recip (same bits, no division).
+template <class T>
+__device__ __forceinline__ T c_over_rho(T c, T r, const T* lr, long long m) {
+  (void)lr;
+  (void)m;
+  return c / r;
+}
+__device__ __forceinline__ double c_over_rho(double c, double r, const double* lr, long long m) {
+  return lr ? div_rn_recip(c, r, lr[m]) : div_ieee(c, r);
+}
+
 template <class T>
 __global__ void k_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* dz, T dt,
-                        const T* rkver, const T* rho, const T* rksz) {
+                        const T* rkver, const T* rho, const T* rksz, const T* lrz) {
   extern __shared__ unsigned char smem_raw[];
   T* l_dz = reinterpret_cast<T*>(smem_raw);  // 0..nz
   T* l_dzdz = l_dz + (d.nz + 1);             // 1..nz
@@ -391,7 +403,8 @@ __global__ void k_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc,
   T cm = C(kb - 1), c0 = C(kb), cp = C(kb + 1);
   T rm = (kb > 1) ? R(kb - 1) : T(0), r0 = R(kb), rp = (kb < nz) ? R(kb + 1) : T(0);
   T Km = (kb > 1) ? K(kb - 1) : T(0), K0 = K(kb), Kp = (kb < nz) ? K(kb + 1) : T(0);
-  T qm = (kb > 1) ? cm / rm : T(0), q0 = c0 / r0, qp = (kb < nz) ? cp / rp : T(0);
+  auto Q = [&](T cv, T rv, int kk) { return c_over_rho(cv, rv, lrz, mb + (long long)(kk - 1) * ms); };
+  T qm = (kb > 1) ? Q(cm, rm, kb - 1) : T(0), q0 = Q(c0, r0, kb), qp = (kb < nz) ? Q(cp, rp, kb + 1) : T(0);
   // gradb of the first interior cell needs the face (kb-1, kb).
   T fprev = (kb >= 3) ? face(kb - 1, qm, q0, rm, r0, Km, K0) : T(0);
   for (int k = kb; k <= ke; ++k) {
@@ -424,20 +437,20 @@ __global__ void k_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc,
       cm = c0; c0 = cp; cp = C(k + 2);
       rm = r0; r0 = rp; rp = (k + 2 <= nz) ? R(k + 2) : T(0);
       Km = K0; K0 = Kp; Kp = (k + 2 <= nz) ? K(k + 2) : T(0);
-      qm = q0; q0 = qp; qp = (k + 2 <= nz) ? cp / rp : T(0);
+      qm = q0; q0 = qp; qp = (k + 2 <= nz) ? Q(cp, rp, k + 2) : T(0);
     }
   }
 }
 
 template <class T>
 void launch_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* dz, T dt,
-                  const T* rkver, const T* rho, const T* rksz, int ncls, cudaStream_t s) {
+                  const T* rkver, const T* rho, const T* rksz, const T* lrz, int ncls, cudaStream_t s) {
   const int bs = 128;
   const long long cols = (long long)d.nx * d.ny;
   const size_t sm = 2 * sizeof(T) * (d.nz + 1);
   k_diffz<T><<<dim3((unsigned)((cols + bs - 1) / bs), ncls), bs, sm, s>>>(c, cstride, d, nz_loc,
                                                                          iz_loc, dz, dt, rkver, rho,
-                                                                         rksz);
+                                                                         rksz, lrz);
   count_launch();
 }
 
@@ -619,6 +632,18 @@ __global__ void k_diff_coeffs(Dims d, const double* rho, const double* rkh1, con
     pky[m] = rkhor[m] * r;
     rksz[m] = m < top ? 0.5 * (rho[m + pl] * rkver[m + pl] + r * rkver[m]) : 0.0;
   }
+}
+
+__global__ void k_recip(long long n, const double* x, double* y) {
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
+       m += (long long)gridDim.x * blockDim.x)
+    y[m] = 1.0 / x[m];
+}
+
+void launch_recip(long long n, const double* x, double* y, cudaStream_t s) {
+  if (n <= 0) return;
+  k_recip<<<(int)std::min<long long>((n + 255) / 256, 152LL * 16), 256, 0, s>>>(n, x, y);
+  count_launch();
 }
 
 void launch_diff_coeffs(Dims d, const double* rho, const double* rkh1, const double* rkhor,
@@ -833,7 +858,7 @@ void launch_f2d(double* dst, const float* src, long long n, cudaStream_t s) {
   template void launch_advcty<T>(T*, long long, Dims, int, int, const T*, T, T, int,             \
                                  cudaStream_t);                                                  \
   template void launch_diffz<T>(T*, long long, Dims, int, int, const T*, T, const T*, const T*,  \
-                                const T*,                                                        \
+                                const T*, const T*,                                              \
                                 int, cudaStream_t);                                              \
   template void launch_diffx<T>(T*, long long, Dims, int, int, T, T, const T*, const T*,        \
                                 const T*, const T*, int, cudaStream_t);                          \

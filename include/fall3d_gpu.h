@@ -244,7 +244,10 @@ int f3d_setvset(const int* nx, const int* ny, const int* nz, const int* nc,
 
 /* Diagnostic: the binary64 log (op 0) or exp (op 1) that setvset's Ganser
  * drag iteration uses in place of pow (a table-driven restatement, within a
- * few ulp), on n host or device values.  No reference counterpart. */
+ * few ulp), on n host or device values; op 2: the quotients a/b of n pairs
+ * x = (a0, b0, a1, b1, ...) formed from the reciprocal of b the way the
+ * plain form's sweeps divide (equal to the IEEE quotient).  No reference
+ * counterpart. */
 int f3d_dmath_eval(int op, long long n, const double* x, double* y);
 
 /* Sources/setvdrydep.f90:1 setvdrydep (module state made explicit). */

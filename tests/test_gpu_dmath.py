@@ -64,4 +64,35 @@ def test_pow_as_used_by_the_drag_iteration():
 
 def test_rejects_bad_op():
     with pytest.raises(F.F3DError):
-        F.dmath_eval(2, np.ones(4))
+        F.dmath_eval(3, np.ones(4))
+
+
+def test_quotient_from_reciprocal_is_the_ieee_quotient():
+    """op 2: RN(a/b) from RN(1/b) by Markstein's correction, as the plain
+    form's limiter (m/dx) and diffz (c/rho) divide: bit for bit the IEEE
+    quotient, across magnitudes, signed zeros, subnormals and non-finite
+    operands (the guarded ones take the division)."""
+    rng = np.random.default_rng(8)
+    n = 2_000_000
+    with np.errstate(over="ignore"):  # magnitudes past the binary64 range become infinities
+        a = rng.choice([-1.0, 1.0], n) * 10.0 ** rng.uniform(-310, 310, n) * rng.uniform(1.0, 10.0, n)
+        b = rng.choice([-1.0, 1.0], n) * 10.0 ** rng.uniform(-310, 310, n) * rng.uniform(1.0, 10.0, n)
+    # the operands of the sweeps: concentrations over densities and grid spacings
+    a[: n // 4] = 10.0 ** rng.uniform(-40, 3, n // 4)
+    b[: n // 4] = rng.uniform(0.05, 1.4, n // 4)
+    a[n // 4: n // 2] = rng.uniform(0.0, 1e-6, n // 4)
+    b[n // 4: n // 2] = rng.choice([0.01, 0.025, 0.1, 1000.0, 2500.0], n // 4)
+    special = np.array([0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, 1.7976931348623157e308,
+                        np.inf, -np.inf, np.nan, 1.0, 3.0, 2.0 ** -900, 2.0 ** 900])
+    sa, sb = np.meshgrid(special, special)
+    a = np.concatenate([a, sa.ravel()])
+    b = np.concatenate([b, sb.ravel()])
+    x = np.empty(2 * a.size)
+    x[0::2], x[1::2] = a, b
+    y = F.dmath_eval(2, x)
+    with np.errstate(all="ignore"):
+        t = a / b
+    nan = np.isnan(t)
+    assert np.array_equal(np.isnan(y), nan)
+    bad = np.nonzero(y[~nan].view(np.uint64) != t[~nan].view(np.uint64))[0]
+    assert bad.size == 0, (bad.size, a[~nan][bad[:3]], b[~nan][bad[:3]])
