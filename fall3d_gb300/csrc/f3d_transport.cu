@@ -124,17 +124,24 @@ void launch_setbcc(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, cons
 // (c(k-1), c(k), c(k+1), c(k+2)) carries them as k advances.
 template <class T>
 struct ZTab {  // per-level constants of advctzc.f90:34-36 (IEEE, as on the host)
-  T dzz, dzk, dzk_1, dzm1;
+  T dzz, dzk, dzk_1, hdzm1;  // hdzm1 = (dt*0.5)*dz(k-1), the first factors of work(k,2)
 };
 
+// work(k,1), work(k,2) (advctzc.f90:37-46) at a level with c0 = c(k),
+// cp = c(k+1), vk = vk(k), vk_1 = vk(k-1), given the previous level's
+// product pm = vk(k-1)*c(k-1) and difference dm = c(k)-c(k-1); returns this
+// level's p0 = vk(k)*c(k) and d0 = c(k+1)-c(k) for the next one (the
+// reference forms both twice, with the same operations).
 template <class T>
-__device__ __forceinline__ void adv_z_work(T cm, T c0, T cp, T vk, T vk_1, const ZTab<T>& z, T dt,
-                                           T& w1, T& w2) {
+__device__ __forceinline__ void adv_z_work(T c0, T cp, T vk, T vk_1, T pm, T dm, const ZTab<T>& z, T dt,
+                                           T& w1, T& w2, T& p0, T& d0) {
   const T vk_12 = T(0.5) * (vk + vk_1);
-  w1 = dt * (vk * c0 - vk_1 * cm) * z.dzz;
-  const T sigma = minmod_ref((cp - c0) * z.dzk, (c0 - cm) * z.dzk_1);
+  p0 = vk * c0;
+  w1 = dt * (p0 - pm) * z.dzz;
+  d0 = cp - c0;
+  const T sigma = minmod_ref(d0 * z.dzk, dm * z.dzk_1);
   const T Crk = absd(vk_12) * dt * z.dzk_1;
-  w2 = dt * T(0.5) * z.dzm1 * (T(1) - Crk) * sigma * absd(vk_12) * z.dzz;
+  w2 = z.hdzm1 * (T(1) - Crk) * sigma * absd(vk_12) * z.dzz;
 }
 
 template <class T>
@@ -147,7 +154,7 @@ __global__ void k_advctzc(T* c, long long cstride, Dims d, int nz_loc, int iz_lo
     tab[k].dzz = T(2) / (dz[k] + dz[k - 1]);
     tab[k].dzk = T(1) / dz[k];
     tab[k].dzk_1 = T(1) / dz[k - 1];
-    tab[k].dzm1 = dz[k - 1];
+    tab[k].hdzm1 = dt * T(0.5) * dz[k - 1];
   }
   __syncthreads();
   const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -163,21 +170,22 @@ __global__ void k_advctzc(T* c, long long cstride, Dims d, int nz_loc, int iz_lo
   const int kb = iz_loc, ke = iz_loc + nz_loc - 1;
   T c_m1 = CO(kb - 1), c_0 = CO(kb), c_p1 = CO(kb + 1);
   T vk_0 = VK(kb), vk_m1 = VK(kb > 1 ? kb - 1 : 1);
-  T w1_k, w2_k, w2_km;
-  adv_z_work(c_m1, c_0, c_p1, vk_0, vk_m1, tab[kb], dt, w1_k, w2_k);
+  T w1_k, w2_k, w2_km, pk, dk;
+  adv_z_work(c_0, c_p1, vk_0, vk_m1, vk_m1 * c_m1, c_0 - c_m1, tab[kb], dt, w1_k, w2_k, pk, dk);
   if (kb == 1) {
     w2_km = w2_k;
   } else {
-    T w1_dummy;
-    adv_z_work(CO(kb - 2), c_m1, c_0, vk_m1, VK(kb - 1 > 1 ? kb - 2 : 1), tab[kb - 1], dt, w1_dummy,
-               w2_km);
+    T w1_dummy, p_dummy, d_dummy;
+    const T c_m2 = CO(kb - 2), vk_m2 = VK(kb - 1 > 1 ? kb - 2 : 1);
+    adv_z_work(c_m1, c_0, vk_m1, vk_m2, vk_m2 * c_m2, c_m1 - c_m2, tab[kb - 1], dt, w1_dummy, w2_km,
+               p_dummy, d_dummy);
   }
   for (int k = kb; k <= ke; ++k) {
     T w1_n, w2_n, c_p2 = T(0), vk_p1 = T(0);
     if (k + 1 <= nz) {
       c_p2 = CO(k + 2);
       vk_p1 = VK(k + 1);
-      adv_z_work(c_0, c_p1, c_p2, vk_p1, vk_0, tab[k + 1], dt, w1_n, w2_n);
+      adv_z_work(c_p1, c_p2, vk_p1, vk_0, pk, dk, tab[k + 1], dt, w1_n, w2_n, pk, dk);
     } else {
       w1_n = dt * vk_0 * (c_p1 - c_0) * dznz;  // work(nz+1,1), advctzc.f90:58-64
       w2_n = w2_k;                             // kmin = nz
