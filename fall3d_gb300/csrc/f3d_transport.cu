@@ -11,13 +11,22 @@
 // addresses of the (nx+2)(ny+2)(nz+2) class block):
 //  * column kernels (advctzc, diffz, wetdep): one thread per (i,j) column,
 //    marching k with a register window;
-//  * x-line kernels (advctx, diffx): one block per x line, the line staged in
-//    shared memory;
+//  * x-line kernels (advctx, diffx): one block per x line, taking it through
+//    every class, the line staged in shared memory;
 //  * y-line kernels (advcty, diffy): one block per tile of TI adjacent y
-//    lines at one k, the tile staged in shared memory, rows of TI
-//    consecutive x addresses per load.
+//    lines at one k, through every class, the tile staged in shared memory,
+//    rows of TI consecutive x addresses per load.
 // A block owns whole lines, so the in-place update cannot race with a
 // neighbour block's reads.
+//
+// GB300 issues binary64 arithmetic at 1/64 of the binary32 rate, and a
+// binary64 division costs many times a multiply-add, so the sweeps keep
+// the reference's results bit for bit while issuing fewer binary64
+// operations: the class-independent factors of a line are formed once for
+// all classes, values shared by neighbouring cells are formed once, the
+// limiter's sign and minimum logic runs on the bit patterns, and divisions
+// by a per-launch or per-meteo-update divisor use its reciprocal with
+// Markstein's correction (div_rn_recip, f3d_common.cuh).
 #include <algorithm>
 #include <cstdio>
 
