@@ -260,12 +260,7 @@ int f3d_diffz(double* c, const int* nx, const int* ny, const int* nz, const int*
   const double* drk = m.arr(rkver, (size_t)d.cells(), false);
   const double* drho = m.arr(rho, (size_t)d.cells(), false);
   if (m.error()) return m.error();
-  // 1/rho, so that c/rho is formed the way the context's sweep forms it
-  TmpBuf lr;
-  if (int r = lr.alloc(sizeof(double) * (size_t)d.cells())) return r;
-  launch_recip(d.cells(), drho, reinterpret_cast<double*>(lr.p), 0);
-  launch_diffz<double>(dc, 0, d, *nz_loc, *iz_loc, ddz, *dt, drk, drho, nullptr,
-                       reinterpret_cast<const double*>(lr.p), 1, 0);
+  launch_diffz<double>(dc, 0, d, *nz_loc, *iz_loc, ddz, *dt, drk, drho, nullptr, nullptr, 1, 0);
   return m.finish();
 }
 

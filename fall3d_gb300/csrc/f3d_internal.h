@@ -44,7 +44,6 @@ void launch_diffx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dx,
 template <class T>
 void launch_diffy(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dy, T dt,
                   const T* rkh, const T* rho, const T* lr, const T* pk, int ncls, cudaStream_t s);
-void launch_recip(long long n, const double* x, double* y, cudaStream_t s);  // y = 1/x
 void launch_diff_coeffs(Dims d, const double* rho, const double* rkh1, const double* rkhor,
                         const double* rkver, double* lr, double* pkx, double* pky, double* rksz,
                         cudaStream_t s);

@@ -651,18 +651,6 @@ __global__ void k_diff_coeffs(Dims d, const double* rho, const double* rkh1, con
   }
 }
 
-__global__ void k_recip(long long n, const double* x, double* y) {
-  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
-       m += (long long)gridDim.x * blockDim.x)
-    y[m] = 1.0 / x[m];
-}
-
-void launch_recip(long long n, const double* x, double* y, cudaStream_t s) {
-  if (n <= 0) return;
-  k_recip<<<(int)std::min<long long>((n + 255) / 256, 152LL * 16), 256, 0, s>>>(n, x, y);
-  count_launch();
-}
-
 void launch_diff_coeffs(Dims d, const double* rho, const double* rkh1, const double* rkhor,
                         const double* rkver, double* lr, double* pkx, double* pky, double* rksz,
                         cudaStream_t s) {

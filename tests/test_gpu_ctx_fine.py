@@ -3,10 +3,10 @@ fine-grained entry points, class by class, on the context's own
 coefficients: bit for bit.
 
 The context's sweeps take each line through all classes, read 1/rho, rkh*rho
-and the diffz face coefficients formed once per meteo update, and divide by
-reciprocals (Markstein's correction); the fine-grained routines run one
-class in the reference's operation order and are bit for bit equal to the
-oracle (tests/test_gpu_fine.py).  So this pins the context's transport to
+and the diffz face coefficients formed once per meteo update, and form
+diffz's c/rho from 1/rho (Markstein's correction); the fine-grained routines
+run one class in the reference's operation order with the IEEE division and
+are bit for bit equal to the oracle (tests/test_gpu_fine.py).  So this pins the context's transport to
 the oracle's on the same coefficients (Sources/sizloop.f90:31-83)."""
 import numpy as np
 import pytest
