@@ -331,7 +331,7 @@ struct ClassConst {
   double num;       // 4*gi*diam*rhop, the numerator of setvset.f90:104
   double rk1, rk2;  // Ganser shape factors (setvset.f90:127-128)
   double rk12;      // rk1 * rk2
-  double sqnum;    // sqrt(num)
+  double sqnum;     // sqrt(num)
   double drk12;     // diam * rk1 * rk2
   double cd100;     // Wilson
   int ok;           // get_gama converged
