@@ -355,12 +355,25 @@ void launch_getc0(double* cdry, double* cwet, double* cload, Dims d, int nc, int
 // Sources/finddt.f90:26-57.  MAX is exact and order independent, so the
 // largest dtcni is found with a bitwise atomicMax on the (non-negative)
 // binary64 patterns; NaN terms are skipped as MAX(dtcn,NaN) keeps dtcn.
+// Every division has a divisor known per launch or per level, so each is
+// formed from that divisor's reciprocal (div_rn_recip: the same quotient).
 __global__ void k_finddt(Dims d, int nc, double dX1, double dX2, const double* dz,
                          const double* vx, const double* vy, const double* vz,
                          const double* vset, const double* rkh1, const double* rkhor,
                          const double* rkver, unsigned long long* dtcn_bits) {
+  extern __shared__ double lvl[];  // per level k (index k-1): 1/ddz, 1/ddz^2, 1/den
   const int nx = d.nx, nz = d.nz;
   const long long s3 = d.cells();
+  for (int k = threadIdx.x + 1; k <= nz; k += blockDim.x) {
+    const double ddz = fmin2(dz[k - 1], dz[k]);
+    const double den = k == 1 ? dz[1] : (k == nz ? dz[nz - 1] : dz[k] + dz[k - 1]);
+    lvl[k - 1] = 1.0 / ddz;
+    lvl[nz + k - 1] = 1.0 / (ddz * ddz);
+    lvl[2 * nz + k - 1] = 1.0 / den;
+  }
+  __syncthreads();
+  const double x2 = dX1 * dX1, y2 = dX2 * dX2;
+  const double rx2 = 1.0 / x2, rx = 1.0 / dX1, ry2 = 1.0 / y2, ry = 1.0 / dX2;
   double best = 0.0;
   // one thread per cell: the five class-independent terms are summed once
   // (the reference's left-to-right order keeps them as a prefix), then the
@@ -371,9 +384,10 @@ __global__ void k_finddt(Dims d, int nc, double dX1, double dX2, const double* d
     const long long r = m / nx;
     const int j = (int)(r % d.ny) + 1, k = (int)(r / d.ny) + 1;
     const double ddz = fmin2(dz[k - 1], dz[k]);
-    const double pre = (2.0 * rkh1[m] / (dX1 * dX1)) + (fabs(vx[m]) / dX1) +
-                       (2.0 * rkhor[m] / (dX2 * dX2)) + (fabs(vy[m]) / dX2) +
-                       (2.0 * rkver[m] / (ddz * ddz));
+    const double rz = lvl[k - 1], rzz = lvl[nz + k - 1], rden = lvl[2 * nz + k - 1];
+    const double pre = div_rn_recip(2.0 * rkh1[m], x2, rx2) + div_rn_recip(fabs(vx[m]), dX1, rx) +
+                       div_rn_recip(2.0 * rkhor[m], y2, ry2) + div_rn_recip(fabs(vy[m]), dX2, ry) +
+                       div_rn_recip(2.0 * rkver[m], ddz * ddz, rzz);
     long long mlo, mhi;
     double den;
     if (k == 1) {
@@ -392,8 +406,8 @@ __global__ void k_finddt(Dims d, int nc, double dX1, double dX2, const double* d
     const double vzm = vz[m];
     for (int ic = 0; ic < nc; ++ic) {
       const double* vs = vset + (long long)ic * s3;
-      const double dvsetdz = (vs[mhi] - vs[mlo]) / den;
-      const double dtcni = pre + (fabs((vzm + vs[m])) / ddz) + (fabs(dvsetdz));
+      const double dvsetdz = div_rn_recip(vs[mhi] - vs[mlo], den, rden);
+      const double dtcni = pre + div_rn_recip(fabs((vzm + vs[m])), ddz, rz) + (fabs(dvsetdz));
       best = fmax2(best, dtcni);
     }
   }
@@ -408,7 +422,8 @@ void launch_finddt(Dims d, int nc, double dX1, double dX2, const double* dz, con
                    cudaStream_t s) {
   const long long n = d.cells();
   const int nb = (int)std::min<long long>((n + 255) / 256, 152LL * 8);
-  k_finddt<<<nb, 256, 0, s>>>(d, nc, dX1, dX2, dz, vx, vy, vz, vset, rkh1, rkhor, rkver, dtcn_bits);
+  k_finddt<<<nb, 256, 3 * sizeof(double) * (size_t)d.nz, s>>>(d, nc, dX1, dX2, dz, vx, vy, vz, vset, rkh1,
+                                                              rkhor, rkver, dtcn_bits);
   count_launch();
 }
 
