@@ -473,11 +473,12 @@ void launch_diffz(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const
 
 // ------------------------------------------------------- diffx / diffy
 // Sources/diffx.f90:20-55, Sources/diffy.f90:20-55.  A line is staged with
-// what its cells share: c (0..n+1), cl = c*(1/rho) (1..n) and the averaged
-// face coefficient fk(q) = 0.5*(pk(q+1)+pk(q)) (1..n-1), pk = rkh*rho, each
-// formed once with the reference's operations, so every cell reads the bits
-// it would have computed itself.  The end cells (non-averaged faces, ghost
-// products) fetch their own factors.
+// what its cells share: c (0..n+1), cl = c*(1/rho) (1..n), the averaged face
+// coefficient fk(q) = 0.5*(pk(q+1)+pk(q)) (1..n-1), pk = rkh*rho, and the
+// interior face flux ff(q) = fk(q)*(cl(q+1)-cl(q)) (1..n-1), each formed once
+// with the reference's operations, so every cell reads the bits it would
+// have computed itself.  The end cells (non-averaged faces, ghost products)
+// fetch their own factors.
 
 // 1/rho and rkh*rho of one position: precomputed (lrp, pkp) or formed here.
 template <class T>
@@ -500,8 +501,10 @@ struct DiffSrc {  // the line's factors in global memory: position q at m1 + (q-
   __device__ void at(int q, T& l, T& p) const { diff_factors(lrp, pkp, rho, rkh, m1 + (q - 1) * ms, l, p); }
 };
 
+// ff(q) = fk(q)*(cl(q+1) - cl(q)): the interior face flux, gradr of cell q
+// and gradl of cell q+1 (diffx.f90:34-40), formed once per face.
 template <class T>
-__device__ __forceinline__ T diff_line_cell(int q, int n, const T* cv, const T* cl, const T* fk,
+__device__ __forceinline__ T diff_line_cell(int q, int n, const T* cv, const T* cl, const T* ff,
                                             const DiffSrc<T>& src, int st, T dtdx2) {
   // st: stride between consecutive line positions in the staged arrays
   auto Cq = [&](int a) { return cv[a * st]; };
@@ -522,8 +525,8 @@ __device__ __forceinline__ T diff_line_cell(int q, int n, const T* cv, const T* 
     gradl = pm * (Q(n) - Q(n - 1));
     gradr = fmin2(T(0), gradr);
   } else {
-    gradr = fk[q * st] * (Q(q + 1) - Q(q));
-    gradl = fk[(q - 1) * st] * (Q(q) - Q(q - 1));
+    gradr = ff[q * st];
+    gradl = ff[(q - 1) * st];
   }
   return Cq(q) + dtdx2 * (gradr - gradl);
 }
@@ -552,6 +555,7 @@ __global__ void k_diffx(T* c, long long cstride, int ncls, Dims d, int iz_loc, T
   T* fk = lr + (nx + 2);
   T* cv = fk + (nx + 2);
   T* cl = cv + (nx + 2);
+  T* ff = cl + (nx + 2);
   const int j = blockIdx.x % ny + 1, k = blockIdx.x / ny + iz_loc;
   const DiffSrc<T> src{lrp, pkp, rho, rkh, d.M(1, j, k), 1};
   for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x) diff_stage(q, nx, src, lr + q, fk + q);
@@ -565,8 +569,10 @@ __global__ void k_diffx(T* c, long long cstride, int ncls, Dims d, int iz_loc, T
       if (q >= 1 && q <= nx) cl[q] = v * lr[q];
     }
     __syncthreads();
+    for (int q = threadIdx.x + 1; q < nx; q += blockDim.x) ff[q] = fk[q] * (cl[q + 1] - cl[q]);
+    __syncthreads();
     for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x)
-      cc[q] = diff_line_cell(q, nx, cv, cl, fk, src, 1, dtdx2);
+      cc[q] = diff_line_cell(q, nx, cv, cl, ff, src, 1, dtdx2);
   }
 }
 
@@ -586,6 +592,7 @@ __global__ void k_diffy(T* c, long long cstride, int ncls, Dims d, int iz_loc, T
   T* fk = lr + n2;
   T* cv = fk + n2;
   T* cl = cv + n2;
+  T* ff = cl + n2;
   const long long rowstride = nx + 2;
   const long long base = d.C(act ? i : nx, 0, k);
   const DiffSrc<T> src{lrp, pkp, rho, rkh, d.M(act ? i : nx, 1, k), nx};
@@ -603,15 +610,18 @@ __global__ void k_diffy(T* c, long long cstride, int ncls, Dims d, int iz_loc, T
       }
     __syncthreads();
     if (act)
+      for (int q = ty + 1; q < ny; q += TJ) ff[q * TI] = fk[q * TI] * (cl[(q + 1) * TI] - cl[q * TI]);
+    __syncthreads();
+    if (act)
       for (int q = ty + 1; q <= ny; q += TJ)
-        cc[base + q * rowstride] = diff_line_cell(q, ny, cv, cl, fk, src, TI, dtdy2);
+        cc[base + q * rowstride] = diff_line_cell(q, ny, cv, cl, ff, src, TI, dtdy2);
   }
 }
 
 template <class T>
 void launch_diffx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dx, T dt,
                   const T* rkh, const T* rho, const T* lr, const T* pk, int ncls, cudaStream_t s) {
-  const size_t sm = 4 * (size_t)(d.nx + 2) * sizeof(T);
+  const size_t sm = 5 * (size_t)(d.nx + 2) * sizeof(T);
   set_smem((const void*)k_diffx<T>, sm);
   const int bs = d.nx >= 256 ? 256 : 128;
   k_diffx<T><<<dim3(d.ny * nz_loc), bs, sm, s>>>(c, cstride, ncls, d, iz_loc, dx, dt, rkh, rho, lr, pk);
@@ -622,10 +632,10 @@ template <class T>
 void launch_diffy(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, T dy, T dt,
                   const T* rkh, const T* rho, const T* lr, const T* pk, int ncls, cudaStream_t s) {
   // at most ~48 KB per block, so that several blocks share an SM
-  int TI = pick_ti(d.ny, sizeof(T), 4);
-  while (TI > 4 && 4 * (size_t)(d.ny + 2) * TI * sizeof(T) > 48 * 1024) TI >>= 1;
+  int TI = pick_ti(d.ny, sizeof(T), 5);
+  while (TI > 4 && 5 * (size_t)(d.ny + 2) * TI * sizeof(T) > 48 * 1024) TI >>= 1;
   const int TJ = 256 / TI;
-  const size_t sm = 4 * (size_t)(d.ny + 2) * TI * sizeof(T);
+  const size_t sm = 5 * (size_t)(d.ny + 2) * TI * sizeof(T);
   set_smem((const void*)k_diffy<T>, sm);
   const int ntile = (d.nx + TI - 1) / TI;
   k_diffy<T><<<dim3(ntile * nz_loc), dim3(TI, TJ), sm, s>>>(c, cstride, ncls, d, iz_loc, dy, dt,
