@@ -237,12 +237,28 @@ void launch_advctzc(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, con
 //   a(q) = |0.5*(v(q)+v(q-1))|,  b(q) = (dt*0.5)*(1 - auxv*a(q)),
 // so that work(q,2) = dt*0.5*(1-Cri)*sigma*|v_12| is (b(q)*sigma)*a(q),
 // the reference's product left to right; then per class the line's
-// concentrations are staged, work(q,1), work(q,2) formed and the line
-// updated.
+// concentrations are staged with the products v(q)*c(q) and differences
+// c(q+1)-c(q) that neighbouring positions share (each formed once, as the
+// reference forms it), work(q,1), work(q,2) formed and the line updated.
 template <class T>
 struct AdvLine {  // a line's staged arrays at stride st
   T *v, *a, *b, *cl, *w1, *w2;
+  T *p, *dc;  // p(q) = v(q)*c(q) (1..n), dc(q) = c(q+1)-c(q) (0..n): shared by neighbours
 };
+
+// Stages position q (0..n+1) of a class's line: c, and the products and
+// differences that work(q,1) and the limiter of neighbouring positions share.
+// c0 = c(q), c1 = c(q+1) (read only for q <= n).  SH: stage p and dc (the
+// x sweep); the y sweep's tiles of lines keep to six arrays, whose shared
+// memory lets more blocks share an SM, and form them per position.
+template <bool SH, class T>
+__device__ __forceinline__ void adv_line_stage(const AdvLine<T>& L, int q, int n, int st, T c0, T c1) {
+  L.cl[q * st] = c0;
+  if constexpr (SH) {
+    if (q >= 1 && q <= n) L.p[q * st] = L.v[q * st] * c0;
+    if (q <= n) L.dc[q * st] = c1 - c0;
+  }
+}
 
 template <class T>
 __device__ __forceinline__ void adv_line_coef(T vq, T vq_1, T auxv, T dth, T& a, T& b) {
@@ -251,16 +267,23 @@ __device__ __forceinline__ void adv_line_coef(T vq, T vq_1, T auxv, T dth, T& a,
 }
 
 // work(q,1), work(q,2) of position q (1..n), or work(n+1,1) (advctx.f90:46)
-template <class T>
+template <bool SH, class T>
 __device__ __forceinline__ void adv_line_work(const AdvLine<T>& L, int q, int n, int st, T dx, T rdx, T auxv) {
   auto C = [&](int i) { return L.cl[i * st]; };
   if (q > n) {
-    L.w1[(n + 1) * st] = auxv * L.v[n * st] * (C(n + 1) - C(n));
+    L.w1[(n + 1) * st] = auxv * L.v[n * st] * (SH ? L.dc[n * st] : C(n + 1) - C(n));
     return;
   }
   const T vq = L.v[q * st], vq_1 = L.v[(q > 1 ? q - 1 : 1) * st];
-  L.w1[q * st] = auxv * (vq * C(q) - vq_1 * C(q - 1));
-  const T sigma = minmod_div(C(q + 1) - C(q), C(q) - C(q - 1), dx, rdx);
+  if constexpr (SH) {
+    // vq_1*c(q-1) is the left neighbour's product, or v(1)*c(0) at q = 1
+    const T pl = q > 1 ? L.p[(q - 1) * st] : vq_1 * C(0);
+    L.w1[q * st] = auxv * (L.p[q * st] - pl);
+  } else {
+    L.w1[q * st] = auxv * (vq * C(q) - vq_1 * C(q - 1));
+  }
+  const T sigma = SH ? minmod_div(L.dc[q * st], L.dc[(q - 1) * st], dx, rdx)
+                     : minmod_div(C(q + 1) - C(q), C(q) - C(q - 1), dx, rdx);
   L.w2[q * st] = L.b[q * st] * sigma * L.a[q * st];
 }
 
@@ -277,7 +300,8 @@ __global__ void k_advctx(T* c, long long cstride, int ncls, Dims d, int iz_loc, 
   extern __shared__ unsigned char smem_raw[];
   const int nx = d.nx, ny = d.ny, n2 = nx + 2;
   T* base = reinterpret_cast<T*>(smem_raw);
-  const AdvLine<T> L{base, base + n2, base + 2 * n2, base + 3 * n2, base + 4 * n2, base + 5 * n2};
+  const AdvLine<T> L{base,          base + n2,     base + 2 * n2, base + 3 * n2,
+                     base + 4 * n2, base + 5 * n2, base + 6 * n2, base + 7 * n2};
   const int j = blockIdx.x % ny + 1, k = blockIdx.x / ny + iz_loc;
   const T* vl = vx + d.M(1, j, k) - 1;  // vl[i] = vx(i,j,k)
   const T auxv = dt / dx, dth = dt * T(0.5), rdx = T(1) / dx;
@@ -289,9 +313,10 @@ __global__ void k_advctx(T* c, long long cstride, int ncls, Dims d, int iz_loc, 
   for (int ic = 0; ic < ncls; ++ic) {
     T* cc = c + (long long)ic * cstride + d.C(0, j, k);
     __syncthreads();  // the coefficients are staged; the previous class is done with cl, w1, w2
-    for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x) L.cl[q] = cc[q];
+    for (int q = threadIdx.x; q <= nx + 1; q += blockDim.x)
+      adv_line_stage<true>(L, q, nx, 1, cc[q], q <= nx ? cc[q + 1] : T(0));
     __syncthreads();
-    for (int q = threadIdx.x + 1; q <= nx + 1; q += blockDim.x) adv_line_work(L, q, nx, 1, dx, rdx, auxv);
+    for (int q = threadIdx.x + 1; q <= nx + 1; q += blockDim.x) adv_line_work<true>(L, q, nx, 1, dx, rdx, auxv);
     __syncthreads();
     for (int q = threadIdx.x + 1; q <= nx; q += blockDim.x) cc[q] = adv_line_update(L, q, nx, 1);
   }
@@ -310,7 +335,7 @@ __global__ void k_advcty(T* c, long long cstride, int ncls, Dims d, int iz_loc, 
   const bool act = i <= nx;
   const size_t n2 = (size_t)(ny + 2) * TI;
   T* base = reinterpret_cast<T*>(smem_raw) + tx;  // [q][TI], this thread's line
-  const AdvLine<T> L{base, base + n2, base + 2 * n2, base + 3 * n2, base + 4 * n2, base + 5 * n2};
+  const AdvLine<T> L{base, base + n2, base + 2 * n2, base + 3 * n2, base + 4 * n2, base + 5 * n2, nullptr, nullptr};
   const long long rowstride = nx + 2;
   const long long cbase = d.C(act ? i : nx, 0, k);
   const long long vb = d.M(act ? i : nx, 1, k) - nx;  // vb + q*nx = vy(i,q,k)
@@ -324,10 +349,12 @@ __global__ void k_advcty(T* c, long long cstride, int ncls, Dims d, int iz_loc, 
   for (int ic = 0; ic < ncls; ++ic) {
     T* cc = c + (long long)ic * cstride;
     __syncthreads();
-    for (int q = ty; q <= ny + 1; q += TJ) L.cl[q * TI] = act ? cc[cbase + q * rowstride] : T(0);
+    if (act)
+      for (int q = ty; q <= ny + 1; q += TJ)
+        adv_line_stage<false>(L, q, ny, TI, cc[cbase + q * rowstride], T(0));
     __syncthreads();
     if (act)
-      for (int q = ty + 1; q <= ny + 1; q += TJ) adv_line_work(L, q, ny, TI, dy, rdy, auxv);
+      for (int q = ty + 1; q <= ny + 1; q += TJ) adv_line_work<false>(L, q, ny, TI, dy, rdy, auxv);
     __syncthreads();
     if (act)
       for (int q = ty + 1; q <= ny; q += TJ) cc[cbase + q * rowstride] = adv_line_update(L, q, ny, TI);
@@ -351,7 +378,7 @@ static void set_smem(const void* fn, size_t bytes) {
 template <class T>
 void launch_advctx(T* c, long long cstride, Dims d, int nz_loc, int iz_loc, const T* vx, T dx,
                    T dt, int ncls, cudaStream_t s) {
-  const size_t sm = 6 * (size_t)(d.nx + 2) * sizeof(T);
+  const size_t sm = 8 * (size_t)(d.nx + 2) * sizeof(T);
   set_smem((const void*)k_advctx<T>, sm);
   const int bs = d.nx >= 256 ? 256 : 128;
   k_advctx<T><<<dim3(d.ny * nz_loc), bs, sm, s>>>(c, cstride, ncls, d, iz_loc, vx, dx, dt);
