@@ -656,12 +656,14 @@ static ChainGeom chain_geom(Dims d, int np) {
   ChainGeom g;
   g.d = d;
   g.L = d.cells() * np;
-  // The segments are the threads of one launch: as many as the device holds
-  // at once (one wave, no tail) when the chain is long enough, else fewer,
-  // longer segments so that the warm-up (W cells recomputed from the
-  // preceding segment, enough for the cd iteration to forget its guess)
-  // stays a small fraction of the work.
-  long long S = (g.L + chain_capacity() - 1) / chain_capacity();
+  // The segments are the threads of one launch: half as many as the device
+  // holds at once when the chain is long enough (measured on cfg1: the
+  // binary64 pipe stays as busy with half the threads resident, and the
+  // warm-up of W cells recomputed from the preceding segment, enough for
+  // the cd iteration to forget its guess, halves relative to the work;
+  // a quarter is slower again), else fewer, longer segments.
+  const long long cap = chain_capacity() / 2;
+  long long S = (g.L + cap - 1) / cap;
   S = std::max<long long>(256, S);
   g.S = S;
   g.W = 64;
