@@ -18,9 +18,9 @@ from helpers import assert_same_bits
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("seed,steps", [(5, 8), (6, 9)])  # both x/y orders (iiter parity)
-def test_context_step_equals_fine_grained_sequence(seed, steps):
-    s = synth.make_scenario("small", seed=seed, wetdep=False)
+@pytest.mark.parametrize("seed,steps,wet", [(5, 8, False), (6, 9, False), (7, 8, True)])  # both x/y orders
+def test_context_step_equals_fine_grained_sequence(seed, steps, wet):
+    s = synth.make_scenario("small", seed=seed, wetdep=wet)
     gr = s.grid
     nx, ny, nz, nc = gr["nx"], gr["ny"], gr["nz"], gr["nc"]
     # a plume to transport
@@ -45,6 +45,12 @@ def test_context_step_equals_fine_grained_sequence(seed, steps):
     dz = np.ascontiguousarray(gr["dz"], dtype=np.float64)
     c = fl["c"].copy()
     cdry = fl["cdry"].copy()
+    cwet = fl["cwet"].copy()
+    # the context's wet inputs: PBLH as read, PRATE in mm/h (reamet.f90:146)
+    zi = np.ascontiguousarray(s.met["pblh"][0], dtype=np.float64)
+    prate = np.ascontiguousarray(s.met["prate"][0], dtype=np.float64) * 3600.0
+    zlayer = np.ascontiguousarray(gr["zlayer"], dtype=np.float64)
+    diam = np.ascontiguousarray(gr["diam"], dtype=np.float64)
     args = (nx, ny, nz, nz, 1)
     for ic in range(nc):
         cc = np.ascontiguousarray(c[ic])
@@ -58,8 +64,13 @@ def test_context_step_equals_fine_grained_sequence(seed, steps):
         difx = lambda: F.diffx(cc, *args, gr["dX1"], dt, co["rkh1"], co["rho"])
         dify = lambda: F.diffy(cc, *args, gr["dX2"], dt, co["rkhor"], co["rho"])
         (difx(), dify()) if it % 2 == 0 else (dify(), difx())
+        if wet and ic < gr["np"]:
+            F.wetdep(cc, cwet, ic + 1, *args, dt, diam, zlayer, dz, zi, prate)
         F.accum(cc, cdry, ic + 1, *args, co["vz"], dt, vs, vd)
         c[ic] = cc
     F.clip(c, nx, ny, nz, nc)
     assert_same_bits(want["c"], c, "c")
     assert_same_bits(want["cdry"], cdry, "cdry")
+    assert_same_bits(want["cwet"], cwet, "cwet")
+    if wet:
+        assert np.max(want["cwet"]) > np.max(fl["cwet"])  # the step deposited
