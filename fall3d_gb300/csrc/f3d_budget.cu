@@ -385,8 +385,8 @@ __global__ void k_finddt(Dims d, int nc, double dX1, double dX2, const double* d
     const int j = (int)(r % d.ny) + 1, k = (int)(r / d.ny) + 1;
     const double ddz = fmin2(dz[k - 1], dz[k]);
     const double rz = lvl[k - 1], rzz = lvl[nz + k - 1], rden = lvl[2 * nz + k - 1];
-    const double pre = div_rn_recip(2.0 * rkh1[m], x2, rx2) + div_rn_recip(fabs(vx[m]), dX1, rx) +
-                       div_rn_recip(2.0 * rkhor[m], y2, ry2) + div_rn_recip(fabs(vy[m]), dX2, ry) +
+    const double pre = div_rn_recip(2.0 * rkh1[m], x2, rx2) + div_rn_recip(absd(vx[m]), dX1, rx) +
+                       div_rn_recip(2.0 * rkhor[m], y2, ry2) + div_rn_recip(absd(vy[m]), dX2, ry) +
                        div_rn_recip(2.0 * rkver[m], ddz * ddz, rzz);
     long long mlo, mhi;
     double den;
@@ -407,7 +407,7 @@ __global__ void k_finddt(Dims d, int nc, double dX1, double dX2, const double* d
     for (int ic = 0; ic < nc; ++ic) {
       const double* vs = vset + (long long)ic * s3;
       const double dvsetdz = div_rn_recip(vs[mhi] - vs[mlo], den, rden);
-      const double dtcni = pre + div_rn_recip(fabs((vzm + vs[m])), ddz, rz) + (fabs(dvsetdz));
+      const double dtcni = pre + div_rn_recip(absd(vzm + vs[m]), ddz, rz) + absd(dvsetdz);
       best = fmax2(best, dtcni);
     }
   }

@@ -25,8 +25,19 @@ F3D_HD T sign1(T b) { return isnan(b) ? T(1) : (signbit(b) ? T(-1) : T(1)); }
 template <class T>
 F3D_HD T fabs_t(T x) { return x < T(0) ? -x : (x == T(0) ? T(0) : x); }
 
-__device__ __forceinline__ double absd(double x) { return fabs(x); }
+// |x| and x > 0 of binary64 values on the bit patterns (integer operations;
+// the binary64 pipe is the plain form's bottleneck): clearing the sign bit
+// is fabs, NaN included; x > 0 holds exactly for the patterns of positive
+// finite values and +inf, 1 .. 0x7ff0000000000000 as signed integers.
+__device__ __forceinline__ double absd(double x) {
+  return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+}
 __device__ __forceinline__ float absd(float x) { return fabsf(x); }
+__device__ __forceinline__ bool gt0(double x) {
+  const long long b = __double_as_longlong(x);
+  return b > 0 && b <= 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool gt0(float x) { return x > 0.0f; }
 
 // RN(a/b) from y = RN(1/b) without a division (P. Markstein, "Computation
 // of elementary functions on the IBM RISC System/6000 processor", IBM J.

@@ -200,7 +200,7 @@ __global__ void k_advctzc(T* c, long long cstride, Dims d, int nz_loc, int iz_lo
       w2_n = w2_k;                             // kmin = nz
     }
     T cn;
-    if (vk_0 > T(0))
+    if (gt0(vk_0))
       cn = c_0 - w1_k - (w2_k - w2_km);
     else
       cn = c_0 - w1_n - (w2_n - w2_k);
@@ -290,7 +290,7 @@ __device__ __forceinline__ void adv_line_work(const AdvLine<T>& L, int q, int n,
 template <class T>
 __device__ __forceinline__ T adv_line_update(const AdvLine<T>& L, int q, int n, int st) {
   const T cq = L.cl[q * st], vq = L.v[q * st];
-  if (vq > T(0)) return cq - L.w1[q * st] - (L.w2[q * st] - L.w2[(q > 1 ? q - 1 : 1) * st]);
+  if (gt0(vq)) return cq - L.w1[q * st] - (L.w2[q * st] - L.w2[(q > 1 ? q - 1 : 1) * st]);
   return cq - L.w1[(q + 1) * st] - (L.w2[(q < n ? q + 1 : n) * st] - L.w2[q * st]);
 }
 
