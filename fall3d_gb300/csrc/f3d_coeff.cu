@@ -413,7 +413,10 @@ __device__ int vsettl_dev(const ClassConst& k, int model, double rhoa, double vi
       const double Q = R + 3305.0;
       const double N = fma(0.4305 * R, R, 24.0 * Q);
       cd = k.rk2 * fma(24.0 * 0.1118, P, N / (R * Q));
-      if (it > 1 && fabs(v - vold) <= eps) {
+      // |v - vold| <= eps on the magnitude bits (the same order for
+      // non-negative values; a NaN difference is above eps as in binary64)
+      const long long dvb = __double_as_longlong(v - vold) & 0x7fffffffffffffffLL;
+      if (it > 1 && dvb <= __double_as_longlong(eps)) {
         vset = T * rsqrt(cd);
         return it;
       }
