@@ -408,7 +408,10 @@ __global__ void k_finddt(Dims d, int nc, double dX1, double dX2, const double* d
       const double* vs = vset + (long long)ic * s3;
       const double dvsetdz = div_rn_recip(vs[mhi] - vs[mlo], den, rden);
       const double dtcni = pre + div_rn_recip(absd(vzm + vs[m]), ddz, rz) + absd(dvsetdz);
-      best = fmax2(best, dtcni);
+      // MAX(best, dtcni) of non-negative values (a NaN dtcni is skipped):
+      // their bit patterns order as signed integers
+      const long long db = __double_as_longlong(dtcni);
+      if (db <= 0x7ff0000000000000LL && db > __double_as_longlong(best)) best = dtcni;
     }
   }
   for (int off = 16; off > 0; off >>= 1) best = fmax2(best, __shfl_down_sync(0xffffffffu, best, off));
