@@ -313,7 +313,8 @@ int f3d_wetdep(double* c, double* cwet, const int* ic, const int* nx, const int*
   const double* dzi = m.arr(zi, (size_t)d.plane(), false);
   const double* dpr = m.arr(prate, (size_t)d.plane(), false);
   if (m.error()) return m.error();
-  launch_wetdep<double>(dc, 0, dcw, *ic - 1, d, *nz_loc, *iz_loc, *dt, ddiam, dzl, ddz, dzi, dpr, 1, 0);
+  launch_wetdep<double>(dc, 0, dcw, *ic - 1, d, *nz_loc, *iz_loc, *dt, ddiam, dzl, ddz, dzi, dpr, nullptr, 1,
+                        0);
   return m.finish();
 }
 

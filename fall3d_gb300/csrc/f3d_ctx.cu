@@ -113,7 +113,7 @@ long long footprint_bytes(const f3d_grid* g) {
     b += 4LL * (11 * s3 + s3 * nc + pl * nc + nz + 1) + 8LL * pl + nc;
   } else {
     b += 8LL * halo * nc;
-    b += 8LL * 4 * s3;  // 1/rho, rkh1*rho, rkhor*rho, diffz face coefficients
+    b += 8LL * 4 * s3 + 8LL * pl;  // 1/rho, rkh1*rho, rkhor*rho, diffz face coefficients; lambda
   }
   b += (long long)f3d::reduce_scratch_bytes(2LL * nc * (nx + ny) * nz + nc * pl, 4);
   b += (long long)f3d::setvset_scratch_bytes(Dims{g->nx, g->ny, g->nz}, g->np);
@@ -270,7 +270,7 @@ void sizloop(f3d_ctx* x) {
   if (x->g.wetdep && np > 0) {
     ProfScope ps(x, "wetdep");
     launch_wetdep<T>(c, hb, x->cwet, 0, d, nz, 1, x->dt, x->diam, x->zlayer, x->dz, x->zi, x->prate,
-                     np, s);
+                     x->lambda2d, np, s);
   }
   {
     ProfScope ps(x, "accum");
@@ -487,11 +487,11 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
     A(pkyh, hb);
     A(pkzh, hb);
     A(vkh, hb * nc);
-    A(lambda2d, pl);
     A(wet_class, nc);
   } else {
     A(c64, hb * nc);
   }
+  A(lambda2d, pl);
 #undef A
   if (!rc) {
     unsigned char* p = nullptr;
@@ -641,7 +641,7 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
   dtcn = fmax2(dtcn, 1e-13);  // finddt.f90:58-66
   x->dtc = 1.0 / dtcn;
   x->dt = g.safety_factor * x->dtc;
-  if (x->prec == F3D_PREC_FP32 && g.wetdep) {
+  if (g.wetdep) {  // the scavenging coefficient of this dt, for every class (wetdep.f90:31)
     launch_wet_lambda((long long)pl, x->dt, x->prate, x->lambda2d, s);
     CK(cudaGetLastError());
   }

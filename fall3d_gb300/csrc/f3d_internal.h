@@ -48,11 +48,12 @@ void launch_diff_coeffs(Dims d, const double* rho, const double* rkh1, const dou
                         const double* rkver, double* lr, double* pkx, double* pky, double* rksz,
                         cudaStream_t s);
 // wetdep for classes ic0..ic0+ncls-1 (0-based, all particle classes);
-// cwet points at cwet(1,1,0) and is binary64 in every form.
+// cwet points at cwet(1,1,0) and is binary64 in every form.  lam2d: the
+// scavenging coefficient of the current dt (launch_wet_lambda) or NULL.
 template <class T>
 void launch_wetdep(T* c, long long cstride, double* cwet, int ic0, Dims d, int nz_loc, int iz_loc,
                    double dt, const double* diam, const double* zlayer, const double* dz,
-                   const double* zi, const double* prate, int ncls, cudaStream_t s);
+                   const double* zi, const double* prate, const double* lam2d, int ncls, cudaStream_t s);
 // accum in binary64 (vset/vdep binary64, c widened).
 template <class T>
 void launch_accum(const T* c, long long cstride, double* cdry, int ic0, Dims d, int iz_loc,

@@ -702,7 +702,8 @@ void launch_diff_coeffs(Dims d, const double* rho, const double* rkh1, const dou
 template <class T>
 __global__ void k_wetdep(T* c, long long cstride, double* cwet, int ic0, Dims d, int nz_loc,
                          int iz_loc, double dt, const double* diam, const double* zlayer,
-                         const double* dz, const double* zi, const double* prate) {
+                         const double* dz, const double* zi, const double* prate,
+                         const double* lam2d) {
   const int ic = ic0 + blockIdx.y;  // 0-based class
   double diam_max = 100.0;
   diam_max = diam_max * 1e-6;
@@ -712,7 +713,8 @@ __global__ void k_wetdep(T* c, long long cstride, double* cwet, int ic0, Dims d,
   const int i = (int)(col % d.nx) + 1, j = (int)(col / d.nx) + 1;
   const double a = 8.4e-5, b = 0.79;
   const long long p = d.P(i, j);
-  const double lambda = fmin2(dt * a * pow(prate[p], b), 1.0);
+  // lam2d: the same lambda formed once per meteo update for all classes
+  const double lambda = lam2d ? lam2d[p] : fmin2(dt * a * pow(prate[p], b), 1.0);
   T* cc = c + (long long)blockIdx.y * cstride;
   double* cw = cwet + (long long)(ic + 1) * d.plane();
   const double z = zi[p];
@@ -731,12 +733,12 @@ __global__ void k_wetdep(T* c, long long cstride, double* cwet, int ic0, Dims d,
 template <class T>
 void launch_wetdep(T* c, long long cstride, double* cwet, int ic0, Dims d, int nz_loc, int iz_loc,
                    double dt, const double* diam, const double* zlayer, const double* dz,
-                   const double* zi, const double* prate, int ncls, cudaStream_t s) {
+                   const double* zi, const double* prate, const double* lam2d, int ncls, cudaStream_t s) {
   if (ncls <= 0) return;
   const int bs = 128;
   const long long cols = (long long)d.nx * d.ny;
   k_wetdep<T><<<dim3((unsigned)((cols + bs - 1) / bs), ncls), bs, 0, s>>>(
-      c, cstride, cwet, ic0, d, nz_loc, iz_loc, dt, diam, zlayer, dz, zi, prate);
+      c, cstride, cwet, ic0, d, nz_loc, iz_loc, dt, diam, zlayer, dz, zi, prate, lam2d);
   count_launch();
 }
 
@@ -908,7 +910,7 @@ void launch_f2d(double* dst, const float* src, long long n, cudaStream_t s) {
                                 const T*, const T*, int, cudaStream_t);                          \
   template void launch_wetdep<T>(T*, long long, double*, int, Dims, int, int, double,            \
                                  const double*, const double*, const double*, const double*,     \
-                                 const double*, int, cudaStream_t);                              \
+                                 const double*, const double*, int, cudaStream_t);               \
   template void launch_accum<T>(const T*, long long, double*, int, Dims, int, double,            \
                                 const double*, long long, const double*, long long, int,         \
                                 cudaStream_t);                                                   \
