@@ -367,10 +367,10 @@ int f3d_cmass2d(const double* c, const double* vx, const double* vy, const doubl
   const double* dvs = m.arr(vset, (size_t)d.cells() * *nc, false);
   const double* ddz = m.arr(dz, (size_t)(*nz + 1), false);
   if (m.error()) return m.error();
-  const long long nterms = 2LL * *nc_loc * (*ny + *nx) * *nz_loc + (long long)*nc_loc * d.plane();
+  const size_t part = cmass2d_scratch_bytes(d, *iz_loc, *nz_loc);
   TmpBuf tmp;
-  if (int r = tmp.alloc(reduce_scratch_bytes(nterms, 1) + 64)) return r;
-  double* dout = reinterpret_cast<double*>(reinterpret_cast<char*>(tmp.p) + reduce_scratch_bytes(nterms, 1));
+  if (int r = tmp.alloc(part + 64)) return r;
+  double* dout = reinterpret_cast<double*>(reinterpret_cast<char*>(tmp.p) + part);
   F3D_CUDA(cudaMemcpy(dout, outmass, sizeof(double), cudaMemcpyHostToDevice));
   launch_cmass2d<double>(dc, dvx, dvy, dvz, dvs, d, *ic_loc, *nc_loc, *iz_loc, *nz_loc, *dx, *dy,
                          ddz, *dt, tmp.p, dout, 0);
@@ -433,8 +433,7 @@ int f3d_cmass2d_noalloc(const double* c, const double* vx, const double* vy, con
   for (int q = 0; q < 6; ++q)
     if (int r = require_device(arrs[q], names[q])) return r;
   const Dims d = dims(*nx, *ny, *nz);
-  const long long nterms = 2LL * *nc_loc * (*ny + *nx) * *nz_loc + (long long)*nc_loc * d.plane();
-  const size_t part = reduce_scratch_bytes(nterms, 1);
+  const size_t part = cmass2d_scratch_bytes(d, *iz_loc, *nz_loc);
   if (part + sizeof(double) > (size_t)F3D_NOALLOC_SCRATCH_BYTES)
     return set_error(F3D_ERR_RANGE, "f3d_cmass2d_noalloc needs %zu scratch bytes, more than the %d available",
                      part + sizeof(double), F3D_NOALLOC_SCRATCH_BYTES);

@@ -264,6 +264,11 @@ __global__ void k_cmass2d_batch_finish(const BatchAux* tab, const DD* partial, i
   }
 }
 
+size_t cmass2d_scratch_bytes(Dims d, int iz_loc, int nz_loc) {
+  const Cm2Items it = cm2_items(d, iz_loc, nz_loc);
+  return reduce_scratch_bytes((long long)it.nT + it.nX + it.nY, 1);
+}
+
 template <class T>
 void launch_cmass2d(const T* c, const double* vx, const double* vy, const double* vz,
                     const double* vset, Dims d, int ic_loc, int nc_loc, int iz_loc, int nz_loc,

@@ -122,6 +122,9 @@ void launch_batch_advance(int* bstep, int nscen, cudaStream_t s);
 // Budget reductions.  `scratch` holds at least reduce_scratch_bytes(...)
 // bytes; results are written as binary64 to device memory `out`.
 size_t reduce_scratch_bytes(long long nterms, int nsums);
+// Scratch bytes launch_cmass2d needs: its block count follows the number of
+// face cells (class independent), so size it from the grid, not the classes.
+size_t cmass2d_scratch_bytes(Dims d, int iz_loc, int nz_loc);
 // Outflow of one step: *out = *out + sum of the terms of cmass2d.f90:42-102
 // (out is the device copy of outmass).
 template <class T>

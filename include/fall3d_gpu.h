@@ -175,11 +175,19 @@ int f3d_cmass2d(const double* c, const double* vx, const double* vy,
  *    partial before reading it and copies outmass in first.
  *  - the first call on each device looks up the array's device address
  *    (cudaGetSymbolAddress with that device current) and caches it; make
- *    that first call before any stream capture begins.
+ *    that first call before any stream capture begins.  The cached address
+ *    does not survive cudaDeviceReset (the module is loaded again at a new
+ *    address): a program that resets a device must not call this entry
+ *    point on that device afterwards.
  *  - the array is shared by all calls in the process on one device: calls
  *    that overlap in time (from several host threads) race on it and give
  *    wrong sums.  Serialise them.
- *  - the call returns when the result is in outmass (legacy default stream). */
+ *  - the call runs on the legacy default stream with synchronous copies and
+ *    returns when the result is in outmass.  The legacy default stream
+ *    waits for, and holds up, every blocking stream of the device; callers
+ *    that keep other work in flight should create those streams with
+ *    cudaStreamNonBlocking (or build with per-thread default streams) so
+ *    that this call does not serialise with them. */
 #define F3D_NOALLOC_SCRATCH_BYTES 32768
 int f3d_cmass2d_noalloc(const double* c, const double* vx, const double* vy,
                         const double* vz, const double* vset, const int* nx,
