@@ -54,3 +54,25 @@ def oracle_state(name="tiny", seed=1, steps=5, **over):
     for _ in range(steps):
         o.step()
     return s, o
+
+
+def compare_runs(o, lo, g, lg, rtol=1e-12, floor=1e-9):
+    """The FP64 context against the oracle after the same run: bit-exact
+    step counts, the time/dt sequence to 1e-14, and ``rtol`` (cells below
+    ``floor`` x max count as empty) in the budgets, the fields and the
+    outputs LOAD / COL_MASS / C_GRND.  Returns both field sets."""
+    so, sg = o.state(), g.state()
+    assert sg["iiter"] == so["iiter"]
+    assert np.array_equal(lg["iiter"], lo["iiter"])
+    for k in ("time", "dt", "dtc", "erumass"):
+        assert_close(lg[k], lo[k], 1e-14, 0.0, k)
+    for k in ("massvol", "massdep", "massdry", "outmass"):
+        assert_close(lg[k], lo[k], rtol, 0.0, k)
+    fo, fg = o.fields(), g.fields()
+    assert_close(fg["c"], fo["c"], rtol, floor, "c")
+    assert_close(fg["cdry"], fo["cdry"], rtol, floor, "cdry")
+    assert_close(fg["cwet"], fo["cwet"], rtol, floor, "cwet")
+    oo, og = o.outputs(), g.outputs()
+    for k in ("load", "col_mass", "c_grnd"):
+        assert_close(og[k], oo[k], rtol, floor, k)
+    return fo, fg

@@ -17,7 +17,7 @@ import pytest
 import fall3d_gb300 as F
 from fall3d_gb300 import synth
 import oracle_lib as O
-from helpers import assert_close, assert_same_bits
+from helpers import assert_close, assert_same_bits, compare_runs
 
 pytestmark = pytest.mark.gpu
 
@@ -33,22 +33,7 @@ def _run_both(scen, precision=F.PREC_FP64, max_steps=0):
     return o, lo, g, lg
 
 
-def _compare(o, lo, g, lg, rtol=RTOL):
-    so, sg = o.state(), g.state()
-    assert sg["iiter"] == so["iiter"]
-    assert np.array_equal(lg["iiter"], lo["iiter"])
-    for k in ("time", "dt", "dtc", "erumass"):
-        assert_close(lg[k], lo[k], 1e-14, 0.0, k)
-    for k in ("massvol", "massdep", "massdry", "outmass"):
-        assert_close(lg[k], lo[k], rtol, 0.0, k)
-    fo, fg = o.fields(), g.fields()
-    assert_close(fg["c"], fo["c"], rtol, FLOOR, "c")
-    assert_close(fg["cdry"], fo["cdry"], rtol, FLOOR, "cdry")
-    assert_close(fg["cwet"], fo["cwet"], rtol, FLOOR, "cwet")
-    oo, og = o.outputs(), g.outputs()
-    for k in ("load", "col_mass", "c_grnd"):
-        assert_close(og[k], oo[k], rtol, FLOOR, k)
-    return fo, fg
+_compare = compare_runs
 
 
 def test_tiny_run_fp64():
