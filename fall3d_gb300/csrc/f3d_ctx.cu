@@ -43,6 +43,7 @@ unsigned long long* small_dtcn(f3d_ctx* x) {
   return reinterpret_cast<unsigned long long*>(x->small + 16);
 }
 int* small_status(f3d_ctx* x) { return reinterpret_cast<int*>(x->small + 24); }
+int* small_step_status(f3d_ctx* x) { return reinterpret_cast<int*>(x->small + 26); }  // F3D_STEP_* bits
 
 template <class T>
 int dalloc(f3d_ctx* x, T** p, size_t n) {
@@ -76,8 +77,9 @@ void refresh_fp32_class(f3d_ctx* x, int ic) {
   launch_d2f(x->vset32 + ic * s3, x->vset + ic * s3, (long long)s3, s);
   launch_vk32((long long)s3, 1, x->vz32, x->vset32 + ic * s3, x->vk32 + ic * s3, s);
   const float* vs = x->vk32 + ic * s3;
-  float* vd = x->vkh + (size_t)ic * (size_t)d.halo();
-  launch_to_halo(d, 1, &vs, &vd, s);
+  const int hp = halo_pitch(d.nx);
+  float* vd = x->vkh + (size_t)ic * (size_t)hp * (d.ny + 2) * (d.nz + 2);
+  launch_to_halo(d, hp, 1, &vs, &vd, s);
 }
 }  // namespace f3d
 
@@ -111,6 +113,7 @@ long long footprint_bytes(const f3d_grid* g) {
   if (g->precision == F3D_PREC_FP32) {
     b += 2 * 4LL * halo * nc;
     b += 4LL * (11 * s3 + s3 * nc + pl * nc + nz + 1) + 8LL * pl + nc;
+    b += 4LL * (6 + nc) * f3d::halo_pitch(g->nx) * (ny + 2) * (nz + 2);  // padded halo-layout met fields
   } else {
     b += 8LL * halo * nc;
     b += 8LL * 4 * s3 + 8LL * pl;  // 1/rho, rkh1*rho, rkhor*rho, diffz face coefficients; lambda
@@ -298,7 +301,7 @@ void sizloop_fused(f3d_ctx* x) {
   {
     ProfScope ps(x, "step_fused");
     if (x->opt_tile == 3)
-      launch_step_fused2(a, s);
+      launch_step_fused2(a, x->maps2, s);
     else
       launch_step_fused(a, x->opt_tile, s);
   }
@@ -360,6 +363,9 @@ FusedArgs ctx_fused_args(f3d_ctx* x) {
   a.pkyh = x->pkyh;
   a.pkzh = x->pkzh;
   a.vkh = x->vkh;
+  a.hpitch = halo_pitch(d.nx);
+  a.hstride = (long long)a.hpitch * (d.ny + 2) * (d.nz + 2);
+  a.status = small_step_status(x);
   a.pair_aligned = (d.nx % 2 == 0) ? 1 : 0;
   return a;
 }
@@ -415,6 +421,8 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
   for (int k = 1; k < g->nz; ++k)
     if (!(g->zlayer[k] >= g->zlayer[k - 1])) x->fused_ok = 0;
   if (x->d.halo() >= (1LL << 31) || x->d.cells() >= (1LL << 31)) x->fused_ok = 0;
+  if ((long long)f3d::halo_pitch(g->nx) * (g->ny + 2) * (g->nz + 2) >= (1LL << 31)) x->fused_ok = 0;
+  if (g->nz > f3d::fused2_max_nz()) x->fused_ok = 0;  // the shape-3 kernel's per-level table
   if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete x;
     return f3d::ctx_error(F3D_ERR_CUDA, "cudaStreamCreate failed");
@@ -480,13 +488,14 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
     A(pky32, s3);
     A(pkz32, s3);
     A(vk32, s3 * nc);
-    A(vxh, hb);
-    A(vyh, hb);
-    A(lrhoh, hb);
-    A(pkxh, hb);
-    A(pkyh, hb);
-    A(pkzh, hb);
-    A(vkh, hb * nc);
+    const size_t hsz = (size_t)f3d::halo_pitch(g->nx) * (g->ny + 2) * (g->nz + 2);
+    A(vxh, hsz);
+    A(vyh, hsz);
+    A(lrhoh, hsz);
+    A(pkxh, hsz);
+    A(pkyh, hsz);
+    A(pkzh, hsz);
+    A(vkh, hsz * nc);
     A(wet_class, nc);
   } else {
     A(c64, hb * nc);
@@ -539,6 +548,9 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
       rc = f3d::ctx_error(F3D_ERR_CUDA, "upload failed");
     launch_d2f(x->dz32, x->dz, (long long)nz + 1, x->stream);
     if (cudaStreamSynchronize(x->stream) != cudaSuccess) rc = f3d::ctx_error(F3D_ERR_CUDA, "sync failed");
+    // the tensor maps of the shape-3 step kernel: the fields stay at these addresses
+    if (!rc && x->fused_ok && f3d::make_fused2_maps(f3d::ctx_fused_args(x), &x->maps2) != 0)
+      rc = f3d::ctx_error(F3D_ERR_CUDA, "cuTensorMapEncodeTiled failed for the step kernel's met fields");
   }
   if (rc) {
     f3d_ctx_destroy(x);
@@ -619,11 +631,12 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
     {  // halo-layout copies for the two-columns-per-lane kernel
       const float* src[6] = {x->vx32, x->vy32, x->lrho32, x->pkx32, x->pky32, x->pkz32};
       float* dst[6] = {x->vxh, x->vyh, x->lrhoh, x->pkxh, x->pkyh, x->pkzh};
-      launch_to_halo(d, 6, src, dst, s);
+      const int hp = halo_pitch(d.nx);
+      launch_to_halo(d, hp, 6, src, dst, s);
       for (int c = 0; c < g.nc; ++c) {
         const float* vs = x->vk32 + (size_t)c * s3;
-        float* vd = x->vkh + (size_t)c * (size_t)d.halo();
-        launch_to_halo(d, 1, &vs, &vd, s);
+        float* vd = x->vkh + (size_t)c * (size_t)hp * (d.ny + 2) * (d.nz + 2);
+        launch_to_halo(d, hp, 1, &vs, &vd, s);
       }
     }
   }
@@ -755,7 +768,7 @@ int f3d_step(f3d_ctx* x) {
 int f3d_sync(f3d_ctx* x) {
   if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
   CK(cudaStreamSynchronize(x->stream));
-  return F3D_OK;
+  return f3d::ctx_check_step_status(x);
 }
 
 int f3d_budget(f3d_ctx* x, double* massvol, double* massdep, double* massdry, double* masswet) {
@@ -1171,6 +1184,19 @@ void ctx_advance(f3d_ctx* x) {  // Fall3d.f90:112-114
   x->erumass = x->erumass + x->flowrate * x->dt;
 }
 
+// After the stream has drained: a staging wait of the step kernel that gave
+// up is an error (the status word is cleared for the next run).
+int ctx_check_step_status(f3d_ctx* x) {
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, small_step_status(x), sizeof st, cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  if (st & F3D_STEP_STAGING_TIMEOUT) {
+    CK(cudaMemsetAsync(small_step_status(x), 0, sizeof st, x->stream));
+    return f3d::ctx_error(F3D_ERR_CUDA, "step kernel: a staging copy did not arrive in time");
+  }
+  return F3D_OK;
+}
+
 int ctx_log(f3d_ctx* x, f3d_log_record* log, int log_cap, int* nlog) {
   // endstep.f90:51: mass budget every 10 minutes of simulated time
   if (x->iiter == 1 || std::fmod(x->time, 600.0) <= x->dt) {
@@ -1233,8 +1259,7 @@ int f3d_run(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, do
     if (x->time >= end_time) go_on = false;
     if (max_steps > 0 && steps >= max_steps) go_on = false;
   }
-  CK(cudaStreamSynchronize(x->stream));
-  return F3D_OK;
+  return f3d::ctx_check_step_status(x);
 }
 
 }  // extern "C"

@@ -61,6 +61,7 @@ struct f3d_ctx {
   // the fused met fields in the halo layout of c (two-columns-per-lane kernel)
   float *vxh = nullptr, *vyh = nullptr, *lrhoh = nullptr, *pkxh = nullptr, *pkyh = nullptr,
         *pkzh = nullptr, *vkh = nullptr;
+  f3d::F2Maps maps2{};  // tensor maps of those fields (shape-3 step kernel)
   double* lambda2d = nullptr;
   unsigned char* wet_class = nullptr;
   int opt_fused = 1, opt_tile = 3;
@@ -105,6 +106,7 @@ void ctx_advance(f3d_ctx* x);
 int ctx_log(f3d_ctx* x, f3d_log_record* log, int log_cap, int* nlog);
 // arguments of the fused precision-form step for the context's state
 FusedArgs ctx_fused_args(f3d_ctx* x);
+int ctx_check_step_status(f3d_ctx* x);
 inline double* ctx_outmass(f3d_ctx* x) { return x->small; }
 // gravity current (f3d_gravity.cu): addradialwind on the scaled winds of
 // a meteo update, divcorr with the budget of a log step

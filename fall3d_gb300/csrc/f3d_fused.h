@@ -1,6 +1,8 @@
 // f3d_fused.h -- arguments of the precision form's fused step kernel.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (types only; the encoder is reached through the runtime)
+
 #include "f3d_internal.h"
 
 namespace f3d {
@@ -35,20 +37,39 @@ struct FusedArgs {
   double* cdry;
   const double* vset64;  // class blocks, vstride apart
   const double* vdep64;  // class blocks of nx*ny
-  // the same binary32 fields in the halo layout of c ((nx+2)(ny+2)(nz+2),
-  // ghost entries zero), so that one offset addresses every field of a
-  // position: used by the two-columns-per-lane kernel (tile shape 3)
+  // the same binary32 fields in the halo layout of c, ghost entries zero, but
+  // with the row pitch hpitch = nx+2 rounded up to a multiple of 4 (padding
+  // zero), so that a tensor copy can stage them: used by the
+  // two-columns-per-lane kernel (tile shape 3)
   const float *vxh, *vyh, *lrhoh, *pkxh, *pkyh, *pkzh;
-  const float* vkh;  // class blocks of the halo size
+  const float* vkh;  // class blocks of hstride values
+  int hpitch;
+  long long hstride;  // hpitch * (ny+2) * (nz+2)
   int pair_aligned;  // nx even: every even column starts an 8-byte pair
+  int* status;       // device status word: F3D_STEP_STAGING_TIMEOUT is or-ed into it
 };
+
+// a staging wait of the step kernel gave up (a tensor copy did not arrive)
+#define F3D_STEP_STAGING_TIMEOUT 0x100
+
+// Tensor maps of the met fields for the shape-3 step kernel's tensor copies:
+// boxes of 68 x 32 x 1 values (x, rows, planes) of the padded halo layout.
+struct F2Maps {
+  enum { VK = 0, VX, VY, L, PZ, PX, PY, N };
+  CUtensorMap m[N];
+};
+// 0 on success
+int make_fused2_maps(const FusedArgs& a, F2Maps* out);
+// the largest nz the shape-3 kernel's shared memory holds
+int fused2_max_nz();
+inline int halo_pitch(int nx) { return (nx + 2 + 3) & ~3; }
 
 // tile region (x by y) / threads: 0 = 32x32 / 256 (default), 1 = 32x64 / 512,
 // 2 = 32x32 / 512, 3 = 64x32 / 512 with two columns per lane.
 void launch_step_fused(const FusedArgs& a, int shape, cudaStream_t s);
-void launch_step_fused2(const FusedArgs& a, cudaStream_t s);
-// met fields (nx,ny,nz) -> halo layout (ghost entries untouched)
-void launch_to_halo(Dims d, int nfield, const float* const* src, float* const* dst, cudaStream_t s);
+void launch_step_fused2(const FusedArgs& a, const F2Maps& maps, cudaStream_t s);
+// met fields (nx,ny,nz) -> halo layout of row pitch hp (ghost entries untouched)
+void launch_to_halo(Dims d, int hp, int nfield, const float* const* src, float* const* dst, cudaStream_t s);
 // tiles of one class of an nx x ny grid for a tile shape
 int fused_tiles(int nx, int ny, int shape);
 

@@ -30,6 +30,12 @@ using namespace fz;
 
 constexpr int HX = 64, HY = 32, NW = 16, NT = 32 * NW, RPW = HY / NW, TX = HX - 6, TY = HY - 6,
               NP = HX * HY;
+// The staged fields are boxes of RS x HY values: a tensor copy's first column
+// must lie on a 16-byte boundary, so a box starts at the region's first
+// column rounded down to a multiple of 4 (gx0 is even: the region then
+// starts 0 or 2 values into the box) and is 4 values wider than the region.
+constexpr int RS = HX + 4, FS = RS * HY;
+constexpr int GUARD = 512;  // bytes before the staging area (reads one row above a field)
 
 // value of the column to the left / right of each of the lane's two columns
 __device__ __forceinline__ float2 left2(float2 v) { return make_float2(shup(v.y), v.x); }
@@ -51,20 +57,55 @@ __device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cas
 __device__ __forceinline__ void sts2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
 
 size_t fused2_smem(int nz) {
-  return sizeof(float) * ((size_t)(2 * NF + 4) * NP + 2 * HX) + (2 * sizeof(double) + sizeof(int)) * TX * TY +
-         sizeof(ZT32) * (size_t)(nz + 1);
+  return 128 + GUARD + sizeof(float) * ((size_t)2 * NF * FS + 4 * (size_t)NP + HX) +
+         (2 * sizeof(double) + sizeof(int)) * TX * TY + sizeof(ZT32) * (size_t)(nz + 1) + 32;
+}
+
+// ------------------------------------------------ tensor copies (TMA)
+// Elected thread 0 stages the eight met fields of a plane with
+// cp.async.bulk.tensor into the buffer of that plane; completion is counted
+// in bytes on the buffer's mbarrier, which every thread waits on.
+__device__ __forceinline__ void mbar_init(unsigned bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// waits for the phase of the given parity, at most ~2^20 polls; false on a timeout
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (int i = 0; i < (1 << 20); ++i) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load3(unsigned dst, const CUtensorMap* map, int x, int y, int z, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
 }
 
 // One tile of one class (see fused_tile in f3d_fused.cu for the arguments).
 // P8: nx is even, so every column pair starts on an 8-byte boundary and lies
 // wholly inside or wholly outside the halo array; otherwise the pairs are
 // copied and stored one value at a time.
-template <bool P8>
-__device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_in, float* c_out, const int xfirst,
-                                            const int commit, const int cls, const int tile,
+// TMA: the met fields come by tensor copies (maps != nullptr); otherwise every
+// thread copies its own positions with cp.async.
+template <bool P8, bool TMA>
+__device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* maps, const float* c_in, float* c_out,
+                                            const int xfirst, const int commit, const int cls, const int tile,
                                             unsigned char* smem_raw) {
-  float* stage = reinterpret_cast<float*>(smem_raw) + HX;  // [2][NF][NP], after a guard row
-  float* P0s = stage + 2 * NF * NP;
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<size_t>(smem_raw) + 127) & ~(size_t)127);
+  float* stage = reinterpret_cast<float*>(base + GUARD);  // [2][NF][FS], 128-byte aligned fields
+  float* P0s = stage + 2 * NF * FS;
   float* W1s = P0s + NP;
   float* W2s = W1s + NP;
   float* P1s = W2s + NP;
@@ -72,6 +113,8 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
   double* wlam = wacc + TX * TY;
   int* wkz = reinterpret_cast<int*>(wlam + TX * TY);
   ZT32* tab = reinterpret_cast<ZT32*>(wkz + TX * TY);
+  unsigned long long* mbar = reinterpret_cast<unsigned long long*>(
+      (reinterpret_cast<size_t>(tab + (a.d.nz + 1)) + 7) & ~(size_t)7);  // one per staging buffer
 
   const Dims d = a.d;
   const int nx = d.nx, ny = d.ny, nz = d.nz;
@@ -81,11 +124,21 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
   const int oi1 = min(nx, i0 + TX - 1), oj1 = min(ny, j0 + TY - 1);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gi = gx0 + 2 * lane;  // the lane's first column; the second is gi + 1
-  const int px = nx + 2;          // halo row pitch
-  const int cs = px * (ny + 2);   // halo plane
+  const int px = nx + 2;          // halo row pitch of c
+  const int cs = px * (ny + 2);   // halo plane of c
+  const int hp = a.hpitch;        // row pitch of the met fields (padded to a multiple of 4)
+  const int hs = hp * (ny + 2);   // their plane
+  const int xs = gx0 & ~3;        // first column of the staged boxes
+  const int sft = gx0 - xs;       // the region's offset in a box row (0 or 2)
   const int pl = nx * ny;
   const bool edge = !(gx0 >= 1 && gx0 + HX - 1 <= nx && gy0 >= 1 && gy0 + HY - 1 <= ny);
 
+  const unsigned mbar0 = (unsigned)__cvta_generic_to_shared(mbar);
+  if (TMA && threadIdx.x == 0) {
+    mbar_init(mbar0);
+    mbar_init(mbar0 + 8);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   for (int k = threadIdx.x; k <= nz; k += NT) {
     ZT32 z;
     const float dzk = a.dz[k];
@@ -122,7 +175,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
 
   const float* __restrict__ cin = c_in + (long long)cls * a.cstride;
   float* __restrict__ cout = c_out + (long long)cls * a.cstride;
-  const float* __restrict__ vkc = a.vkh + (long long)cls * a.cstride;
+  const float* __restrict__ vkc = a.vkh + (long long)cls * a.hstride;
   const float dt = a.dt;
   const float dznz = 1.0f / a.dz[nz];
   const float auxvx = a.auxvx, auxvy = a.auxvy;
@@ -133,6 +186,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
   // same lane's other row
   unsigned kin = 0, kgx = 0, kgy = 0, inr = 0;  // inr: the pair of row r lies in the halo array
   int h0[RPW];                                  // halo offset of (gi, gj, plane 0), clamped
+  int m0[RPW];                                  // the same position in the met fields' layout
 #pragma unroll
   for (int r = 0; r < RPW; ++r) {
     const int gj = gy0 + 2 * warp + r;
@@ -148,6 +202,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
       if (g >= 0 && g <= nx + 1 && gj >= 0 && gj <= ny + 1) inr |= bit;
     }
     h0[r] = (inr >> (2 * r) & 1u) ? gi + px * gj : cs;  // clamped for pairs outside (plane 1 stays in range)
+    m0[r] = (inr >> (2 * r) & 1u) ? gi + hp * gj : hs;
   }
   float2 o_0[RPW], o_p1[RPW], vk0[RPW], w1k[RPW], w2km[RPW], w2k[RPW], gtop[RPW];
   float2 ra[RPW], rb[RPW], rc[RPW], fprev[RPW], gprev[RPW], pb[RPW];
@@ -156,7 +211,9 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     o_0[r] = o_p1[r] = vk0[r] = w1k[r] = w2km[r] = w2k[r] = gtop[r] = make_float2(0.0f, 0.0f);
     ra[r] = rb[r] = rc[r] = fprev[r] = gprev[r] = pb[r] = make_float2(0.0f, 0.0f);
   }
-  const unsigned sbase = (unsigned)__cvta_generic_to_shared(stage) + 4u * (unsigned)(2 * warp * HX + 2 * lane);
+  const unsigned stage0 = (unsigned)__cvta_generic_to_shared(stage);
+  const unsigned sbase = stage0 + 4u * (unsigned)(2 * warp * RS + sft + 2 * lane);
+  bool timed_out = false;
 
   // the staged inputs of iteration t into buffer t&1 (fields as in
   // f3d_fused.cu); positions outside the halo array copy nothing (zero fill)
@@ -168,41 +225,79 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
   // iteration t.
   auto prefetch = [&](auto edge_c, const int t, const int group) {
     constexpr bool EDGE = decltype(edge_c)::value;
-    const unsigned sb = sbase + 4u * (unsigned)((t & 1) * NF * NP);
+    const unsigned sb = sbase + 4u * (unsigned)((t & 1) * NF * FS);
     const bool g0 = group != 1, g1 = group != 0;
     const bool okc = g0 && t + 2 <= nz, okk = g0 && t + 1 <= nz, okv = g0 && t <= nz, okm = g1 && t <= nz,
-               okl = g1 && t >= 2;
+               okl = g1 && t >= 2 && t <= nz + 1;
+    if constexpr (TMA) {
+      if (threadIdx.x == 0) {
+        const unsigned bar = mbar0 + 8u * (unsigned)(t & 1);
+        const unsigned db = stage0 + 4u * (unsigned)((t & 1) * NF * FS);
+        // the warps' reads of this buffer (ordered before this point by a
+        // block barrier) come before the tensor copies overwrite it
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (g0) {  // the buffer's next phase: every met box of plane t, both groups
+          const unsigned n = (unsigned)((t + 1 <= nz) + 4 * (t <= nz) + 3 * (t >= 2 && t <= nz + 1));
+          if (n) mbar_expect(bar, n * (unsigned)(FS * sizeof(float)));
+        }
+        auto ld = [&](int field, int map, int z) { tma_load3(db + 4u * (unsigned)(field * FS), &maps->m[map], xs, gy0, z, bar); };
+        if (okk) ld(F_VK, F2Maps::VK, cls * (nz + 2) + t + 1);
+        if (okv) {
+          ld(F_VX, F2Maps::VX, t);
+          ld(F_VY, F2Maps::VY, t);
+        }
+        if (okm) {
+          ld(F_L, F2Maps::L, t);
+          ld(F_PZ, F2Maps::PZ, t);
+        }
+        if (okl) {
+          ld(F_L1, F2Maps::L, t - 1);
+          ld(F_PX, F2Maps::PX, t - 1);
+          ld(F_PY, F2Maps::PY, t - 1);
+        }
+      }
+    }
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
-      const unsigned dst = sb + 4u * (unsigned)(r * HX);
-      const int ht = h0[r] + t * cs;  // this row's offset at plane t
+      const unsigned dst = sb + 4u * (unsigned)(r * RS);
+      const int ht = h0[r] + t * cs;  // this row's offset at plane t (c)
+      const int hm = m0[r] + t * hs;  // and in the met fields
       const bool v0 = !EDGE || (inr >> (2 * r) & 1u), v1 = !EDGE || (inr >> (2 * r + 1) & 1u);
-      auto cp = [&](int field, const float* base, int off) {
-        const unsigned dd = dst + 4u * (unsigned)(field * NP);
+      auto cp = [&](int field, const float* src, int off) {
+        const unsigned dd = dst + 4u * (unsigned)(field * FS);
         if constexpr (P8) {
-          cp_async8(dd, base + off, v0);
+          cp_async8(dd, src + off, v0);
         } else {  // an odd nx: a pair may straddle the last ghost column
-          cp_async4s(dd, base + off, v0);
-          cp_async4s(dd + 4u, v1 ? base + off + 1 : base + off, v1);
+          cp_async4s(dd, src + off, v0);
+          cp_async4s(dd + 4u, v1 ? src + off + 1 : src + off, v1);
         }
       };
       if (okc) cp(F_C, cin, ht + 2 * cs);
-      if (okk) cp(F_VK, vkc, ht + cs);
-      if (okv) {
-        cp(F_VX, a.vxh, ht);
-        cp(F_VY, a.vyh, ht);
-      }
-      if (okm) {
-        cp(F_L, a.lrhoh, ht);
-        cp(F_PZ, a.pkzh, ht);
-      }
-      if (okl) {
-        cp(F_L1, a.lrhoh, ht - cs);
-        cp(F_PX, a.pkxh, ht - cs);
-        cp(F_PY, a.pkyh, ht - cs);
+      if constexpr (!TMA) {
+        if (okk) cp(F_VK, vkc, hm + hs);
+        if (okv) {
+          cp(F_VX, a.vxh, hm);
+          cp(F_VY, a.vyh, hm);
+        }
+        if (okm) {
+          cp(F_L, a.lrhoh, hm);
+          cp(F_PZ, a.pkzh, hm);
+        }
+        if (okl) {
+          cp(F_L1, a.lrhoh, hm - hs);
+          cp(F_PX, a.pkxh, hm - hs);
+          cp(F_PY, a.pkyh, hm - hs);
+        }
       }
     }
     cp_async_commit();
+  };
+  // all staged inputs of iteration t are in buffer t&1
+  auto staged = [&](const int t) {
+    cp_async_wait_all();
+    if constexpr (TMA) {
+      if (!mbar_wait(mbar0 + 8u * (unsigned)(t & 1), (unsigned)(((t - 1) >> 1) & 1))) timed_out = true;
+    }
   };
   if (edge)
     prefetch(True_{}, 1, 2);
@@ -220,7 +315,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
       const int g = gi + c;
       const int hb = g + px * gj, mb = (g - 1) + nx * (gj - 1);
       const float c1 = cin[hb + cs], c2 = cin[hb + 2 * cs];
-      const float vk1 = __ldg(vkc + hb + cs);
+      const float vk1 = __ldg(vkc + g + hp * gj + hs);
       float gb;
       if (vk1 >= 0.0f)
         gb = 0.0f;
@@ -249,13 +344,13 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
   auto plane = [&](auto edge_c, auto steady_c, const int t) {
     constexpr bool EDGE = decltype(edge_c)::value;
     constexpr bool STEADY = decltype(steady_c)::value;  // 3 <= t <= nz-2
-    cp_async_wait_all();
+    staged(t);
     // from iteration 3 on, the previous iteration ended with the diffy
     // barrier, after which no warp reads its advection fields
     const bool early = STEADY || (t >= 3 && t <= nz);
     if (early) prefetch(edge_c, t + 1, 0);
-    const float* sb = stage + (t & 1) * (NF * NP) + 2 * warp * HX + 2 * lane;  // this lane's row-0 position
-    auto at = [&](int field, int r) { return sb + field * NP + r * HX; };
+    const float* sb = stage + (t & 1) * (NF * FS) + 2 * warp * RS + sft + 2 * lane;  // this lane's row-0 position
+    auto at = [&](int field, int r) { return sb + field * FS + r * RS; };
     auto km = [&](int r, int c) { return (kin >> (2 * r + c) & 1u) != 0; };
     float2 s2[RPW];
     if (STEADY || t <= nz) {
@@ -282,9 +377,8 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
               const int g = gi + c;
               float gv = 0.0f;
               if (g >= 1 && g <= nx) {
-                const int hh = g + px * ja + t * cs;
-                const float cadj = cin[hh];
-                const float v = __ldg(a.vyh + hh);
+                const float cadj = cin[g + px * ja + t * cs];
+                const float v = __ldg(a.vyh + g + hp * ja + t * hs);
                 gv = (gj == 0) ? (v >= 0.0f ? 0.0f : cadj) : (v <= 0.0f ? 0.0f : cadj);
               }
               cmp(ghost, c) = gv;
@@ -378,7 +472,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
         vs[1] = lds2(at(F_VY, 1));
         const float2 cmv[RPW] = {lds2(P0 - HX), in[0]};
         const float2 cpv[RPW] = {in[1], lds2(P0 + 2 * HX)};
-        const float2 vmv[RPW] = {lds2(at(F_VY, 0) - HX), vs[0]};  // vy(i, j-1)
+        const float2 vmv[RPW] = {lds2(at(F_VY, 0) - RS), vs[0]};  // vy(i, j-1)
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
           const int gj = gy0 + 2 * warp + r;
@@ -471,7 +565,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
           const bool ok = (inr >> (2 * r + c) & 1u) != 0;
-          const int hh = ok ? gi + c + px * (gy0 + 2 * warp + r) + (nz - 1) * cs : 0;
+          const int hh = ok ? gi + c + hp * (gy0 + 2 * warp + r) + (nz - 1) * hs : 0;
           cmp(la, c) = __ldg(a.lrhoh + hh);
           cmp(pa, c) = __ldg(a.pkzh + hh);
         }
@@ -519,8 +613,8 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
     auto dif_y = [&](const float2* in, float2* out) {
       float* P1 = P1s + 2 * warp * HX + 2 * lane;
       const float2 P0v[RPW] = {lds2(at(F_PY, 0)), lds2(at(F_PY, 1))};
-      const float2 Pmv[RPW] = {lds2(at(F_PY, 0) - HX), P0v[0]};
-      const float2 Ppv[RPW] = {P0v[1], lds2(at(F_PY, 1) + HX)};
+      const float2 Pmv[RPW] = {lds2(at(F_PY, 0) - RS), P0v[0]};
+      const float2 Ppv[RPW] = {P0v[1], lds2(at(F_PY, 1) + RS)};
       if constexpr (!EDGE) {
         // neighbours read c/rho: the products c*(1/rho) of diffy.f90:34-40,
         // each computed once by its owner
@@ -547,8 +641,8 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
       __syncthreads();
       const float2 cmv[RPW] = {lds2(P1 - HX), in[0]};
       const float2 cpv[RPW] = {in[1], lds2(P1 + 2 * HX)};
-      const float2 lmv[RPW] = {lds2(at(F_L1, 0) - HX), lbv[0]};
-      const float2 lpv[RPW] = {lbv[1], lds2(at(F_L1, 1) + HX)};
+      const float2 lmv[RPW] = {lds2(at(F_L1, 0) - RS), lbv[0]};
+      const float2 lpv[RPW] = {lbv[1], lds2(at(F_L1, 1) + RS)};
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
         const float2 cm = cmv[r], cp = cpv[r];
@@ -682,13 +776,20 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const float* c_i
       a.cwet[(long long)(cls + 1) * pl + (oi - 1) + nx * (oj - 1)] = wacc[o];
     }
   }
+  if constexpr (TMA) {
+    if (timed_out) {  // a tensor copy did not arrive in time: report, and let copies in flight land
+      atomicOr(a.status, F3D_STEP_STAGING_TIMEOUT);
+      mbar_wait(mbar0 + 8u * (unsigned)(nz & 1), (unsigned)(((nz - 1) >> 1) & 1));
+      mbar_wait(mbar0 + 8u * (unsigned)((nz + 1) & 1), (unsigned)((nz >> 1) & 1));
+    }
+  }
 }
 
 template <bool P8>
-__global__ void __launch_bounds__(NT, 1) k_step_fused2(const FusedArgs a) {
+__global__ void __launch_bounds__(NT, 1) k_step_fused2(const FusedArgs a, const __grid_constant__ F2Maps maps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  fused2_tile<P8>(a, a.c_in, a.c_out, a.xfirst, 1, (int)(blockIdx.x % a.ncls), (int)(blockIdx.x / a.ncls),
-                  smem_raw);
+  fused2_tile<P8, true>(a, &maps, a.c_in, a.c_out, a.xfirst, 1, (int)(blockIdx.x % a.ncls),
+                        (int)(blockIdx.x / a.ncls), smem_raw);
 }
 
 // Batched form (see k_step_fused_batch in f3d_fused.cu).  The scenarios with
@@ -721,35 +822,84 @@ __global__ void __launch_bounds__(NT, 1)
     const float* cin = (bs & 1) ? a.c_out : a.c_in;
     float* cout = (bs & 1) ? const_cast<float*>(a.c_in) : a.c_out;
     const int iiter = iiter0[lo] + bs + 1;
-    fused2_tile<P8>(a, cin, cout, (iiter % 2 == 0) ? 1 : 0, commit, local % a.ncls, local / a.ncls, smem_raw);
+    fused2_tile<P8, false>(a, nullptr, cin, cout, (iiter % 2 == 0) ? 1 : 0, commit, local % a.ncls, local / a.ncls,
+                           smem_raw);
   }
 }
 
-// met field (nx,ny,nz) -> halo layout
-__global__ void k_to_halo(Dims d, const float* src, float* dst) {
+// met field (nx,ny,nz) -> halo layout with row pitch hp
+__global__ void k_to_halo(Dims d, int hp, const float* src, float* dst) {
   const long long s3 = d.cells();
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < s3;
        m += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(m % d.nx) + 1;
     const long long r = m / d.nx;
     const int j = (int)(r % d.ny) + 1, k = (int)(r / d.ny) + 1;
-    dst[d.C(i, j, k)] = src[m];
+    dst[i + (long long)hp * (j + (long long)(d.ny + 2) * k)] = src[m];
   }
 }
 
 }  // namespace
 
-void launch_step_fused2(const FusedArgs& a, cudaStream_t s) {
+void launch_step_fused2(const FusedArgs& a, const F2Maps& maps, cudaStream_t s) {
   const int tiles = ((a.d.nx + TX - 1) / TX) * ((a.d.ny + TY - 1) / TY);
   const size_t sm = fused2_smem(a.d.nz);
   if (a.pair_aligned) {
     cudaFuncSetAttribute(k_step_fused2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_step_fused2<true><<<tiles * a.ncls, NT, sm, s>>>(a);
+    k_step_fused2<true><<<tiles * a.ncls, NT, sm, s>>>(a, maps);
   } else {
     cudaFuncSetAttribute(k_step_fused2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_step_fused2<false><<<tiles * a.ncls, NT, sm, s>>>(a);
+    k_step_fused2<false><<<tiles * a.ncls, NT, sm, s>>>(a, maps);
   }
   count_launch();
+}
+
+int fused2_max_nz() {
+  const size_t cap = (size_t)227 * 1024, base = fused2_smem(0);
+  return cap > base ? (int)((cap - base) / sizeof(ZT32)) - 1 : 0;
+}
+
+// cuTensorMapEncodeTiled, reached through the runtime's driver entry point
+// (no link against the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int make_fused2_maps(const FusedArgs& a, F2Maps* out) {
+  static EncodeTiledFn enc = nullptr;
+  if (!enc) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return 1;
+    enc = reinterpret_cast<EncodeTiledFn>(fn);
+  }
+  const Dims d = a.d;
+  if (a.hpitch % 4 != 0 || a.hpitch < d.nx + 2) return 2;
+  // x (the padded row), y (rows 0..ny+1), z (planes 0..nz+1, times the classes for vz+vset)
+  auto one = [&](CUtensorMap* m, const float* p, long long planes) {
+    const cuuint64_t dim[3] = {(cuuint64_t)a.hpitch, (cuuint64_t)(d.ny + 2), (cuuint64_t)planes};
+    const cuuint64_t stride[2] = {(cuuint64_t)a.hpitch * sizeof(float),
+                                  (cuuint64_t)a.hpitch * (d.ny + 2) * sizeof(float)};
+    const cuuint32_t box[3] = {(cuuint32_t)RS, (cuuint32_t)HY, 1u};
+    const cuuint32_t es[3] = {1u, 1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(p), dim, stride, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
+               ? 0
+               : 3;
+  };
+  const long long np = d.nz + 2;
+  int rc = one(&out->m[F2Maps::VK], a.vkh, np * a.ncls);
+  if (!rc) rc = one(&out->m[F2Maps::VX], a.vxh, np);
+  if (!rc) rc = one(&out->m[F2Maps::VY], a.vyh, np);
+  if (!rc) rc = one(&out->m[F2Maps::L], a.lrhoh, np);
+  if (!rc) rc = one(&out->m[F2Maps::PZ], a.pkzh, np);
+  if (!rc) rc = one(&out->m[F2Maps::PX], a.pkxh, np);
+  if (!rc) rc = one(&out->m[F2Maps::PY], a.pkyh, np);
+  return rc;
 }
 
 int upload_batch_args2(const FusedArgs* h, int n, cudaStream_t s) {
@@ -788,10 +938,10 @@ void launch_step_fused2_batch(int grid, const int* item_off, int nscen, int spli
   }
 }
 
-void launch_to_halo(Dims d, int nfield, const float* const* src, float* const* dst, cudaStream_t s) {
+void launch_to_halo(Dims d, int hp, int nfield, const float* const* src, float* const* dst, cudaStream_t s) {
   const int nb = (int)std::min<long long>((d.cells() + 255) / 256, 152LL * 16);
   for (int f = 0; f < nfield; ++f) {
-    k_to_halo<<<nb, 256, 0, s>>>(d, src[f], dst[f]);
+    k_to_halo<<<nb, 256, 0, s>>>(d, hp, src[f], dst[f]);
     count_launch();
   }
 }

@@ -567,7 +567,10 @@ int f3d_profile_read(f3d_ctx* ctx, int cap, char* names, int name_len,
 /* Number of CUDA kernels this library launched since load (diagnostic). */
 long long f3d_kernel_launches(void);
 
-/* Synchronise the context's stream. */
+/* Synchronise the context's stream.  Returns F3D_ERR_CUDA if a staging wait
+ * of the step kernel gave up since the last check (a tensor copy that did not
+ * arrive within its bounded wait; the kernel then continues without hanging
+ * and its results are not to be used); f3d_run checks the same at its end. */
 int f3d_sync(f3d_ctx* ctx);
 
 /* ------------------------------------------------------------------------
