@@ -68,6 +68,8 @@ struct f3d_batch {
   // pinned staging of the tables
   BatchAux* h_aux = nullptr;
   FusedArgs* h_args = nullptr;
+  F2Maps* h_maps = nullptr;  // the scenarios' tensor maps (shape 3), batch order
+  F2Maps* d_maps = nullptr;
   int *h_item_off = nullptr, *h_bstep = nullptr, *h_iiter0 = nullptr;
   // graph of one step
   cudaGraphExec_t exec = nullptr;
@@ -103,6 +105,7 @@ int table_rebuild(f3d_batch* b) {
     a.c_in = s.c_a;
     a.c_out = s.c_b;
     b->h_args[q] = a;
+    b->h_maps[q] = x->maps2;
     BatchAux& u = b->h_aux[q];
     u = BatchAux{};
     u.c_a = s.c_a;
@@ -143,6 +146,7 @@ int table_rebuild(f3d_batch* b) {
   if (n > 0) {
     if (upload_batch_args(b->h_args, n, b->stream)) return ctx_error(F3D_ERR_CUDA, "constant table upload failed");
     BK(cudaMemcpyAsync(b->d_aux, b->h_aux, sizeof(BatchAux) * n, cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(b->d_maps, b->h_maps, sizeof(F2Maps) * n, cudaMemcpyHostToDevice, b->stream));
     BK(cudaMemcpyAsync(b->d_bstep, b->h_bstep, sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
     BK(cudaMemcpyAsync(b->d_iiter0, b->h_iiter0, sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
   }
@@ -158,7 +162,7 @@ int enqueue_step(f3d_batch* b, int commit_only_fused) {
   BK(cudaMemsetAsync(b->d_counter, 0, 2 * sizeof(int), b->stream));
   if (!commit_only_fused) launch_setsrc_batch(b->d_aux, b->d_bstep, n, b->max_nc, b->max_nsou, b->stream);
   launch_step_fused_batch(b->shape, b->grid, b->d_item_off, n, b->split, b->total, b->d_counter, b->d_bstep,
-                          b->d_iiter0, commit_only_fused ? 0 : 1, b->max_nz, b->stream);
+                          b->d_iiter0, commit_only_fused ? 0 : 1, b->max_nz, b->d_maps, b->stream);
   if (!commit_only_fused) {
     launch_cmass2d_batch(b->d_aux, b->d_bstep, n, b->d_red, b->stream);
     launch_batch_advance(b->d_bstep, n, b->stream);
@@ -224,6 +228,8 @@ int f3d_batch_create(int max_scenarios, f3d_batch** out) {
   ok = ok && cudaMalloc(&b->d_red, cmass2d_batch_scratch_bytes(n)) == cudaSuccess;
   ok = ok && cudaMallocHost(&b->h_aux, sizeof(BatchAux) * n) == cudaSuccess;
   ok = ok && cudaMallocHost(&b->h_args, sizeof(FusedArgs) * n) == cudaSuccess;
+  ok = ok && cudaMallocHost(&b->h_maps, sizeof(F2Maps) * n) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_maps, sizeof(F2Maps) * n) == cudaSuccess;
   ok = ok && cudaMallocHost(&b->h_item_off, sizeof(int) * (n + 1)) == cudaSuccess;
   ok = ok && cudaMallocHost(&b->h_bstep, sizeof(int) * n) == cudaSuccess;
   ok = ok && cudaMallocHost(&b->h_iiter0, sizeof(int) * n) == cudaSuccess;
@@ -248,6 +254,8 @@ int f3d_batch_destroy(f3d_batch* b) {
   cudaFree(b->d_red);
   cudaFreeHost(b->h_aux);
   cudaFreeHost(b->h_args);
+  cudaFreeHost(b->h_maps);
+  cudaFree(b->d_maps);
   cudaFreeHost(b->h_item_off);
   cudaFreeHost(b->h_bstep);
   cudaFreeHost(b->h_iiter0);

@@ -794,10 +794,10 @@ int fused_batch_grid(int shape, int max_nz) {
 
 void launch_step_fused_batch(int shape, int grid, const int* item_off, int nscen, int split, int total,
                              int* counter, const int* bstep, const int* iiter0, int commit, int max_nz,
-                             cudaStream_t s) {
+                             const F2Maps* maps, cudaStream_t s) {
   switch (shape) {
     case 3:
-      launch_step_fused2_batch(grid, item_off, nscen, split, total, counter, bstep, iiter0, commit, max_nz, s);
+      launch_step_fused2_batch(grid, item_off, nscen, split, total, counter, bstep, iiter0, commit, max_nz, maps, s);
       break;
     case 1:
       launch_fused_batch_t<64, 16>(grid, item_off, nscen, counter, bstep, iiter0, commit, max_nz, s);

@@ -81,14 +81,16 @@ int upload_batch_args(const FusedArgs* h, int n, cudaStream_t s);
 int upload_batch_args2(const FusedArgs* h, int n, cudaStream_t s);  // the shape-3 kernel's table
 int fused2_batch_grid(int max_nz);
 // items [0, split) belong to scenarios with an even nx (two counters)
+// maps: the scenarios' tensor maps (device array in batch order)
 void launch_step_fused2_batch(int grid, const int* item_off, int nscen, int split, int total, int* counter,
-                              const int* bstep, const int* iiter0, int commit, int max_nz, cudaStream_t s);
+                              const int* bstep, const int* iiter0, int commit, int max_nz, const F2Maps* maps,
+                              cudaStream_t s);
 // sets the kernel's shared-memory limit and returns its persistent grid (-1 on error)
 int fused_batch_grid(int shape, int max_nz);
 // counter: two ints; split / total: see launch_step_fused2_batch (shape 3)
 void launch_step_fused_batch(int shape, int grid, const int* item_off, int nscen, int split, int total,
                              int* counter, const int* bstep, const int* iiter0, int commit, int max_nz,
-                             cudaStream_t s);
+                             const F2Maps* maps, cudaStream_t s);
 void launch_vk32(long long n, int nc, const float* vz, const float* vset, float* vk, cudaStream_t s);
 void launch_wet_lambda(long long n, double dt, const double* prate, double* lam, cudaStream_t s);
 void launch_fp32_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,

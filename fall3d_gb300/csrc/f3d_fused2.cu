@@ -97,9 +97,9 @@ __device__ __forceinline__ void tma_load3(unsigned dst, const CUtensorMap* map, 
 // P8: nx is even, so every column pair starts on an 8-byte boundary and lies
 // wholly inside or wholly outside the halo array; otherwise the pairs are
 // copied and stored one value at a time.
-// TMA: the met fields come by tensor copies (maps != nullptr); otherwise every
-// thread copies its own positions with cp.async.
-template <bool P8, bool TMA>
+// The met fields come by tensor copies (maps: this scenario's tensor maps),
+// c by every thread's own cp.async copies.
+template <bool P8>
 __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* maps, const float* c_in, float* c_out,
                                             const int xfirst, const int commit, const int cls, const int tile,
                                             unsigned char* smem_raw) {
@@ -134,7 +134,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
   const bool edge = !(gx0 >= 1 && gx0 + HX - 1 <= nx && gy0 >= 1 && gy0 + HY - 1 <= ny);
 
   const unsigned mbar0 = (unsigned)__cvta_generic_to_shared(mbar);
-  if (TMA && threadIdx.x == 0) {
+  if (threadIdx.x == 0) {
     mbar_init(mbar0);
     mbar_init(mbar0 + 8);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -186,7 +186,6 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
   // same lane's other row
   unsigned kin = 0, kgx = 0, kgy = 0, inr = 0;  // inr: the pair of row r lies in the halo array
   int h0[RPW];                                  // halo offset of (gi, gj, plane 0), clamped
-  int m0[RPW];                                  // the same position in the met fields' layout
 #pragma unroll
   for (int r = 0; r < RPW; ++r) {
     const int gj = gy0 + 2 * warp + r;
@@ -202,7 +201,6 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
       if (g >= 0 && g <= nx + 1 && gj >= 0 && gj <= ny + 1) inr |= bit;
     }
     h0[r] = (inr >> (2 * r) & 1u) ? gi + px * gj : cs;  // clamped for pairs outside (plane 1 stays in range)
-    m0[r] = (inr >> (2 * r) & 1u) ? gi + hp * gj : hs;
   }
   float2 o_0[RPW], o_p1[RPW], vk0[RPW], w1k[RPW], w2km[RPW], w2k[RPW], gtop[RPW];
   float2 ra[RPW], rb[RPW], rc[RPW], fprev[RPW], gprev[RPW], pb[RPW];
@@ -216,20 +214,21 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
   bool timed_out = false;
 
   // the staged inputs of iteration t into buffer t&1 (fields as in
-  // f3d_fused.cu); positions outside the halo array copy nothing (zero fill)
-  // group 0: the fields the advection phases read (c, vz+vset, vx, vy);
-  // group 1: those the diffusion phases read (1/rho, K*rho); 2: both.
-  // Group 0 of iteration t+1 is issued as iteration t starts where every
-  // warp has passed the last barrier of iteration t-1 (after which nobody
-  // reads those fields of that buffer), group 1 after the first barrier of
-  // iteration t.
+  // f3d_fused.cu): c by each thread for its own positions (positions outside
+  // the halo array copy nothing: zero fill), the met boxes by thread 0's
+  // tensor copies (outside the arrays: zero fill).  Group 0: the fields the
+  // advection phases read (c, vz+vset, vx, vy); group 1: those the diffusion
+  // phases read (1/rho, K*rho); 2: both.  Group 0 of iteration t+1 is issued
+  // as iteration t starts where every warp has passed the last barrier of
+  // iteration t-1 (after which nobody reads those fields of that buffer),
+  // group 1 after the first barrier of iteration t.
   auto prefetch = [&](auto edge_c, const int t, const int group) {
     constexpr bool EDGE = decltype(edge_c)::value;
     const unsigned sb = sbase + 4u * (unsigned)((t & 1) * NF * FS);
     const bool g0 = group != 1, g1 = group != 0;
     const bool okc = g0 && t + 2 <= nz, okk = g0 && t + 1 <= nz, okv = g0 && t <= nz, okm = g1 && t <= nz,
                okl = g1 && t >= 2 && t <= nz + 1;
-    if constexpr (TMA) {
+    {
       if (threadIdx.x == 0) {
         const unsigned bar = mbar0 + 8u * (unsigned)(t & 1);
         const unsigned db = stage0 + 4u * (unsigned)((t & 1) * NF * FS);
@@ -261,11 +260,11 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
     for (int r = 0; r < RPW; ++r) {
       const unsigned dst = sb + 4u * (unsigned)(r * RS);
       const int ht = h0[r] + t * cs;  // this row's offset at plane t (c)
-      const int hm = m0[r] + t * hs;  // and in the met fields
       const bool v0 = !EDGE || (inr >> (2 * r) & 1u), v1 = !EDGE || (inr >> (2 * r + 1) & 1u);
       auto cp = [&](int field, const float* src, int off) {
         const unsigned dd = dst + 4u * (unsigned)(field * FS);
         if constexpr (P8) {
+          (void)v1;
           cp_async8(dd, src + off, v0);
         } else {  // an odd nx: a pair may straddle the last ghost column
           cp_async4s(dd, src + off, v0);
@@ -273,31 +272,13 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
         }
       };
       if (okc) cp(F_C, cin, ht + 2 * cs);
-      if constexpr (!TMA) {
-        if (okk) cp(F_VK, vkc, hm + hs);
-        if (okv) {
-          cp(F_VX, a.vxh, hm);
-          cp(F_VY, a.vyh, hm);
-        }
-        if (okm) {
-          cp(F_L, a.lrhoh, hm);
-          cp(F_PZ, a.pkzh, hm);
-        }
-        if (okl) {
-          cp(F_L1, a.lrhoh, hm - hs);
-          cp(F_PX, a.pkxh, hm - hs);
-          cp(F_PY, a.pkyh, hm - hs);
-        }
-      }
     }
     cp_async_commit();
   };
   // all staged inputs of iteration t are in buffer t&1
   auto staged = [&](const int t) {
     cp_async_wait_all();
-    if constexpr (TMA) {
-      if (!mbar_wait(mbar0 + 8u * (unsigned)(t & 1), (unsigned)(((t - 1) >> 1) & 1))) timed_out = true;
-    }
+    if (!mbar_wait(mbar0 + 8u * (unsigned)(t & 1), (unsigned)(((t - 1) >> 1) & 1))) timed_out = true;
   };
   if (edge)
     prefetch(True_{}, 1, 2);
@@ -776,11 +757,16 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
       a.cwet[(long long)(cls + 1) * pl + (oi - 1) + nx * (oj - 1)] = wacc[o];
     }
   }
-  if constexpr (TMA) {
+  {
     if (timed_out) {  // a tensor copy did not arrive in time: report, and let copies in flight land
       atomicOr(a.status, F3D_STEP_STAGING_TIMEOUT);
       mbar_wait(mbar0 + 8u * (unsigned)(nz & 1), (unsigned)(((nz - 1) >> 1) & 1));
       mbar_wait(mbar0 + 8u * (unsigned)((nz + 1) & 1), (unsigned)((nz >> 1) & 1));
+    }
+    __syncthreads();  // nobody waits on the barriers any more: they may be reused (next batch item)
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(mbar0) : "memory");
+      asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(mbar0 + 8) : "memory");
     }
   }
 }
@@ -788,7 +774,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
 template <bool P8>
 __global__ void __launch_bounds__(NT, 1) k_step_fused2(const FusedArgs a, const __grid_constant__ F2Maps maps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  fused2_tile<P8, true>(a, &maps, a.c_in, a.c_out, a.xfirst, 1, (int)(blockIdx.x % a.ncls),
+  fused2_tile<P8>(a, &maps, a.c_in, a.c_out, a.xfirst, 1, (int)(blockIdx.x % a.ncls),
                         (int)(blockIdx.x / a.ncls), smem_raw);
 }
 
@@ -801,7 +787,8 @@ static_assert(sizeof(FusedArgs) * F3D_BATCH_MAX <= 48 * 1024, "batch argument ta
 template <bool P8>
 __global__ void __launch_bounds__(NT, 1)
     k_step_fused2_batch(const int* __restrict__ item_off, int nscen, int begin, int end, int* counter,
-                        const int* __restrict__ bstep, const int* __restrict__ iiter0, int commit) {
+                        const int* __restrict__ bstep, const int* __restrict__ iiter0, int commit,
+                        const F2Maps* __restrict__ maps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   for (;;) {
@@ -822,8 +809,8 @@ __global__ void __launch_bounds__(NT, 1)
     const float* cin = (bs & 1) ? a.c_out : a.c_in;
     float* cout = (bs & 1) ? const_cast<float*>(a.c_in) : a.c_out;
     const int iiter = iiter0[lo] + bs + 1;
-    fused2_tile<P8, false>(a, nullptr, cin, cout, (iiter % 2 == 0) ? 1 : 0, commit, local % a.ncls, local / a.ncls,
-                           smem_raw);
+    fused2_tile<P8>(a, maps + lo, cin, cout, (iiter % 2 == 0) ? 1 : 0, commit, local % a.ncls,
+                          local / a.ncls, smem_raw);
   }
 }
 
@@ -925,15 +912,16 @@ int fused2_batch_grid(int max_nz) {
 }
 
 void launch_step_fused2_batch(int grid, const int* item_off, int nscen, int split, int total, int* counter,
-                              const int* bstep, const int* iiter0, int commit, int max_nz, cudaStream_t s) {
+                              const int* bstep, const int* iiter0, int commit, int max_nz, const F2Maps* maps,
+                              cudaStream_t s) {
   const size_t sm = fused2_smem(max_nz);
   if (split > 0) {
-    k_step_fused2_batch<true><<<grid, NT, sm, s>>>(item_off, nscen, 0, split, counter, bstep, iiter0, commit);
+    k_step_fused2_batch<true><<<grid, NT, sm, s>>>(item_off, nscen, 0, split, counter, bstep, iiter0, commit, maps);
     count_launch();
   }
   if (total > split) {
     k_step_fused2_batch<false><<<grid, NT, sm, s>>>(item_off, nscen, split, total, counter + 1, bstep, iiter0,
-                                                     commit);
+                                                     commit, maps);
     count_launch();
   }
 }
