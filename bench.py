@@ -33,6 +33,7 @@ of the workload with no collective ("scaling": "weak").
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -342,15 +343,23 @@ def run_ours(args, rank, world, local_rank):
         alg_bytes = bpc * cells
         avg_ms = dom_ms / dom_n
         achieved = alg_bytes / (avg_ms / 1e3) / 1e9
-        traffic = None
+        # DRAM bytes of one launch from the committed ncu capture, valid only
+        # while the kernel's source is the one that was captured
+        traffic, traffic_note = None, "no capture"
         tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
         if os.path.exists(tpath):
             try:
-                traffic = json.load(open(tpath)).get(WORKLOAD, {}).get(dom_name)
+                rec = json.load(open(tpath)).get(WORKLOAD, {})
+                src = os.path.join(ROOT, "fall3d_gb300", "csrc", "f3d_fused2.cu")
+                sha = hashlib.sha256(open(src, "rb").read()).hexdigest()
+                if rec.get("kernel_sha256") == sha:
+                    traffic, traffic_note = rec.get(dom_name), "ncu capture of this kernel source"
+                else:
+                    traffic_note = "stale: the kernel source changed since the capture"
             except Exception:
                 traffic = None
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "kernel": dom_name,
+                "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_note, "kernel": dom_name,
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
                 "peak_source": f"{peak_kind} hbm_gbs"}
     step_bytes = 12 + 28 / nc  # binary32 algorithmic bytes per cell-class-step
