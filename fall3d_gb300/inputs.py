@@ -23,11 +23,9 @@ host.
   around each column point, linear between the two model levels).
 * ``scenario_from_files``: a Scenario for fall3d_gb300.Context from an .inp,
   a .grn and a .src file (grid from the .inp GRID block as reagrd.f90 derives
-  it from the DBS properties, meteorology from fall3d_gb300.synth).
-
-The netCDF DBS reader (libMaster/get_dbs_*.f90) is not restated: the
-image has no netCDF library, and the met series is an array argument of
-f3d_run.
+  it from the DBS properties), with the meteorology of a DBS file
+  (fall3d_gb300.dbs, libMaster/get_dbs_value_plane.f90 and reamet.f90) or
+  synthetic (fall3d_gb300.synth).
 """
 from __future__ import annotations
 
@@ -432,12 +430,14 @@ def src_interval(src, t1, t2, xorigr, yorigr, dx, dy, zmodel):
 # ------------------------------------------------------------------ scenario
 
 
-def scenario_from_files(inp_path: str, grn_path: str, src_path: str, seed: int = 0, **met_over):
+def scenario_from_files(inp_path: str, grn_path: str, src_path: str, seed: int = 0, dbs_path: str = None,
+                        **met_over):
     """A Scenario for fall3d_gb300.Context from the reference's input
     files: grid from the .inp GRID block (LON-LAT: LONMIN..LATMAX, NX, NY,
     ZLAYER_(M)), classes from the .grn file, sources from the .src file,
-    run window from TIME_UTC; meteorology synthetic (fall3d_gb300.synth,
-    as the image has no netCDF DBS reader)."""
+    run window from TIME_UTC; meteorology from the DBS file ``dbs_path``
+    (fall3d_gb300.dbs.read_dbs on the grid's levels, Sources/reamet.f90), or
+    synthetic (fall3d_gb300.synth) when none is given."""
     from fall3d_gb300 import synth
 
     inp = read_inp(inp_path)
@@ -474,4 +474,12 @@ def scenario_from_files(inp_path: str, grn_path: str, src_path: str, seed: int =
     s.src = {k: srcd[k] for k in ("t1", "t2", "nsou", "isrc", "jsrc", "ksrc", "tmrat")}
     s.info["zs"] = list(srcd["zs"])
     s.info["fc"] = grn["fc"]
+    if dbs_path is not None:
+        from fall3d_gb300 import dbs
+
+        met, warnings = dbs.read_dbs(dbs_path, zl, wetdep=bool(g["wetdep"]))
+        if met["u"].shape[2:] != (ny, nx):
+            raise ValueError("the DBS grid differs from the .inp GRID block")
+        s.met = met
+        s.info["dbs_warnings"] = warnings
     return s

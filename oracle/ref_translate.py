@@ -2,13 +2,24 @@
 
 TEST INFRASTRUCTURE ONLY.  There is no Fortran compiler in this environment,
 so this recipe translates the reference's Fortran 90 source files, as they
-lie under /root/reference/Sources, mechanically into C and compiles that C
+lie in the reference's Sources/ and libMaster/ directories (the reference's
+root is F3D_REFERENCE_ROOT, or --reference DIR, and defaults to a directory
+named "reference" beside this repository), mechanically into C and compiles that C
 with gcc (-O2 -ffp-contract=off).  Only the generated C and the library go
 to oracle/_ref/ (git-ignored); nothing of the reference is copied into the
 repository.  The result is used to generate the golden vectors of
 tests/golden/ that pin the CPU oracle (oracle/f3d_oracle.cpp).
 
-    python oracle/ref_translate.py   -> oracle/_ref/libf3dref.so
+    python oracle/ref_translate.py [--reference DIR] [--force]   -> oracle/_ref/libf3dref.so
+
+One routine is rewritten at the source level before its translation:
+libMaster/get_dbs_value_plane.f90 keeps its own statements for the time
+interval and the vertical interpolation, while its netCDF calls (nf90_open,
+nf90_inq_varid, nf90_get_var, nf90_close, get_dbs_property_int) become calls
+of small C accessors (dbs_nt, dbs_nz, dbs_time, dbs_alt, dbs_plane) that
+serve a database registered from memory (ref_dbs_set), and its word
+dictionary and message strings are dropped (the caller passes the case the
+dictionary would select).
 
 The translator covers the Fortran subset of the transport path: modules
 with declarations (scalars, explicit-shape and allocatable arrays, SAVE and
@@ -41,7 +52,10 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF = "/root/reference/Sources"
+REF_ROOT = os.environ.get("F3D_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
+REF = os.path.join(REF_ROOT, "Sources")
+DBS_PLANE_FILE = os.path.join("..", "libMaster", "get_dbs_value_plane.f90")  # relative to Sources/
 
 MODULE_FILES = ["KindType.f90", "Numeric.f90", "Master.f90", "InpOut.f90"]
 UNIT_FILES = ["setbcc.f90", "advctzc.f90", "advctx.f90", "advcty.f90", "diffz.f90", "diffx.f90",
@@ -72,6 +86,85 @@ RUNTIME_DECLS = {
 
 class TranslateError(Exception):
     pass
+
+
+# C accessors standing in for the netCDF calls of get_dbs_value_plane
+# (name -> arguments as (name, ctype, is_array))
+EXTERN_PROTOS = {
+    "dbs_nt": [("nt", "int", False)],
+    "dbs_nz": [("nz", "int", False)],
+    "dbs_time": [("time", "int", True)],
+    "dbs_alt": [("alt", "double", True)],
+    "dbs_plane": [("var", "double", True), ("ialt", "int", False), ("itime", "int", False)],
+}
+EXTERN_C = r"""
+/* an in-memory DBS for the rewritten get_dbs_value_plane: data is
+   (nt, nz, ny, nx) binary32 for a 3-D word, (nt, ny, nx) or (ny, nx) for 2-D */
+static struct { int nt, nz, nx, ny, rank; const int* time; const float* alt; const float* data; } dbs_mem;
+void ref_dbs_set(int nt, int nz, int nx, int ny, int rank, const int* time, const float* alt,
+                 const float* data) {
+  dbs_mem.nt = nt; dbs_mem.nz = nz; dbs_mem.nx = nx; dbs_mem.ny = ny; dbs_mem.rank = rank;
+  dbs_mem.time = time; dbs_mem.alt = alt; dbs_mem.data = data;
+}
+void f90_dbs_nt(int* v) { *v = dbs_mem.nt; }
+void f90_dbs_nz(int* v) { *v = dbs_mem.nz; }
+void f90_dbs_time(int* t) { for (int i = 0; i < dbs_mem.nt; ++i) t[i] = dbs_mem.time[i]; }
+void f90_dbs_alt(double* a) { for (int i = 0; i < dbs_mem.nz; ++i) a[i] = (double)dbs_mem.alt[i]; }
+void f90_dbs_plane(double* v, int* ialt, int* itime) {
+  const size_t pl = (size_t)dbs_mem.nx * dbs_mem.ny;
+  const float* p = dbs_mem.data;
+  if (dbs_mem.rank == 1) p += (size_t)(*itime - 1) * pl;
+  if (dbs_mem.rank == 2) p += ((size_t)(*itime - 1) * dbs_mem.nz + (size_t)(*ialt - 1)) * pl;
+  for (size_t i = 0; i < pl; ++i) v[i] = (double)p[i];
+}
+"""
+
+
+def rewrite_dbs_plane(lines):
+    """libMaster/get_dbs_value_plane.f90 with its netCDF calls replaced by
+    the C accessors of EXTERN_PROTOS, its word dictionary and message strings
+    dropped, and the dictionary's case (varcase) taken as the first argument."""
+    out, skip_dict = [], False
+    for label, st in lines:
+        low = st.strip()
+        if low.startswith("subroutine get_dbs_value_plane"):
+            out.append((label, "subroutine get_dbs_value_plane(varcase,timesec,z,nx,ny,var,endsec,istat)"))
+            continue
+        if low.startswith("use netcdf") or re.match(r"^character\b", low):
+            continue
+        if low.startswith("if(word(") or low.startswith("if (word("):
+            skip_dict = True
+        if skip_dict:
+            if re.match(r"^end\s*if$", low):
+                skip_dict = False
+            continue
+        if low.startswith("ilen =") or low.startswith("message(") or low.startswith("mymessage"):
+            continue
+        m = re.match(r"^call get_dbs_property_int\(fname,'(nt|nz)',(\w+),istat,message\)$", low, re.I)
+        if m:
+            out.append((label, f"call dbs_{m.group(1).lower()}({m.group(2)})"))
+            continue
+        if "nf90_open" in low or "nf90_inq_varid" in low or "nf90_close" in low:
+            if label:  # keep a goto target
+                out.append((label, "continue"))
+            continue
+        m = re.match(r"^if\s*\(\s*nf90_get_var\(ncid,(\w+),(\w+)(?:,start=\(/(.*)/\))?\)\s*/=\s*0\s*\)\s*goto\s+\d+$", low)
+        if m:
+            src, dst, start = m.group(1), m.group(2), m.group(3)
+            if src == "timeid":
+                out.append((label, f"call dbs_time({dst})"))
+            elif src == "altid":
+                out.append((label, f"call dbs_alt({dst})"))
+            else:
+                idx = [x.strip() for x in start.split(",")]
+                ialt = idx[2] if len(idx) == 4 else "0"
+                itime = idx[-1] if len(idx) >= 3 else "0"
+                out.append((label, f"call dbs_plane({dst},{ialt},{itime})"))
+            continue
+        if "nf90_" in low:
+            raise TranslateError(f"unhandled netCDF statement in get_dbs_value_plane: {st}")
+        out.append((label, st))
+    return out
 
 
 # ------------------------------------------------------------------ lexing
@@ -1280,6 +1373,9 @@ static void f90_runend(const char* m) { fprintf(stderr, "translated reference: %
 def translate(ref_dir=REF) -> str:
     g = Gen()
     g.out.append(RUNTIME_C)
+    g.out.append(EXTERN_C)
+    for name, args in EXTERN_PROTOS.items():
+        g.protos[name] = list(args)
     # serial runtime of Parallel/Domain
     for name, (ty, val) in RUNTIME_DECLS.items():
         g.globals[name] = Sym(name, ty, module="runtime")
@@ -1295,6 +1391,9 @@ def translate(ref_dir=REF) -> str:
         text = open(os.path.join(ref_dir, f), encoding="latin-1").read()
         mods, units = split_units(logical_lines(text), f)
         all_units += [u for u in units if u.name in WANTED]
+    text = open(os.path.join(ref_dir, DBS_PLANE_FILE), encoding="latin-1").read()
+    mods, units = split_units(rewrite_dbs_plane(logical_lines(text)), "get_dbs_value_plane.f90")
+    all_units += [u for u in units if u.name == "get_dbs_value_plane"]
     for u in all_units:
         g.unit_syms = {}
         g.proto(u)
@@ -1326,4 +1425,8 @@ def build(force=False, ref_dir=REF) -> str:
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv))
+    args = sys.argv[1:]
+    ref = REF
+    if "--reference" in args:
+        ref = os.path.join(args[args.index("--reference") + 1], "Sources")
+    print(build(force="--force" in args, ref_dir=ref))

@@ -3,8 +3,8 @@ Fortran source.
 
     python tests/golden/make_golden.py
 
-oracle/ref_translate.py translates the reference's hot-path Fortran (under
-/root/reference/Sources) into C and compiles it into oracle/_ref/.  This
+oracle/ref_translate.py translates the reference's hot-path Fortran (its
+Sources/ directory) into C and compiles it into oracle/_ref/.  This
 script drives that library through the time loop of Sources/Fall3d.f90:73-121
 on seeded synthetic scenarios and stores its state (concentrations, deposits,
 the mass-budget log, the coefficient fields after the first meteo update) as
