@@ -550,10 +550,31 @@ def split_units(lines, fname):
                 i += 1
             units.append(u)
         elif m_fun:
-            # skip functions (none needed); consume to end function
+            # a function: a unit whose result variable is declared from its header
+            hdr = re.match(r"^(real\s*(?:\([^)]*\))?|integer\s*(?:\([^)]*\))?|logical)?\s*function\s+(\w+)\s*\((.*)\)$", low)
+            if not hdr or not hdr.group(1):
+                raise TranslateError(f"unsupported function header: {low}")
+            u = Unit("fun", hdr.group(2), [a.strip() for a in hdr.group(3).split(",") if a.strip()])
+            u.module = cur_mod.name if cur_mod else None
+            u.decls.append(f"{hdr.group(1)} :: {hdr.group(2)}")
             i += 1
-            while i < len(lines) and not re.match(r"^end\s*function", lines[i][1].strip()):
+            depth_decl = True
+            while i < len(lines):
+                lb, s2 = lines[i]
+                l2 = s2.strip()
+                if re.match(r"^end\s*function", l2) or (l2 == "end"):
+                    break
+                if depth_decl and is_decl(l2):
+                    if l2.startswith("use "):
+                        u.uses.append(l2[4:].split(",")[0].strip())
+                    else:
+                        u.decls.append(l2)
+                else:
+                    if l2 not in ("implicit none",):
+                        depth_decl = False
+                        u.body.append((lb, l2))
                 i += 1
+            units.append(u)
         elif cur_mod and not in_contains:
             if low.startswith("use "):
                 cur_mod.uses.append(low[4:].split(",")[0].strip())
@@ -574,6 +595,7 @@ class Gen:
         self.globals = {}   # name -> Sym
         self.unit_syms = {}
         self.protos = {}
+        self.funcs = {}  # user function -> result ctype
         self.out = []
         self.tmp = 0
 
@@ -788,6 +810,14 @@ class Gen:
         return f"_t{self.tmp}"
 
     def intrinsic(self, name, args, elem):
+        if name in self.funcs:  # a user function: arguments by reference
+            out = []
+            for a, (pname, ptype, parr) in zip(args, self.protos[name]):
+                t, ty = self.e(a, elem)
+                tmp = self.newtmp()
+                self.pre.append(f"{ptype} {tmp} = {self.cast(t, ty, ptype)};")
+                out.append(f"&{tmp}")
+            return f"f90_{name}({', '.join(out)})", self.funcs[name]
         if name == "sum":
             return self.reduce_sum(args[0])
         if name in ("maxval", "minval"):
@@ -1207,7 +1237,8 @@ class Gen:
         for a in u.args:
             s = syms[a]
             params.append(f"{'char' if s.ctype == 'char' else s.ctype}* {s.c}")
-        body = [f"void f90_{u.name}({', '.join(params) if params else 'void'}) {{"]
+        rtype = syms[u.name].ctype if u.kind == "fun" else "void"
+        body = [f"{rtype} f90_{u.name}({', '.join(params) if params else 'void'}) {{"]
         # locals
         for name, s in syms.items():
             if s.is_arg:
@@ -1259,6 +1290,8 @@ class Gen:
                 raise TranslateError(f"{u.name}: {e}")
             body.extend("  " + ln for ln in lines)
         body.append("  L_end:;")
+        if u.kind == "fun":
+            body.append(f"  return {syms[u.name].c};")
         body.append("}")
         self.out.extend(body)
 
@@ -1394,18 +1427,74 @@ def translate(ref_dir=REF) -> str:
     text = open(os.path.join(ref_dir, DBS_PLANE_FILE), encoding="latin-1").read()
     mods, units = split_units(rewrite_dbs_plane(logical_lines(text)), "get_dbs_value_plane.f90")
     all_units += [u for u in units if u.name == "get_dbs_value_plane"]
+    emit_units(g, all_units)
+    return "\n".join(g.out) + "\n"
+
+
+def emit_units(g, all_units):
     for u in all_units:
         g.unit_syms = {}
-        g.proto(u)
+        syms = g.proto(u)
+        if u.kind == "fun":
+            g.funcs[u.name] = syms[u.name].ctype
     # prototypes
     for u in all_units:
         params = []
         for a, ty, arr in g.protos[u.name]:
             params.append(f"{ty}* v_{a}")
-        g.out.append(f"void f90_{u.name}({', '.join(params) if params else 'void'});")
+        rtype = g.funcs.get(u.name, "void") if u.kind == "fun" else "void"
+        g.out.append(f"{rtype} f90_{u.name}({', '.join(params) if params else 'void'});")
     for u in all_units:
         g.emit_unit(u)
+
+
+# The pre-processing utilities whose generators the input layer restates:
+# each is a program of its own with its own Master module, so each becomes a
+# library of its own.  name -> (directory under Utilities/, module files,
+# unit files, wanted units)
+UTILITIES = {
+    "settgsd": ("SetTgsd", ["KindType.f90", "Master.f90"], ["setfrac.f90"],
+                {"setfrac", "m0_fi_gaussian", "fer", "getmem"}),
+    "setsrc": ("SetSrc", ["KindType.f90", "Master.f90"], ["solvesuzuki.f90", "getsrc.f90"],
+               {"solvesuzuki", "getsrc", "getshape"}),
+}
+
+
+def translate_utility(name, ref_root=REF_ROOT) -> str:
+    sub, module_files, unit_files, wanted = UTILITIES[name]
+    d = os.path.join(ref_root, "Utilities", sub)
+    g = Gen()
+    g.out.append(RUNTIME_C)
+    for rname, (ty, val) in RUNTIME_DECLS.items():
+        g.globals[rname] = Sym(rname, ty, module="runtime")
+        g.out.append(f"{ty} m_{rname} = {val};")
+    all_units = []
+    for f in module_files:
+        text = open(os.path.join(d, f), encoding="latin-1").read()
+        mods, units = split_units(logical_lines(text), f)
+        for m in mods:
+            g.emit_module_vars(m)
+        all_units += [u for u in units if u.name in wanted]
+    for f in unit_files:
+        text = open(os.path.join(d, f), encoding="latin-1").read()
+        mods, units = split_units(logical_lines(text), f)
+        all_units += [u for u in units if u.name in wanted]
+    emit_units(g, all_units)
     return "\n".join(g.out) + "\n"
+
+
+def build_utility(name, force=False, ref_root=REF_ROOT) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    lib = os.path.join(OUT, f"lib{name}.so")
+    if os.path.exists(lib) and not force:
+        return lib
+    csrc = os.path.join(OUT, f"{name}.c")
+    with open(csrc, "w") as f:
+        f.write(translate_utility(name, ref_root))
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=gnu11",
+           "-w", "-o", lib, csrc, "-lm"]
+    subprocess.run(cmd, check=True)
+    return lib
 
 
 def build(force=False, ref_dir=REF) -> str:
@@ -1430,3 +1519,6 @@ if __name__ == "__main__":
     if "--reference" in args:
         ref = os.path.join(args[args.index("--reference") + 1], "Sources")
     print(build(force="--force" in args, ref_dir=ref))
+    root = os.path.dirname(ref)
+    for name in UTILITIES:
+        print(build_utility(name, force="--force" in args, ref_root=root))
