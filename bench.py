@@ -19,14 +19,17 @@ setbcc, advection, diffusion, wet and dry deposition, clip, cmass2d).
 ``forms``    the plain binary64 form on the same workload; the batched form
              (64 ensemble members, nx, ny ~ U[64,320], nz ~ U[20,60], 4-20
              classes, one persistent launch per batch step, 30 timed batch
-             steps); the served form on a bounded sample of the Poisson
-             request stream (p50/p99 latency, beside the same requests run
-             one after another in the FP64 form).
+             steps, beside the same members run alone one after another);
+             the served form on a bounded sample of the Poisson request
+             stream (p50/p99 latency, beside the same requests run to their
+             end one after another in the FP64 form).
 ``accuracy_vs_fp64``  relative L2 / Linf error of every output of the
              precision form against the FP64 form over the e2e window, and
              the mass drift |massvol+massdep+outmass-erumass|/erumass.
-``--impl reference`` times the CPU oracle (the restatement of the reference's
-Fortran path; the Fortran itself cannot be built here) on all host cores.
+``--impl reference`` times the reference's own Fortran path (translated to C
+by oracle/ref_translate.py, oracle/_ref) on the host cores, one process per
+class group as in its MPI class decomposition, with a serial (1 core)
+sample beside it; the CPU oracle port stands in where no translation exists.
 Multi-GPU: classes and scenarios are independent, so N GPUs run N replicas
 of the workload with no collective ("scaling": "weak").
 """
@@ -132,7 +135,9 @@ def kernel_bytes_per_cell_class(S, nc):
 
 def cpu_baseline(threads, steps=2):
     """The CPU oracle on this host's cores on a bounded sample: one meteo
-    update (timed separately) then ``steps`` full steps of the workload."""
+    update (timed separately), ``steps`` full steps of the workload on all
+    cores (OpenMP over classes), then one step on one core (the serial
+    build's rate)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
 
@@ -147,45 +152,94 @@ def cpu_baseline(threads, steps=2):
     for _ in range(steps):
         o.step()
     t = time.perf_counter() - t0
+    o.set_threads(1)
+    t0 = time.perf_counter()
+    o.step()
+    t1 = time.perf_counter() - t0
     units = s.cell_classes * steps
     o.close()
     return {"value": units / t, "unit": METRIC, "cores": threads, "kind": "port",
             "sample": f"{WORKLOAD} 400x300x50x16: {steps} full steps after one meteo update "
                       f"(meteo update {t_met:.1f} s, not in the rate); oracle -O2 -ffp-contract=off, "
-                      f"OpenMP over classes"}
+                      f"OpenMP over classes",
+            "serial_1core": {"value": s.cell_classes / t1, "unit": METRIC, "cores": 1,
+                             "sample": "one full step on one core after the sample above"}}
+
+
+def _reference_lib():
+    """The translated reference (oracle/_ref), built if needed; None with the
+    reason when it cannot be."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    try:
+        import ref_translate
+
+        ref_translate.build()
+        return True, None
+    except Exception as e:  # no sources and no translation: the port stands in
+        return False, str(e).splitlines()[0] if str(e) else type(e).__name__
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU path on the host cores.  With the translated
+    reference available (the reference's own Fortran, oracle/_ref): one
+    process per class group as in the reference's MPI class decomposition,
+    after the serial set-up and a serial sample; otherwise the CPU oracle
+    port with OpenMP over classes."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib
-
     s = _scenario(max_snapshots=2)
-    o = oracle_lib.OracleCtx(s, nthreads=threads)
-    o.source(0)
-    o.meteo(0)
-    for _ in range(args.warmup):
-        o.step()
-    done = 0
-    t0 = time.perf_counter()
-    while done < args.steps:
-        o.step()
-        done += 1
-        if time.perf_counter() - t0 > 150.0:
-            break
-    t = time.perf_counter() - t0
-    v = s.cell_classes * done / t
+    nc = s.grid["nc"]
+    ok, why = _reference_lib()
+    extra = {}
+    if ok:
+        import ref_driver
+
+        ngrp = max(1, min(threads, nc))
+        r = ref_driver.time_class_parallel(s, ngrp, args.steps, serial_steps=2, budget_s=45.0)
+        par, ser = r["parallel"], r["serial"]
+        done, t = par["steps"], par["seconds"]
+        v = par["cell_class_steps"] / t
+        kind, cores = "reference", ngrp
+        form = (f"the reference's own Fortran (translated to C, gcc -O2 -ffp-contract=off), "
+                f"{ngrp} processes over class groups (Sources/Parallel.F90 localdim/globalindex)")
+        sample = (f"{done} steps of {WORKLOAD} per class group, all groups started together, after one "
+                  f"untimed step; set-up: the serial meteo update ({r['meteo_s']:.1f} s, not in the rate)")
+        extra["serial_1core"] = {"value": ser["cell_class_steps"] / ser["seconds"], "unit": METRIC, "cores": 1,
+                                 "steps": ser["steps"], "seconds": ser["seconds"],
+                                 "sample": "full steps over every class in one process (the serial build)"}
+        extra["meteo_update_s"] = r["meteo_s"]
+    else:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+
+        o = oracle_lib.OracleCtx(s, nthreads=threads)
+        o.source(0)
+        o.meteo(0)
+        for _ in range(args.warmup):
+            o.step()
+        done = 0
+        t0 = time.perf_counter()
+        while done < args.steps:
+            o.step()
+            done += 1
+            if time.perf_counter() - t0 > 150.0:
+                break
+        t = time.perf_counter() - t0
+        o.close()
+        v = s.cell_classes * done / t
+        kind, cores = "port", threads
+        form = "CPU oracle (binary64), OpenMP over classes, all host cores"
+        sample = f"{done} full steps of {WORKLOAD} after one meteo update"
+        extra["reference_unavailable"] = why
     line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world, "steps": done,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / done, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "grid": [400, 300, 50], "classes": 16,
-                       "form": "CPU oracle (binary64), all host cores"},
-            "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
-                             "sample": f"{done} full steps of {WORKLOAD} after one meteo update"},
+            "config": {"workload": WORKLOAD, "grid": [400, 300, 50], "classes": nc, "form": form},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line.update(extra)
     print(json.dumps(line), flush=True)
 
 
@@ -350,8 +404,8 @@ def run_ours(args, rank, world, local_rank):
         if os.path.exists(tpath):
             try:
                 rec = json.load(open(tpath)).get(WORKLOAD, {})
-                src = os.path.join(ROOT, "fall3d_gb300", "csrc", "f3d_fused2.cu")
-                sha = hashlib.sha256(open(src, "rb").read()).hexdigest()
+                kpath = os.path.join(ROOT, "fall3d_gb300", "csrc", "f3d_fused2.cu")
+                sha = hashlib.sha256(open(kpath, "rb").read()).hexdigest()
                 if rec.get("kernel_sha256") == sha:
                     traffic, traffic_note = rec.get(dom_name), "ncu capture of this kernel source"
                 else:
@@ -414,14 +468,19 @@ def run_ours(args, rank, world, local_rank):
         from fall3d_gb300 import serve
 
         try:
-            line["forms"]["fp32_batched"] = serve.ensemble(members=64, steps=30)
-            line["forms"]["fp32_batched"]["over_fp64_plain"] = line["forms"]["fp32_batched"]["value"] / value64
+            fb = serve.ensemble(members=64, steps=30)
+            fb["over_fp64_plain"] = fb["value"] / value64
+            alone = serve.ensemble_alone(members=64, steps=10)
+            fb["members_alone"] = alone
+            fb["over_members_alone"] = fb["value"] / alone["value"]
+            line["forms"]["fp32_batched"] = fb
         except Exception as e:
             line["forms"]["fp32_batched"] = {"error": str(e)}
         try:
             sv = serve.serving(rate=2.0, window=10.0, dmin=0.3, dmax=4.8, met_dt_h=1.0)
             sv["sample"] = ("Poisson 2 req/s for 10 s, ensemble-member requests with durations "
-                            "U(0.3, 4.8) h (one tenth of the serving config's 3-48 h), hourly met")
+                            "U(0.3, 4.8) h (one tenth of the serving config's 3-48 h), hourly met; "
+                            "the FP64 baseline runs every request to its end, one after another")
             line["forms"]["served"] = sv
         except Exception as e:
             line["forms"]["served"] = {"error": str(e)}

@@ -7,10 +7,9 @@ serving    forecast requests (each an ensemble member with a duration
            U[dmin, dmax] h) arriving as a Poisson stream, submitted to the
            continuous-batching server (f3d_server_*) at their arrival times
            under an HBM admission cap; p50/p99 latency (arrival to result)
-           and throughput, beside the latencies the same requests would see
-           run one after another in the plain FP64 form (service times from
-           the FP64 form's step and meteo-update rates measured here on a
-           sample of the requests).
+           and throughput, beside the latencies of the same requests run
+           one after another in the plain FP64 form (each run to its end and
+           timed; a FIFO of the measured service times on the same arrivals).
 
     python -m fall3d_gb300.serve ensemble [--members 64] [--steps 40]
     python -m fall3d_gb300.serve serving [--rate 2] [--window 600] [--cap-gb 150]
@@ -60,32 +59,57 @@ def ensemble(members=64, steps=40, run_h=12.0, seed=0, tune=True, warm=3):
     return out
 
 
-def _fp64_rates(scens, steps=3):
-    """Plain FP64 form on a few requests: (cell-class-steps/s of the step,
-    seconds per meteo update per cell-class)."""
-    step_rates, met_costs = [], []
-    for s in scens:
-        g = F.Context(s, F.PREC_FP64)
+def ensemble_alone(members=64, steps=40, run_h=12.0, seed=0, warm=3):
+    """The members of ``ensemble`` each alone in its own context, one after
+    another (``warm`` steps, then ``steps`` timed steps each): the
+    single-context rate on the batch's work, cell-class-steps/s."""
+    import torch
+
+    cc_total, t_total = 0, 0.0
+    for i in range(members):
+        s = synth.ensemble_member(seed + i, run_h=run_h, max_snapshots=2)
+        g = F.Context(s, F.PREC_FP32)
         g.source(0)
-        t0 = time.perf_counter()
         g.meteo(0)
+        for _ in range(warm):
+            g.step()
         g.sync()
-        t_met = time.perf_counter() - t0
-        g.step(1)
-        g.sync()
-        t0 = time.perf_counter()
-        g.step(steps)
-        g.sync()
-        t = time.perf_counter() - t0
-        cc = s.grid["nx"] * s.grid["ny"] * s.grid["nz"] * s.grid["nc"]
-        step_rates.append(cc * steps / t)
-        met_costs.append(t_met / cc)
+        ext = torch.cuda.ExternalStream(g.stream_handle())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(steps):
+            g.step()
+        e1.record(ext)
+        e1.synchronize()
+        t_total += e0.elapsed_time(e1) / 1e3
+        cc_total += s.grid["nx"] * s.grid["ny"] * s.grid["nz"] * s.grid["nc"] * steps
         g.close()
-    return float(np.mean(step_rates)), float(np.mean(met_costs))
+    return dict(members=members, steps=steps, seconds=t_total, value=cc_total / t_total)
+
+
+def fp64_sequential(scens, arrivals):
+    """The same requests one after another in the plain FP64 form: each is
+    run to its end (context creation, f3d_run with its meteorology and
+    sources, the deposit maps read back) and timed; a single FIFO server
+    then gives request i the latency finish_i - arrival_i with finish_i =
+    max(finish_{i-1}, arrival_i) + service_i."""
+    service = []
+    for s in scens:
+        t0 = time.perf_counter()
+        g = F.Context(s, F.PREC_FP64)
+        g.run()
+        g.outputs()
+        g.close()
+        service.append(time.perf_counter() - t0)
+    fin, lat = 0.0, []
+    for a, sv in zip(arrivals, service):
+        fin = max(fin, a) + sv
+        lat.append(fin - a)
+    return np.array(service), np.array(lat), fin
 
 
 def serving(rate=2.0, window=600.0, cap_gb=150.0, dmin=3.0, dmax=48.0, met_dt_h=12.0, seed=0,
-            max_running=128, steps_per_poll=2, fp64_sample=2):
+            max_running=128, steps_per_poll=2, fp64=True):
     rng = np.random.default_rng(seed)
     arrivals = []
     t = 0.0
@@ -121,31 +145,23 @@ def serving(rate=2.0, window=600.0, cap_gb=150.0, dmin=3.0, dmax=48.0, met_dt_h=
     lat = np.array([p["t_done"] - (t0 + a) for p, a in zip(polls, arrivals)])
     makespan = max(p["t_done"] for p in polls) - t0
     st = srv.stats()
-    steps = np.array([p["steps"] for p in polls])
-    cc = np.array([s.grid["nx"] * s.grid["ny"] * s.grid["nz"] * s.grid["nc"] for s in scen], dtype=float)
     srv.close()
-    # the same requests one after another in the plain FP64 form
-    r_step, met_cost = _fp64_rates(scen[:fp64_sample])
-    n_met = np.array([len([x for x in s.met["times"] if x < s.end_time]) for s in scen])
-    service = cc * steps / r_step + n_met * cc * met_cost
-    fin, seq_lat = 0.0, []
-    for a, sv in zip(arrivals, service):
-        fin = max(fin, a) + sv
-        seq_lat.append(fin - a)
-    seq_lat = np.array(seq_lat)
-    return dict(
+    out = dict(
         requests=n, failed=len(failed), rate_per_s=rate, window_s=window, cap_gb=cap_gb,
         duration_h=[dmin, dmax], met_interval_h=met_dt_h,
         p50_latency_s=float(np.percentile(lat, 50)), p99_latency_s=float(np.percentile(lat, 99)),
         mean_latency_s=float(lat.mean()), makespan_s=float(makespan),
         value=float(st["cell_class_steps"] / makespan), cell_class_steps=float(st["cell_class_steps"]),
-        peak_running=peak_running, peak_hbm_gb=peak_used / 1e9,
-        fp64_sequential=dict(p50_latency_s=float(np.percentile(seq_lat, 50)),
-                             p99_latency_s=float(np.percentile(seq_lat, 99)),
-                             makespan_s=float(max(fin, 0.0)), step_rate=r_step,
-                             meteo_s_per_cell_class=met_cost, sampled_requests=fp64_sample,
-                             note="service times from the FP64 form's rates measured on the sampled "
-                                  "requests; same step counts as served"))
+        peak_running=peak_running, peak_hbm_gb=peak_used / 1e9)
+    if fp64:
+        # the same requests one after another in the plain FP64 form, run and timed
+        service, seq_lat, seq_makespan = fp64_sequential(scen, arrivals)
+        out["fp64_sequential"] = dict(
+            p50_latency_s=float(np.percentile(seq_lat, 50)), p99_latency_s=float(np.percentile(seq_lat, 99)),
+            makespan_s=float(seq_makespan), service_s_total=float(service.sum()), requests_run=len(service),
+            note="every request run to its end in the FP64 form, one after another; latency from the "
+                 "measured service times and the same arrivals")
+    return out
 
 
 def main():

@@ -1371,6 +1371,9 @@ orc_ctx* orc_ctx_create(const f3d_grid* g, int nthreads) {
 
 void orc_ctx_destroy(orc_ctx* x) { delete x; }
 
+/* Threads of the class loop of later steps (1 = the serial build). */
+void orc_ctx_set_threads(orc_ctx* x, int nthreads) { x->nthreads = nthreads > 0 ? nthreads : 1; }
+
 /* gfortran MAX/MIN of two reals (see the header) */
 static double orc_fmin2(double a, double b) { return (b < a || std::isnan(a)) ? b : a; }
 

@@ -8,7 +8,10 @@ named "reference" beside this repository), mechanically into C and compiles that
 with gcc (-O2 -ffp-contract=off).  Only the generated C and the library go
 to oracle/_ref/ (git-ignored); nothing of the reference is copied into the
 repository.  The result is used to generate the golden vectors of
-tests/golden/ that pin the CPU oracle (oracle/f3d_oracle.cpp).
+tests/golden/ that pin the CPU oracle (oracle/f3d_oracle.cpp), and bench.py
+times it as the reference's CPU path.  On a host without the sources (the
+oracle/_ref/ folder copied there, its library left behind) ``build``
+compiles the translation already in oracle/_ref/.
 
     python oracle/ref_translate.py [--reference DIR] [--force]   -> oracle/_ref/libf3dref.so
 
@@ -1502,11 +1505,13 @@ def build(force=False, ref_dir=REF) -> str:
     lib = os.path.join(OUT, "libf3dref.so")
     if os.path.exists(lib) and not force:
         return lib
-    if not os.path.isdir(ref_dir):
-        raise FileNotFoundError(f"reference sources not found at {ref_dir}")
     csrc = os.path.join(OUT, "f3dref.c")
-    with open(csrc, "w") as f:
-        f.write(translate(ref_dir))
+    if os.path.isdir(ref_dir):
+        with open(csrc, "w") as f:
+            f.write(translate(ref_dir))
+    elif not os.path.exists(csrc):
+        raise FileNotFoundError(f"reference sources not found at {ref_dir} and no translation in {OUT}")
+    # else: compile the translation made where the sources were mounted
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=gnu11",
            "-w", "-o", lib, csrc, "-lm"]
     subprocess.run(cmd, check=True)

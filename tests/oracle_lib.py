@@ -69,6 +69,7 @@ def load():
         "orc_out_con": [DP, I, I, I, I, I, DP, DP, DP, I, DP],
         "orc_ctx_create": [VP, I],
         "orc_ctx_destroy": [VP],
+        "orc_ctx_set_threads": [VP, I],
         "orc_meteo": [VP] + [DP] * 12,
         "orc_source": [VP, I, IP, IP, IP, DP],
         "orc_step": [VP],
@@ -202,6 +203,10 @@ class OracleCtx:
 
     def __del__(self):
         self.close()
+
+    def set_threads(self, nthreads):
+        """Threads of the class loop of the following steps."""
+        self.lib.orc_ctx_set_threads(self.h, int(nthreads))
 
     def set_gravity_current(self, params=None):
         if params is None:

@@ -27,7 +27,7 @@ import pytest
 import fall3d_gb300 as F
 from fall3d_gb300 import synth
 import oracle_lib as O
-from helpers import compare_runs
+from helpers import assert_close, compare_runs
 
 pytestmark = pytest.mark.gpu
 
@@ -65,3 +65,44 @@ def test_stress_class_set_fp64_slice():
     o, lo, g, lg = _run_both(s, None, 12)
     compare_runs(o, lo, g, lg)
     assert np.array_equal(g.iters(), o.iters())
+
+
+def test_reference_size_full_run_against_the_reference():
+    """The CPU-runnable workload (80x80x25 at 0.05 deg, 6 classes, 3 h: 550
+    steps, three meteo updates, the eruption's end) run in full by the plain
+    FP64 form and compared with the reference's own run of it
+    (tests/golden/cfg0_full_run.npz, the translated Fortran): bit-exact step
+    count, time and dt sequences to 1e-14, the mass-budget log and every
+    sampled concentration, ground deposit and the outputs to 1e-12.  The
+    precision form takes the same steps, and its LOAD and COL_MASS are within
+    1e-4 of the FP64 form's."""
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    gold = np.load(os.path.join(here, "cfg0_full_run.npz"))
+    stride = int(gold["sample_stride"])
+    s = synth.make_scenario("cfg0", seed=0)
+    g = F.Context(s, F.PREC_FP64)
+    lg = g.run()
+    st = g.state()
+    assert st["iiter"] == int(gold["iiter"]) == 550
+    assert np.array_equal(lg["iiter"], gold["log_iiter"].astype(lg["iiter"].dtype))
+    for k in ("time", "dt", "dtc", "erumass"):
+        assert_close(lg[k], gold["log_" + k], 1e-14, 0.0, k)
+    for k in ("massvol", "massdep", "massdry", "masswet", "outmass"):
+        assert_close(lg[k], gold["log_" + k], 1e-12, 0.0, k)
+    f = g.fields()
+    assert_close(f["c"].ravel()[::stride], gold["c"].ravel(), 1e-12, 1e-9, "c")
+    assert_close(f["cdry"], gold["cdry"], 1e-12, 1e-9, "cdry")
+    assert_close(f["cwet"], gold["cwet"], 1e-12, 1e-9, "cwet")
+    assert_close(np.array([st["outmass"]]), np.array([float(gold["outmass"])]), 1e-12, 0.0, "outmass")
+    # the reference scheme's own budget closure over the run, reproduced
+    eru = lg["erumass"][-1]
+    closure = (lg["massvol"][-1] + lg["massdep"][-1] + lg["outmass"][-1] - eru) / eru
+    gclosure = (gold["log_massvol"][-1] + gold["log_massdep"][-1] + gold["log_outmass"][-1] - eru) / eru
+    assert abs(closure - gclosure) <= 1e-10
+    out64 = g.outputs()
+    g32 = F.Context(s, F.PREC_FP32)
+    l32 = g32.run()
+    assert g32.state()["iiter"] == 550 and np.array_equal(l32["dt"], lg["dt"])
+    out32 = g32.outputs()
+    for k in ("load", "col_mass"):
+        assert_close(out32[k], out64[k], 1e-4, 1e-9, k)
