@@ -27,7 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfall3d_gb300.so")
 
 PREC_FP64, PREC_FP32 = 64, 32
-OPT_FUSED, OPT_TILE, OPT_GRAPH = 1, 2, 3
+OPT_FUSED, OPT_TILE, OPT_GRAPH, OPT_PREFETCH = 1, 2, 3, 4
 # output variables of printres_nc.f90 (f3d_output)
 (OUT_LOAD, OUT_WET, OUT_THICK, OUT_COL_MASS, OUT_PM_COL, OUT_C_GRND, OUT_PM_GRND, OUT_AOT05,
  OUT_CON, OUT_WIND, OUT_MAGGR) = range(1, 12)

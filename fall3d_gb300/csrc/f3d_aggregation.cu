@@ -297,6 +297,7 @@ extern "C" {
 
 int f3d_set_aggregation(f3d_ctx* x, const f3d_aggregation* ag) {
   if (!x) return ctx_error(F3D_ERR_ARG, "NULL context");
+  ctx_prefetch_drop(x);  // a look-ahead meteo update does not run the aggregation model
   if (!ag) {
     x->agr_on = 0;
     return F3D_OK;

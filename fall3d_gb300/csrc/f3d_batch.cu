@@ -273,6 +273,7 @@ int f3d_batch_add(f3d_batch* b, f3d_ctx* x, const f3d_met_series* met, const f3d
     return ctx_error(F3D_ERR_ARG, "batched contexts must be precision-form (FP32) contexts of the fused step");
   if (x->gc_on) return ctx_error(F3D_ERR_ARG, "the gravity current is not supported in a batch");
   if (x->agr_on) return ctx_error(F3D_ERR_ARG, "aggregation is not supported in a batch");
+  ctx_prefetch_drop(x);  // the batch makes each update when it is due
   if (met->nt < 1) return ctx_error(F3D_ERR_ARG, "no meteorological snapshot");
   int id = -1;
   for (int q = 0; q < b->cap; ++q) {

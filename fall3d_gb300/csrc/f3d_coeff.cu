@@ -519,15 +519,13 @@ __device__ void chain_run(const ChainGeom& g, long long q0, long long q1, int mo
   }
 }
 
-__global__ void k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, const double* visc,
-                                 const double2* cf, const double* rho, double* vset, int* iters,
-                                 const double* cd_state, double* entry, double* exitv,
-                                 int* nonconv) {
-  __shared__ DMathTab tab;
-  dmath_tab_init(tab);
-  __syncthreads();
-  const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (s >= g.nseg) return;
+// Segment s of the chain: its entry cd (the chain's state for the first
+// segment, else the value a warm-up of W cells from cd = 1 reaches), its
+// cells and its exit cd.
+__device__ __forceinline__ void chain_segment(const ChainGeom& g, long long s, int modv, const ClassConst* cc,
+                                              const double* visc, const double2* cf, const double* rho,
+                                              double* vset, int* iters, const double* cd_state, double* entry,
+                                              double* exitv, int* nonconv, const DMathTab& tab) {
   const long long q0 = s * g.S, q1 = min(g.L, q0 + g.S);
   double cd;
   int nc_flag = 0, dummy = 0;
@@ -541,6 +539,49 @@ __global__ void k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, co
   chain_run(g, q0, q1, modv, cc, visc, cf, rho, vset, iters, cd, true, nc_flag, tab);
   exitv[s] = cd;
   nonconv[s] = nc_flag;
+}
+
+// One segment per thread; a segment's result does not depend on the thread
+// or block that computes it.
+__global__ void __launch_bounds__(64, 16)
+    k_chain_segments(ChainGeom g, int modv, const ClassConst* cc, const double* visc, const double2* cf,
+                     const double* rho, double* vset, int* iters, const double* cd_state, double* entry,
+                     double* exitv, int* nonconv) {
+  __shared__ DMathTab tab;
+  dmath_tab_init(tab);
+  __syncthreads();
+  const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (s >= g.nseg) return;
+  chain_segment(g, s, modv, cc, visc, cf, rho, vset, iters, cd_state, entry, exitv, nonconv, tab);
+}
+
+// The same segments computed beside the step kernel (a look-ahead meteo
+// update on a second stream): blocks of four warps, one per SM sub-partition,
+// at most 64 registers and 2.5 KB of shared memory, which is what a resident
+// step-kernel block (four 112-register warps per sub-partition, 222 KB)
+// leaves free.  Only the first block that starts on an SM works (claim[smid]);
+// later ones on the same SM return at once, so that an SM idle at launch
+// time does not fill up with chain blocks and shut the steps out.  The
+// working blocks take segments from a counter until none is left.
+__global__ void __launch_bounds__(128, 8)
+    k_chain_beside(ChainGeom g, int modv, const ClassConst* cc, const double* visc, const double2* cf,
+                   const double* rho, double* vset, int* iters, const double* cd_state, double* entry,
+                   double* exitv, int* nonconv, int* claim, unsigned long long* next) {
+  __shared__ DMathTab tab;
+  __shared__ int mine;
+  if (threadIdx.x == 0) {
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    mine = atomicCAS(claim + (smid & 255u), 0, 1) == 0;
+  }
+  dmath_tab_init(tab);
+  __syncthreads();
+  if (!mine) return;
+  for (;;) {
+    const unsigned long long s = atomicAdd(next, 1ULL);
+    if (s >= (unsigned long long)g.nseg) break;
+    chain_segment(g, (long long)s, modv, cc, visc, cf, rho, vset, iters, cd_state, entry, exitv, nonconv, tab);
+  }
 }
 
 // Collects segments whose speculative entry differs from the predecessor's exit.
@@ -681,6 +722,7 @@ size_t setvset_scratch_bytes(Dims d, int np) {
   size_t b = sizeof(ClassConst) * (size_t)(np + 1);
   b += 2 * sizeof(double) * (size_t)g.nseg + sizeof(int) * (size_t)g.nseg;
   b += sizeof(int) * (kBadCap + 8) + 1024;
+  b += sizeof(int) * 256 + sizeof(unsigned long long) + 512;  // per-SM claims, segment counter
   b += sizeof(double) * (size_t)d.cells() + 256;      // viscosity per cell
   b += 2 * sizeof(double) * (size_t)d.cells() + 256;  // Ganser cell factors
   return b;
@@ -689,7 +731,8 @@ size_t setvset_scratch_bytes(Dims d, int np) {
 void launch_setvset(Dims d, int nc, int np, int modv, const double* diam, const double* rhop,
                     const double* psi, const double* sphe, const double* tempe,
                     const double* rho, int aggregate, double vset_factor, double* vset,
-                    int* iters, double* cd_state, void* scratch, int* status, cudaStream_t s) {
+                    int* iters, double* cd_state, void* scratch, int* status, cudaStream_t s,
+                    int beside_step) {
   const ChainGeom g = chain_geom(d, np);
   unsigned char* p = reinterpret_cast<unsigned char*>(scratch);
   auto take = [&](size_t bytes) {
@@ -705,6 +748,8 @@ void launch_setvset(Dims d, int nc, int np, int modv, const double* diam, const 
   int* bad = reinterpret_cast<int*>(take(sizeof(int) * kBadCap));
   double* visc = reinterpret_cast<double*>(take(sizeof(double) * (size_t)d.cells()));
   double2* cf = reinterpret_cast<double2*>(take(2 * sizeof(double) * (size_t)d.cells()));
+  int* claim = reinterpret_cast<int*>(take(sizeof(int) * 256));
+  unsigned long long* next = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
   cudaMemsetAsync(nbad, 0, sizeof(int), s);
   cudaMemsetAsync(status, 0, sizeof(int), s);
   if (np > 0 && g.L > 0) {
@@ -712,8 +757,26 @@ void launch_setvset(Dims d, int nc, int np, int modv, const double* diam, const 
     k_visc<<<(int)std::min<long long>((d.cells() + 255) / 256, 152LL * 16), 256, 0, s>>>(d.cells(), tempe,
                                                                                          rho, visc, cf);
     const int bs = 64;
-    k_chain_segments<<<(unsigned)((g.nseg + bs - 1) / bs), bs, 0, s>>>(
-        g, modv, cc, visc, cf, rho, vset, iters, cd_state, entry, exitv, nonconv);
+    const long long nb = (g.nseg + bs - 1) / bs;
+    if (beside_step) {
+      static int nsm = 0;
+      if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        // an SM holding this block must still take a step-kernel block
+        cudaFuncSetAttribute(k_chain_beside, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+      }
+      cudaMemsetAsync(claim, 0, sizeof(int) * 256, s);
+      cudaMemsetAsync(next, 0, sizeof(unsigned long long), s);
+      k_chain_beside<<<(unsigned)(4 * std::max(1, nsm)), 128, 0, s>>>(g, modv, cc, visc, cf, rho, vset, iters,
+                                                                      cd_state, entry, exitv, nonconv, claim,
+                                                                      next);
+    } else {
+      k_chain_segments<<<(unsigned)nb, bs, 0, s>>>(g, modv, cc, visc, cf, rho, vset, iters, cd_state, entry,
+                                                   exitv, nonconv);
+    }
     k_chain_check<<<(unsigned)((g.nseg + 255) / 256), 256, 0, s>>>(g, entry, exitv, bad, nbad, kBadCap);
     k_chain_fix<<<1, 32, 0, s>>>(g, modv, cc, visc, cf, rho, vset, iters, entry, exitv, nonconv, bad,
                                  nbad, kBadCap, cd_state);

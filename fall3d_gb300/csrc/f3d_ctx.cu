@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -44,6 +45,10 @@ unsigned long long* small_dtcn(f3d_ctx* x) {
 }
 int* small_status(f3d_ctx* x) { return reinterpret_cast<int*>(x->small + 24); }
 int* small_step_status(f3d_ctx* x) { return reinterpret_cast<int*>(x->small + 26); }  // F3D_STEP_* bits
+// the look-ahead meteo update's chain state, CFL maximum and status
+double* small_pref_cd(f3d_ctx* x) { return x->small + 32; }
+unsigned long long* small_pref_dtcn(f3d_ctx* x) { return reinterpret_cast<unsigned long long*>(x->small + 33); }
+int* small_pref_status(f3d_ctx* x) { return reinterpret_cast<int*>(x->small + 34); }
 
 template <class T>
 int dalloc(f3d_ctx* x, T** p, size_t n) {
@@ -58,6 +63,74 @@ int dalloc(f3d_ctx* x, T** p, size_t n) {
     return f3d::ctx_error(F3D_ERR_CUDA, "cudaMemsetAsync failed");
   *p = reinterpret_cast<T*>(q);
   return F3D_OK;
+}
+
+// Device buffers of one met set (f3d_met_set) for the context's grid and
+// precision; the members a precision does not use stay null.
+int met_set_alloc(f3d_ctx* x, f3d_met_set* m) {
+  const Dims d = x->d;
+  const size_t s3 = (size_t)d.cells(), pl = (size_t)d.plane(), nc = (size_t)x->g.nc;
+  const size_t hsz = (size_t)f3d::halo_pitch(d.nx) * (d.ny + 2) * (d.nz + 2);
+  int rc = 0;
+#define A(p, n) \
+  if (!rc) rc = dalloc(x, &m->p, (n))
+  A(vx, s3);
+  A(vy, s3);
+  A(vz, s3);
+  A(tempe, s3);
+  A(vptemp, s3);
+  A(rho, s3);
+  A(rkhor, s3);
+  A(rkh1, s3);
+  A(rkver, s3);
+  A(divu, s3);
+  A(vset, s3 * nc);
+  A(vdep, pl * nc);
+  A(ustar, pl);
+  A(zi, pl);
+  A(rl, pl);
+  A(znt, pl);
+  A(prate, pl);
+  A(iters, s3 * nc);
+  if (x->prec == F3D_PREC_FP64) {
+    A(lrho64, s3);
+    A(pkx64, s3);
+    A(pky64, s3);
+    A(rksz64, s3);
+  } else {
+    A(vx32, s3);
+    A(vy32, s3);
+    A(vz32, s3);
+    A(rho32, s3);
+    A(rkhor32, s3);
+    A(rkh132, s3);
+    A(rkver32, s3);
+    A(vset32, s3 * nc);
+    A(vdep32, pl * nc);
+    A(lrho32, s3);
+    A(pkx32, s3);
+    A(pky32, s3);
+    A(pkz32, s3);
+    A(vk32, s3 * nc);
+    A(vxh, hsz);
+    A(vyh, hsz);
+    A(lrhoh, hsz);
+    A(pkxh, hsz);
+    A(pkyh, hsz);
+    A(pkzh, hsz);
+    A(vkh, hsz * nc);
+  }
+#undef A
+  return rc;
+}
+
+// Exchanges the context's current met set with *m (pointers only).
+void met_set_swap(f3d_ctx* x, f3d_met_set* m) {
+#define F3D_X(T, n) std::swap(x->n, m->n);
+  F3D_MET_SET_D(F3D_X)
+  F3D_MET_SET_F(F3D_X)
+#undef F3D_X
+  std::swap(x->maps2, m->maps2);
 }
 
 }  // namespace
@@ -95,11 +168,13 @@ int is_dev(const void* p) {
   return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) ? 1 : 0;
 }
 
-int upload(f3d_ctx* x, double* dst, const double* src, size_t n) {
+int upload_on(double* dst, const double* src, size_t n, cudaStream_t s) {
   CK(cudaMemcpyAsync(dst, src, n * sizeof(double),
-                     is_dev(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, x->stream));
+                     is_dev(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
   return F3D_OK;
 }
+
+int upload(f3d_ctx* x, double* dst, const double* src, size_t n) { return upload_on(dst, src, n, x->stream); }
 
 long long footprint_bytes(const f3d_grid* g) {
   const long long nx = g->nx, ny = g->ny, nz = g->nz, nc = g->nc;
@@ -375,6 +450,215 @@ namespace f3d {
 int ctx_error(int code, const char* msg);
 }
 
+namespace {
+
+// The kernels of one meteo update on stream s (Sources/meteo.f90:27-149 with
+// reamet.f90's fixes), writing the context's current met set: the raw
+// fields are copied in (from host or device memory), the settling-velocity
+// chain continues from *cd_state (setvset.f90:89), finddt's CFL maximum goes
+// to *dtcn and a non-convergence to *status.  beside_step: the chain runs
+// next to the step kernel (a look-ahead update on the second stream).
+int meteo_enqueue(f3d_ctx* x, cudaStream_t s, const double* u, const double* v, const double* w,
+                  const double* t, const double* tp, const double* rho, const double* ust,
+                  const double* pblh, const double* rmol, const double* znt, const double* prate,
+                  const double* ldu, double* cd_state, unsigned long long* dtcn, int* status,
+                  int beside_step) {
+  const Dims d = x->d;
+  const size_t s3 = (size_t)d.cells(), pl = (size_t)d.plane();
+  int rc = 0;
+  // reamet.f90:20-153
+  if (!rc) rc = upload_on(x->vx, u, s3, s);
+  if (!rc) rc = upload_on(x->vy, v, s3, s);
+  if (!rc) rc = upload_on(x->vz, w, s3, s);
+  if (!rc) rc = upload_on(x->tempe, t, s3, s);
+  if (!rc) rc = upload_on(x->vptemp, tp, s3, s);
+  if (!rc) rc = upload_on(x->rho, rho, s3, s);
+  if (!rc) rc = upload_on(x->ustar, ust, pl, s);
+  if (!rc) rc = upload_on(x->zi, pblh, pl, s);
+  if (!rc) rc = upload_on(x->rl, rmol, pl, s);
+  if (!rc) rc = upload_on(x->znt, znt, pl, s);
+  if (!rc && ldu) rc = upload_on(x->ldu, ldu, pl, s);
+  if (!rc && x->g.wetdep) rc = upload_on(x->prate, prate, pl, s);
+  if (rc) return rc;
+  const f3d_grid& g = x->g;
+  launch_reamet_fix(d, g.wetdep, x->vz, x->prate, s);
+  // meteo.f90:27 kappa3 (unscaled vx, vy)
+  launch_kappa3(d, g.modkv, g.modkh, g.coord_sys, g.rkv0, g.rkh0, g.Csh, g.dX1, g.dX2, g.dx, g.dy,
+                x->dz, x->zlayer, x->Hm1, x->vx, x->vy, x->vptemp, x->ustar, x->zi, x->rl, x->rkver,
+                x->rkhor, s);
+  // meteo.f90:81 setvset (unscaled rho), continuing the cd chain
+  launch_setvset(d, g.nc, g.np, g.modv, x->diam, x->rhop, x->psi, x->sphe, x->tempe, x->rho,
+                 g.aggregate, g.vset_factor, x->vset, x->iters, cd_state, x->vset_scratch, status, s,
+                 beside_step);
+  // meteo.f90:100 setvdrydep (tempe(:,:,1), unscaled rho(:,:,1))
+  launch_setvdrydep(d, g.nc, x->diam, x->zlayer, x->ldu, x->rl, x->znt, x->ustar, x->tempe, x->rho,
+                    x->vdep, s);
+  // meteo.f90:108-135 scaling and corvver, :140 addradialwind, :145 setdivu
+  launch_meteo_scale(d, g.coord_sys, g.dX1, g.dX2, x->dz, x->Hm1, x->topg, x->vx, x->vy, x->vz,
+                     x->rho, x->rkhor, x->rkh1, nullptr, s);
+  if (x->gc_on) {  // the context's stream only: no look-ahead with the gravity current
+    if (int r = f3d::gc_addradialwind(x)) return r;
+  }
+  launch_setdivu(d, g.dX1, g.dX2, x->dz, x->Hm1, x->vx, x->vy, x->vz, x->divu, s);
+  // meteo.f90:149 finddt
+  CK(cudaMemsetAsync(dtcn, 0, sizeof(unsigned long long), s));
+  launch_finddt(d, g.nc, g.dX1, g.dX2, x->dz, x->vx, x->vy, x->vz, x->vset, x->rkh1, x->rkhor,
+                x->rkver, dtcn, s);
+  if (x->prec == F3D_PREC_FP64)
+    launch_diff_coeffs(d, x->rho, x->rkh1, x->rkhor, x->rkver, x->lrho64, x->pkx64, x->pky64, x->rksz64, s);
+  if (x->prec == F3D_PREC_FP32) {
+    launch_d2f(x->vx32, x->vx, (long long)s3, s);
+    launch_d2f(x->vy32, x->vy, (long long)s3, s);
+    launch_d2f(x->vz32, x->vz, (long long)s3, s);
+    launch_d2f(x->rho32, x->rho, (long long)s3, s);
+    launch_d2f(x->rkhor32, x->rkhor, (long long)s3, s);
+    launch_d2f(x->rkh132, x->rkh1, (long long)s3, s);
+    launch_d2f(x->rkver32, x->rkver, (long long)s3, s);
+    launch_d2f(x->vset32, x->vset, (long long)(s3 * g.nc), s);
+    launch_d2f(x->vdep32, x->vdep, (long long)(pl * g.nc), s);
+    launch_fp32_coeffs((long long)s3, x->rho, x->rkh1, x->rkhor, x->rkver, x->lrho32, x->pkx32,
+                       x->pky32, x->pkz32, s);
+    launch_vk32((long long)s3, g.nc, x->vz32, x->vset32, x->vk32, s);
+    {  // halo-layout copies for the two-columns-per-lane kernel
+      const float* src[6] = {x->vx32, x->vy32, x->lrho32, x->pkx32, x->pky32, x->pkz32};
+      float* dst[6] = {x->vxh, x->vyh, x->lrhoh, x->pkxh, x->pkyh, x->pkzh};
+      const int hp = halo_pitch(d.nx);
+      launch_to_halo(d, hp, 6, src, dst, s);
+      for (int c = 0; c < g.nc; ++c) {
+        const float* vs = x->vk32 + (size_t)c * s3;
+        float* vd = x->vkh + (size_t)c * (size_t)hp * (d.ny + 2) * (d.nz + 2);
+        launch_to_halo(d, hp, 1, &vs, &vd, s);
+      }
+    }
+  }
+  CK(cudaGetLastError());
+  return F3D_OK;
+}
+
+// What follows an update on the host: finddt.f90:58-66 from the CFL
+// maximum, the wet-scavenging rate of the new dt (wetdep.f90:31), the
+// aggregation flags (Fall3d.f90:94-96).
+int meteo_finish(f3d_ctx* x, unsigned long long dtcn_bits, int status) {
+  if (status) return f3d::ctx_error(F3D_ERR_NOCONV, "No convergence in vsettl routine");
+  double dtcn;
+  memcpy(&dtcn, &dtcn_bits, sizeof dtcn);
+  dtcn = fmax2(dtcn, 1e-13);
+  x->dtc = 1.0 / dtcn;
+  x->dt = x->g.safety_factor * x->dtc;
+  if (x->g.wetdep) {
+    launch_wet_lambda((long long)x->d.plane(), x->dt, x->prate, x->lambda2d, x->stream);
+    CK(cudaGetLastError());
+  }
+  x->have_met = 1;
+  if (x->agr_on) {
+    x->agr_due = 1;
+    x->agr_npar = 0;
+  }
+  return F3D_OK;
+}
+
+// The second met set, the staging buffer of the next snapshot's raw fields,
+// the second stream (lowest priority) and its events, made on first use.
+int prefetch_setup(f3d_ctx* x) {
+  if (x->pref_alloc) return F3D_OK;
+  f3d_met_set m;
+  if (int rc = met_set_alloc(x, &m)) return rc;
+  if (x->prec == F3D_PREC_FP32 && x->fused_ok) {  // tensor maps of the second set's fields
+    met_set_swap(x, &m);
+    const int r2 = f3d::make_fused2_maps(f3d::ctx_fused_args(x), &x->maps2);
+    met_set_swap(x, &m);
+    if (r2) return f3d::ctx_error(F3D_ERR_CUDA, "cuTensorMapEncodeTiled failed for the second met set");
+  }
+  x->shadow = m;
+  const size_t s3 = (size_t)x->d.cells(), pl = (size_t)x->d.plane();
+  if (int rc = dalloc(x, &x->pref_stage, 6 * s3 + 5 * pl)) return rc;
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  CK(cudaStreamCreateWithPriority(&x->side, cudaStreamNonBlocking, least));
+  CK(cudaEventCreateWithFlags(&x->ev_pref, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&x->ev_free, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&x->ev_staged, cudaEventDisableTiming));
+  CK(cudaMallocHost((void**)&x->pref_host, 2 * sizeof(unsigned long long)));
+  CK(cudaStreamSynchronize(x->stream));  // the zero fills of the new buffers
+  x->pref_alloc = 1;
+  return F3D_OK;
+}
+
+// Enqueues the meteo update of snapshot itime of the series on the second
+// stream, into the second met set.  Its raw fields are staged first; the
+// update itself waits for the steps enqueued so far (they read the set it
+// overwrites).  Its chain starts from the committed chain state and writes
+// its own slot, so a dropped look-ahead leaves the run as it was.
+int prefetch_start(f3d_ctx* x, const f3d_met_series* met, int itime) {
+  if (!x->opt_prefetch || x->pref_failed || x->gc_on || x->agr_on) return F3D_OK;
+  if (x->g.wetdep && !met->prate) return F3D_OK;
+  if (prefetch_setup(x)) {  // no room for a second set: the updates stay where they are due
+    cudaGetLastError();
+    x->pref_failed = 1;
+    return F3D_OK;
+  }
+  const size_t s3 = (size_t)x->d.cells(), pl = (size_t)x->d.plane();
+  const size_t o3 = (size_t)itime * s3, o2 = (size_t)itime * pl;
+  cudaStream_t s = x->side;
+  double* st = x->pref_stage;
+  const double* src3[6] = {met->u + o3, met->v + o3, met->w + o3, met->t + o3, met->tp + o3, met->rho + o3};
+  const double* src2[5] = {met->ust + o2, met->pblh + o2, met->rmol + o2, met->znt + o2,
+                           met->prate ? met->prate + o2 : nullptr};
+  double* f3[6];
+  double* f2[5];
+  for (int q = 0; q < 6; ++q) {
+    f3[q] = st + q * s3;
+    if (int rc = upload_on(f3[q], src3[q], s3, s)) return rc;
+  }
+  for (int q = 0; q < 5; ++q) {
+    f2[q] = st + 6 * s3 + q * pl;
+    if (src2[q])
+      if (int rc = upload_on(f2[q], src2[q], pl, s)) return rc;
+  }
+  CK(cudaEventRecord(x->ev_staged, s));  // f3d_run returns only after these reads of the series
+  CK(cudaEventRecord(x->ev_free, x->stream));
+  CK(cudaStreamWaitEvent(s, x->ev_free, 0));
+  CK(cudaMemcpyAsync(small_pref_cd(x), small_cd(x), sizeof(double), cudaMemcpyDeviceToDevice, s));
+  met_set_swap(x, &x->shadow);
+  const int rc = meteo_enqueue(x, s, f3[0], f3[1], f3[2], f3[3], f3[4], f3[5], f2[0], f2[1], f2[2], f2[3],
+                               src2[4] ? f2[4] : nullptr, nullptr, small_pref_cd(x), small_pref_dtcn(x),
+                               small_pref_status(x), 1);
+  met_set_swap(x, &x->shadow);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(x->pref_host, small_pref_dtcn(x), sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(x->pref_host + 1, small_pref_status(x), sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(x->ev_pref, s));
+  x->pref_ready = 1;
+  x->pref_itime = itime;
+  return F3D_OK;
+}
+
+// The look-ahead update becomes the current one: the two met sets are
+// exchanged, its chain state is committed (the state before it kept for a
+// checkpoint) and the host finishes the update as f3d_meteo does.
+int prefetch_commit(f3d_ctx* x) {
+  CK(cudaEventSynchronize(x->ev_pref));
+  const unsigned long long bits = x->pref_host[0];
+  int status = 0;
+  memcpy(&status, x->pref_host + 1, sizeof status);
+  CK(cudaStreamWaitEvent(x->stream, x->ev_pref, 0));
+  met_set_swap(x, &x->shadow);
+  x->pref_ready = 0;
+  CK(cudaMemcpyAsync(small_cd_prev(x), small_cd(x), sizeof(double), cudaMemcpyDeviceToDevice, x->stream));
+  CK(cudaMemcpyAsync(small_cd(x), small_pref_cd(x), sizeof(double), cudaMemcpyDeviceToDevice, x->stream));
+  return meteo_finish(x, bits, status);
+}
+
+}  // namespace
+
+namespace f3d {
+void ctx_prefetch_drop(f3d_ctx* x) {
+  if (!x->pref_ready) return;
+  cudaEventSynchronize(x->ev_pref);
+  x->pref_ready = 0;
+}
+}  // namespace f3d
+
 extern "C" {
 
 int f3d_ctx_footprint(const f3d_grid* g, long long* bytes) {
@@ -385,7 +669,14 @@ int f3d_ctx_footprint(const f3d_grid* g, long long* bytes) {
 
 int f3d_ctx_destroy(f3d_ctx* x) {
   if (!x) return F3D_OK;
+  f3d::ctx_prefetch_drop(x);
+  if (x->side) cudaStreamSynchronize(x->side);
   if (x->stream) cudaStreamSynchronize(x->stream);
+  if (x->ev_pref) cudaEventDestroy(x->ev_pref);
+  if (x->ev_free) cudaEventDestroy(x->ev_free);
+  if (x->ev_staged) cudaEventDestroy(x->ev_staged);
+  if (x->pref_host) cudaFreeHost(x->pref_host);
+  if (x->side) cudaStreamDestroy(x->side);
   for (auto& r : x->prof_pending) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
@@ -423,7 +714,11 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
   if (x->d.halo() >= (1LL << 31) || x->d.cells() >= (1LL << 31)) x->fused_ok = 0;
   if ((long long)f3d::halo_pitch(g->nx) * (g->ny + 2) * (g->nz + 2) >= (1LL << 31)) x->fused_ok = 0;
   if (g->nz > f3d::fused2_max_nz()) x->fused_ok = 0;  // the shape-3 kernel's per-level table
-  if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  // the highest priority: a look-ahead meteo update on the context's second
+  // stream (lowest priority) runs in what the steps leave free
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  if (cudaStreamCreateWithPriority(&x->stream, cudaStreamNonBlocking, prio_greatest) != cudaSuccess) {
     delete x;
     return f3d::ctx_error(F3D_ERR_CUDA, "cudaStreamCreate failed");
   }
@@ -441,67 +736,26 @@ int f3d_ctx_create(const f3d_grid* g, f3d_ctx** out) {
   A(rhop, nc);
   A(psi, nc);
   A(sphe, nc);
-  A(vx, s3);
-  A(vy, s3);
-  A(vz, s3);
-  A(tempe, s3);
-  A(vptemp, s3);
-  A(rho, s3);
-  A(rkhor, s3);
-  A(rkh1, s3);
-  A(rkver, s3);
-  A(divu, s3);
-  A(vset, s3 * nc);
-  A(vdep, pl * nc);
-  A(ustar, pl);
-  A(zi, pl);
-  A(rl, pl);
-  A(znt, pl);
-  A(prate, pl);
   A(ldu, pl);
-  A(iters, s3 * nc);
   A(cdry, pl * (nc + 1));
   A(cwet, pl * (nc + 1));
   A(cload, pl * (nc + 1));
   A(small, 64);
-  if (x->prec == F3D_PREC_FP64) {
-    A(lrho64, s3);
-    A(pkx64, s3);
-    A(pky64, s3);
-    A(rksz64, s3);
-  }
   if (x->prec == F3D_PREC_FP32) {
     A(c32, hb * nc);
-    A(vx32, s3);
-    A(vy32, s3);
-    A(vz32, s3);
-    A(rho32, s3);
-    A(rkhor32, s3);
-    A(rkh132, s3);
-    A(rkver32, s3);
-    A(vset32, s3 * nc);
-    A(vdep32, pl * nc);
     A(dz32, nz + 1);
     A(c32b, hb * nc);
-    A(lrho32, s3);
-    A(pkx32, s3);
-    A(pky32, s3);
-    A(pkz32, s3);
-    A(vk32, s3 * nc);
-    const size_t hsz = (size_t)f3d::halo_pitch(g->nx) * (g->ny + 2) * (g->nz + 2);
-    A(vxh, hsz);
-    A(vyh, hsz);
-    A(lrhoh, hsz);
-    A(pkxh, hsz);
-    A(pkyh, hsz);
-    A(pkzh, hsz);
-    A(vkh, hsz * nc);
     A(wet_class, nc);
   } else {
     A(c64, hb * nc);
   }
   A(lambda2d, pl);
 #undef A
+  if (!rc) {  // the met set (f3d_met_set) the meteo updates fill
+    f3d_met_set m;
+    rc = met_set_alloc(x, &m);
+    if (!rc) met_set_swap(x, &m);
+  }
   if (!rc) {
     unsigned char* p = nullptr;
     rc = dalloc(x, &p, f3d::reduce_scratch_bytes(2LL * g->nc * (g->nx + g->ny) * g->nz +
@@ -566,81 +820,14 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
   if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
   if (!u || !v || !w || !t || !tp || !rho || !ust || !pblh || !rmol || !znt)
     return f3d::ctx_error(F3D_ERR_ARG, "NULL meteorological field");
-  const Dims d = x->d;
-  const size_t s3 = (size_t)d.cells(), pl = (size_t)d.plane();
+  if (x->g.wetdep && !prate) return f3d::ctx_error(F3D_ERR_ARG, "PRATE required with wet deposition");
+  f3d::ctx_prefetch_drop(x);
   cudaStream_t s = x->stream;
-  int rc = 0;
-  // reamet.f90:20-153
-  if (!rc) rc = upload(x, x->vx, u, s3);
-  if (!rc) rc = upload(x, x->vy, v, s3);
-  if (!rc) rc = upload(x, x->vz, w, s3);
-  if (!rc) rc = upload(x, x->tempe, t, s3);
-  if (!rc) rc = upload(x, x->vptemp, tp, s3);
-  if (!rc) rc = upload(x, x->rho, rho, s3);
-  if (!rc) rc = upload(x, x->ustar, ust, pl);
-  if (!rc) rc = upload(x, x->zi, pblh, pl);
-  if (!rc) rc = upload(x, x->rl, rmol, pl);
-  if (!rc) rc = upload(x, x->znt, znt, pl);
-  if (!rc && ldu) rc = upload(x, x->ldu, ldu, pl);
-  if (!rc && x->g.wetdep) {
-    if (!prate) return f3d::ctx_error(F3D_ERR_ARG, "PRATE required with wet deposition");
-    rc = upload(x, x->prate, prate, pl);
-  }
-  if (rc) return rc;
-  const f3d_grid& g = x->g;
-  launch_reamet_fix(d, g.wetdep, x->vz, x->prate, s);
-  // meteo.f90:27 kappa3 (unscaled vx, vy)
-  launch_kappa3(d, g.modkv, g.modkh, g.coord_sys, g.rkv0, g.rkh0, g.Csh, g.dX1, g.dX2, g.dx, g.dy,
-                x->dz, x->zlayer, x->Hm1, x->vx, x->vy, x->vptemp, x->ustar, x->zi, x->rl, x->rkver,
-                x->rkhor, s);
-  // meteo.f90:81 setvset (unscaled rho), continuing the cd chain
   // the chain state this update starts from (a checkpoint replays the update)
-  CK(cudaMemcpyAsync(small_cd_prev(x), small_cd(x), sizeof(double), cudaMemcpyDeviceToDevice, x->stream));
-  launch_setvset(d, g.nc, g.np, g.modv, x->diam, x->rhop, x->psi, x->sphe, x->tempe, x->rho,
-                 g.aggregate, g.vset_factor, x->vset, x->iters, small_cd(x), x->vset_scratch,
-                 small_status(x), s);
-  // meteo.f90:100 setvdrydep (tempe(:,:,1), unscaled rho(:,:,1))
-  launch_setvdrydep(d, g.nc, x->diam, x->zlayer, x->ldu, x->rl, x->znt, x->ustar, x->tempe, x->rho,
-                    x->vdep, s);
-  // meteo.f90:108-135 scaling and corvver, :140 addradialwind, :145 setdivu
-  launch_meteo_scale(d, g.coord_sys, g.dX1, g.dX2, x->dz, x->Hm1, x->topg, x->vx, x->vy, x->vz,
-                     x->rho, x->rkhor, x->rkh1, nullptr, s);
-  if (x->gc_on) {
-    if (int r = f3d::gc_addradialwind(x)) return r;
-  }
-  launch_setdivu(d, g.dX1, g.dX2, x->dz, x->Hm1, x->vx, x->vy, x->vz, x->divu, s);
-  // meteo.f90:149 finddt
-  CK(cudaMemsetAsync(small_dtcn(x), 0, sizeof(unsigned long long), s));
-  launch_finddt(d, g.nc, g.dX1, g.dX2, x->dz, x->vx, x->vy, x->vz, x->vset, x->rkh1, x->rkhor,
-                x->rkver, small_dtcn(x), s);
-  if (x->prec == F3D_PREC_FP64)
-    launch_diff_coeffs(d, x->rho, x->rkh1, x->rkhor, x->rkver, x->lrho64, x->pkx64, x->pky64, x->rksz64, s);
-  if (x->prec == F3D_PREC_FP32) {
-    launch_d2f(x->vx32, x->vx, (long long)s3, s);
-    launch_d2f(x->vy32, x->vy, (long long)s3, s);
-    launch_d2f(x->vz32, x->vz, (long long)s3, s);
-    launch_d2f(x->rho32, x->rho, (long long)s3, s);
-    launch_d2f(x->rkhor32, x->rkhor, (long long)s3, s);
-    launch_d2f(x->rkh132, x->rkh1, (long long)s3, s);
-    launch_d2f(x->rkver32, x->rkver, (long long)s3, s);
-    launch_d2f(x->vset32, x->vset, (long long)(s3 * g.nc), s);
-    launch_d2f(x->vdep32, x->vdep, (long long)(pl * g.nc), s);
-    launch_fp32_coeffs((long long)s3, x->rho, x->rkh1, x->rkhor, x->rkver, x->lrho32, x->pkx32,
-                       x->pky32, x->pkz32, s);
-    launch_vk32((long long)s3, g.nc, x->vz32, x->vset32, x->vk32, s);
-    {  // halo-layout copies for the two-columns-per-lane kernel
-      const float* src[6] = {x->vx32, x->vy32, x->lrho32, x->pkx32, x->pky32, x->pkz32};
-      float* dst[6] = {x->vxh, x->vyh, x->lrhoh, x->pkxh, x->pkyh, x->pkzh};
-      const int hp = halo_pitch(d.nx);
-      launch_to_halo(d, hp, 6, src, dst, s);
-      for (int c = 0; c < g.nc; ++c) {
-        const float* vs = x->vk32 + (size_t)c * s3;
-        float* vd = x->vkh + (size_t)c * (size_t)hp * (d.ny + 2) * (d.nz + 2);
-        launch_to_halo(d, hp, 1, &vs, &vd, s);
-      }
-    }
-  }
-  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(small_cd_prev(x), small_cd(x), sizeof(double), cudaMemcpyDeviceToDevice, s));
+  if (int rc = meteo_enqueue(x, s, u, v, w, t, tp, rho, ust, pblh, rmol, znt, prate, ldu, small_cd(x),
+                             small_dtcn(x), small_status(x), 0))
+    return rc;
   struct {
     unsigned long long dtcn;
     int status;
@@ -648,22 +835,7 @@ int f3d_meteo(f3d_ctx* x, const double* u, const double* v, const double* w, con
   CK(cudaMemcpyAsync(&h.dtcn, small_dtcn(x), sizeof h.dtcn, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&h.status, small_status(x), sizeof h.status, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  if (h.status) return f3d::ctx_error(F3D_ERR_NOCONV, "No convergence in vsettl routine");
-  double dtcn;
-  memcpy(&dtcn, &h.dtcn, sizeof dtcn);
-  dtcn = fmax2(dtcn, 1e-13);  // finddt.f90:58-66
-  x->dtc = 1.0 / dtcn;
-  x->dt = g.safety_factor * x->dtc;
-  if (g.wetdep) {  // the scavenging coefficient of this dt, for every class (wetdep.f90:31)
-    launch_wet_lambda((long long)pl, x->dt, x->prate, x->lambda2d, s);
-    CK(cudaGetLastError());
-  }
-  x->have_met = 1;
-  if (x->agr_on) {  // Fall3d.f90:94-96
-    x->agr_due = 1;
-    x->agr_npar = 0;
-  }
-  return F3D_OK;
+  return meteo_finish(x, h.dtcn, h.status);
 }
 
 int f3d_source(f3d_ctx* x, int nsou, const int* isrc, const int* jsrc, const int* ksrc,
@@ -975,6 +1147,7 @@ int f3d_ctx_restore(f3d_ctx* x, const char* path) {
   if (!ok) return f3d::ctx_error(F3D_ERR_ARG, "truncated checkpoint file");
   if (has_agg != (x->agr_on != 0))
     return f3d::ctx_error(F3D_ERR_ARG, "aggregation is on in only one of the checkpoint and the context");
+  f3d::ctx_prefetch_drop(x);
   cudaStream_t s = x->stream;
   CK(cudaMemcpyAsync(x->prec == F3D_PREC_FP32 ? (void*)x->c32 : (void*)x->c64, c.data(), hb * esz,
                      cudaMemcpyHostToDevice, s));
@@ -1052,6 +1225,15 @@ int f3d_set_option(f3d_ctx* x, int key, int value) {
   } else if (key == F3D_OPT_TILE) {
     if (value < 0 || value > 3) return f3d::ctx_error(F3D_ERR_ARG, "tile shape must be 0..3");
     x->opt_tile = value;
+  } else if (key == F3D_OPT_PREFETCH) {
+    if (!value) f3d::ctx_prefetch_drop(x);
+    x->opt_prefetch = value ? 1 : 0;
+    if (value && !x->gc_on && !x->agr_on) {  // the second set now rather than at the first use
+      if (int rc = prefetch_setup(x)) {
+        x->pref_failed = 1;
+        return rc;
+      }
+    }
   } else {
     return f3d::ctx_error(F3D_ERR_ARG, "unknown option");
   }
@@ -1064,6 +1246,8 @@ int f3d_get_option(const f3d_ctx* x, int key, int* value) {
     *value = x->opt_fused;
   else if (key == F3D_OPT_TILE)
     *value = x->opt_tile;
+  else if (key == F3D_OPT_PREFETCH)
+    *value = x->opt_prefetch;
   else
     return f3d::ctx_error(F3D_ERR_ARG, "unknown option");
   return F3D_OK;
@@ -1103,6 +1287,7 @@ int f3d_profile_read(f3d_ctx* x, int cap, char* names, int name_len, long long* 
 
 int f3d_run_reset(f3d_ctx* x) {
   if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  f3d::ctx_prefetch_drop(x);
   x->run_started = 0;
   return F3D_OK;
 }
@@ -1112,7 +1297,8 @@ int f3d_run_reset(f3d_ctx* x) {
 namespace f3d {
 // Sources/Fall3d.f90:83-101 with the interval selection of
 // libMaster/get_dbs_value_plane.f90:100-114 and get_source_nsrc.f90:41-59.
-int ctx_run_prepare(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, double end_time) {
+int ctx_run_prepare(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, double end_time,
+                    int lookahead) {
   const size_t s3 = (size_t)x->d.cells(), pl = (size_t)x->d.plane();
   const int nc = x->g.nc;
   if (x->source_time <= x->time) {
@@ -1164,14 +1350,24 @@ int ctx_run_prepare(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series*
           endsec = met->times[it + 1];
         }
       const size_t o3 = (size_t)itime * s3, o2 = (size_t)itime * pl;
-      if (x->agr_on && met->qv && met->p) {
-        if (int r2 = f3d_aggregation_met(x, met->qv + o3, met->p + o3)) return r2;
+      int rc;
+      if (lookahead && x->pref_ready && x->pref_itime == itime) {
+        rc = prefetch_commit(x);  // computed while the previous interval stepped
+      } else {
+        if (x->agr_on && met->qv && met->p) {
+          if (int r2 = f3d_aggregation_met(x, met->qv + o3, met->p + o3)) return r2;
+        }
+        rc = f3d_meteo(x, met->u + o3, met->v + o3, met->w + o3, met->t + o3, met->tp + o3, met->rho + o3,
+                       met->ust + o2, met->pblh + o2, met->rmol + o2, met->znt + o2,
+                       met->prate ? met->prate + o2 : nullptr, met->ldu);
       }
-      const int rc = f3d_meteo(x, met->u + o3, met->v + o3, met->w + o3, met->t + o3, met->tp + o3,
-                               met->rho + o3, met->ust + o2, met->pblh + o2, met->rmol + o2,
-                               met->znt + o2, met->prate ? met->prate + o2 : nullptr, met->ldu);
       if (rc) return rc;
       x->meteo_time = (double)endsec - met->time_lag;
+      // the next snapshot's update while this interval steps: the update due
+      // at meteo_time reads snapshot itime + 1 (the steps are shorter than
+      // a DBS interval; otherwise it is dropped and made when due)
+      if (lookahead && x->meteo_time < end_time && itime + 1 < nt)
+        if (int r3 = prefetch_start(x, met, itime + 1)) return r3;
     }
     if (x->meteo_time >= end_time) x->meteotime = 0;
   }
@@ -1248,10 +1444,15 @@ int f3d_run(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, do
     x->run_started = 1;
   } else {
     go_on = x->time < end_time;
+    // a later end time than the last call's: the updates that call switched
+    // off at its end (Fall3d.f90 stops them once their next time is past
+    // the end) are due again
+    if (x->meteo_time < end_time) x->meteotime = 1;
+    if (x->source_time < end_time) x->sourcetime = 1;
   }
   int steps = 0;
   while (go_on) {
-    if (int rc = f3d::ctx_run_prepare(x, met, src, end_time)) return rc;
+    if (int rc = f3d::ctx_run_prepare(x, met, src, end_time, x->opt_prefetch)) return rc;
     const int rc = f3d_step(x);
     if (rc) return rc;
     ++steps;
@@ -1259,6 +1460,10 @@ int f3d_run(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, do
     if (x->time >= end_time) go_on = false;
     if (max_steps > 0 && steps >= max_steps) go_on = false;
   }
+  // a look-ahead update still in flight has copied what it reads of the
+  // caller's series before the series may change
+  if (x->pref_ready && cudaEventSynchronize(x->ev_staged) != cudaSuccess)
+    return f3d::ctx_error(F3D_ERR_CUDA, "look-ahead meteo update failed");
   return f3d::ctx_check_step_status(x);
 }
 

@@ -9,6 +9,30 @@
 #include "f3d_internal.h"
 #include "f3d_fused.h"
 
+// The fields a meteo update writes and the steps read (f3d_meteo): the
+// binary64 met and coefficients, the plain form's diffusion factors, the
+// binary32 copies and the halo-layout copies of the precision form.  A
+// look-ahead update (F3D_OPT_PREFETCH) fills a second set of them for the
+// next DBS snapshot and the two sets are exchanged at the update.
+#define F3D_MET_SET_D(X) \
+  X(double, vx) X(double, vy) X(double, vz) X(double, tempe) X(double, vptemp) X(double, rho) \
+  X(double, rkhor) X(double, rkh1) X(double, rkver) X(double, divu) X(double, vset) X(double, vdep) \
+  X(double, ustar) X(double, zi) X(double, rl) X(double, znt) X(double, prate) X(int, iters) \
+  X(double, lrho64) X(double, pkx64) X(double, pky64) X(double, rksz64)
+#define F3D_MET_SET_F(X) \
+  X(float, vx32) X(float, vy32) X(float, vz32) X(float, rho32) X(float, rkhor32) X(float, rkh132) \
+  X(float, rkver32) X(float, vset32) X(float, vdep32) X(float, lrho32) X(float, pkx32) X(float, pky32) \
+  X(float, pkz32) X(float, vk32) X(float, vxh) X(float, vyh) X(float, lrhoh) X(float, pkxh) \
+  X(float, pkyh) X(float, pkzh) X(float, vkh)
+
+struct f3d_met_set {
+#define F3D_X(T, n) T* n = nullptr;
+  F3D_MET_SET_D(F3D_X)
+  F3D_MET_SET_F(F3D_X)
+#undef F3D_X
+  f3d::F2Maps maps2{};
+};
+
 struct f3d_ctx {
   f3d_grid g{};
   Dims d{};
@@ -82,6 +106,17 @@ struct f3d_ctx {
   // f3d_run loop state (Fall3d.f90:73-78)
   int run_started = 0, meteotime = 1, sourcetime = 1;
   double meteo_time = 0.0, source_time = 0.0;
+  // look-ahead meteo update (F3D_OPT_PREFETCH, f3d_run only): the next
+  // snapshot's coefficients computed into `shadow` on the lower-priority
+  // stream `side` while the current interval steps
+  int opt_prefetch = 1;
+  int pref_ready = 0;      // a look-ahead update was enqueued (for snapshot pref_itime)
+  int pref_itime = -1, pref_alloc = 0, pref_failed = 0;
+  f3d_met_set shadow{};
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_pref = nullptr, ev_free = nullptr, ev_staged = nullptr;
+  unsigned long long* pref_host = nullptr;  // page-locked: dtcn bits, status
+  double* pref_stage = nullptr;             // the next snapshot's raw fields
   // per-kernel event profiler (f3d_profile_*)
   int prof = 0;
   struct ProfRec {
@@ -99,7 +134,10 @@ namespace f3d {
 int ctx_error(int code, const char* msg);
 // Pieces of the time loop (Fall3d.f90:79-121) shared with the batched form.
 // Source and meteo updates due at x->time (Fall3d.f90:83-101).
-int ctx_run_prepare(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, double end_time);
+// lookahead: compute the next snapshot's meteo update on the second stream
+// while this interval steps (f3d_run with F3D_OPT_PREFETCH).
+int ctx_run_prepare(f3d_ctx* x, const f3d_met_series* met, const f3d_src_series* src, double end_time,
+                    int lookahead = 0);
 // time = time + dt, iiter = iiter + 1, erumass (Fall3d.f90:112-114)
 void ctx_advance(f3d_ctx* x);
 // the mass-budget log of endstep.f90:51 when due
@@ -122,4 +160,7 @@ int ctx_alloc(f3d_ctx* x, void** p, size_t bytes);
 // the binary32 copies of class ic's settling velocity (vset32, vk32 and
 // its halo-layout copy) after vset changed on the device
 void refresh_fp32_class(f3d_ctx* x, int ic);
+// waits for a look-ahead meteo update in flight and drops it (its chain
+// state is not committed)
+void ctx_prefetch_drop(f3d_ctx* x);
 }  // namespace f3d

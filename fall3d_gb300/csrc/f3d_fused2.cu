@@ -772,7 +772,10 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
 }
 
 template <bool P8>
-__global__ void __launch_bounds__(NT, 1) k_step_fused2(const FusedArgs a, const __grid_constant__ F2Maps maps) {
+// At most 112 registers: four warps of it take 14336 of an SM sub-partition's
+// 16384 registers, which leaves one 64-register warp of the settling-velocity
+// chain room beside it on each sub-partition (a look-ahead meteo update).
+__global__ void __maxnreg__(112) k_step_fused2(const FusedArgs a, const __grid_constant__ F2Maps maps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   fused2_tile<P8>(a, &maps, a.c_in, a.c_out, a.xfirst, 1, (int)(blockIdx.x % a.ncls),
                         (int)(blockIdx.x / a.ncls), smem_raw);

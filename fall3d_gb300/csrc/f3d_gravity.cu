@@ -150,6 +150,7 @@ int gc_divcorr(f3d_ctx* x, double massvol, double massdep, double outmass) {
 
 extern "C" int f3d_set_gravity_current(f3d_ctx* x, const f3d_gravity_current* gc) {
   if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  f3d::ctx_prefetch_drop(x);  // a look-ahead meteo update does not add the radial wind
   if (!gc) {
     x->gc_on = 0;
     return F3D_OK;

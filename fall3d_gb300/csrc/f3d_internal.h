@@ -170,10 +170,14 @@ void launch_reamet_fix(Dims d, int wetdep, double* vz, double* prate, cudaStream
 size_t setvset_scratch_bytes(Dims d, int np);
 // Returns non-zero through *status (device int): 1 = vsettl/get_gama did not
 // converge.  cd_state is a device double (entry value in, exit value out).
+// beside_step != 0: the chain runs as one 64-thread block per SM, sized to
+// fit next to a resident step-kernel block (a look-ahead update on a second
+// stream); the results do not depend on it.
 void launch_setvset(Dims d, int nc, int np, int modv, const double* diam, const double* rhop,
                     const double* psi, const double* sphe, const double* tempe,
                     const double* rho, int aggregate, double vset_factor, double* vset,
-                    int* iters, double* cd_state, void* scratch, int* status, cudaStream_t s);
+                    int* iters, double* cd_state, void* scratch, int* status, cudaStream_t s,
+                    int beside_step = 0);
 // The drag iteration's table-driven log (op 0) and exp (op 1) on n values.
 void launch_dmath_eval(int op, long long n, const double* x, double* y, cudaStream_t s);
 

@@ -58,6 +58,7 @@ module fall3d_gpu
   integer(c_int), parameter :: F3D_OPT_FUSED = 1
   integer(c_int), parameter :: F3D_OPT_TILE = 2
   integer(c_int), parameter :: F3D_OPT_GRAPH = 3
+  integer(c_int), parameter :: F3D_OPT_PREFETCH = 4
 
   ! f3d_grid: the static description of one scenario (reagrd.f90, reagrn.f90, readat.f90)
   type, bind(C) :: f3d_grid

@@ -549,6 +549,18 @@ int f3d_ctx_restore(f3d_ctx* ctx, const char* path);
                             (default); results do not depend on it       */
 #define F3D_OPT_GRAPH 3  /* batches: 1 = replay one CUDA graph per batch step
                             (default), 0 = launch the kernels one by one   */
+#define F3D_OPT_PREFETCH 4 /* f3d_run: 1 = compute the next DBS snapshot's
+                            meteo update (meteo.f90:27-149) on a second,
+                            lowest-priority stream while the current
+                            interval steps, into a second set of the
+                            coefficient fields, and exchange the sets when
+                            the update is due (default); 0 = compute it
+                            when due.  Results do not depend on it.  Not
+                            used with the gravity current, aggregation or
+                            in a batch; the second set is allocated on the
+                            first use (or when the option is set to 1) and
+                            is not counted by f3d_ctx_footprint (without
+                            room for it the updates are made when due).    */
 int f3d_set_option(f3d_ctx* ctx, int key, int value);
 int f3d_get_option(const f3d_ctx* ctx, int key, int* value);
 

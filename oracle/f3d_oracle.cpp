@@ -1918,6 +1918,9 @@ int orc_run(orc_ctx* x, const f3d_met_series* met, const f3d_src_series* src,
     x->run_started = 1;
   } else {
     go_on = x->time < end_time;  // resuming a run that already reached end_time
+    // a later end time than the last call's: the updates it switched off are due again
+    if (x->meteo_time < end_time) x->meteotime = 1;
+    if (x->source_time < end_time) x->sourcetime = 1;
   }
   int steps = 0;
   while (go_on) {

@@ -115,3 +115,26 @@ def test_errors_are_status_codes():
     bad["nx"] = 2
     with pytest.raises(F.F3DError):
         F.Context(synth.Scenario("bad", 0, bad, s.met, s.src, 0.0, 1.0))
+
+
+def test_run_in_pieces_equals_one_run():
+    """f3d_run called with increasing end times continues the one run: the
+    meteo and source updates that the end of a call switched off are due again
+    in the next call (the DBS updates at 1800 s and 3600 s fall in the second
+    and third pieces), bit for bit in the FP32 form and to the oracle's
+    tolerance in the FP64 form."""
+    s = synth.make_scenario("small", seed=41, run_h=1.5, met_dt_h=0.5)
+    for prec in (F.PREC_FP32, F.PREC_FP64):
+        whole = F.Context(s, prec)
+        lw = whole.run()
+        part = F.Context(s, prec)
+        for t in (1000.0, 2500.0, 4000.0, s.end_time):
+            part.run(end_time=t)
+        assert part.state()["iiter"] == whole.state()["iiter"]
+        assert np.array_equal(part.fields()["c"], whole.fields()["c"])
+        assert np.array_equal(part.fields()["vset"], whole.fields()["vset"])
+    o = O.OracleCtx(s, nthreads=8)
+    for t in (1000.0, 2500.0, 4000.0, s.end_time):
+        o.run(end_time=t)
+    assert o.state()["iiter"] == whole.state()["iiter"]
+    assert lw["iiter"][-1] == o.state()["iiter"]

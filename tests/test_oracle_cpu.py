@@ -153,3 +153,18 @@ def test_similarity_bottom_ghost_is_non_finite():
                    O.p(np.ascontiguousarray(f["vdep"][0])), O.p(co["rkver"]), O.p(g["dz"]))
     down = (co["vz"][0] + f["vset"][0][0]) < 0
     assert np.all(~np.isfinite(c[0, 1:-1, 1:-1][down]))
+
+
+def test_run_in_pieces_equals_one_run():
+    """orc_run called with increasing end times continues the one run: the
+    meteo updates at 1800 s and 3600 s fall in later pieces and happen."""
+    s = synth.make_scenario("tiny", seed=42, run_h=1.5, met_dt_h=0.5)
+    whole = O.OracleCtx(s)
+    whole.run()
+    part = O.OracleCtx(s)
+    for t in (1000.0, 2500.0, 4000.0, s.end_time):
+        part.run(end_time=t)
+    assert part.state()["iiter"] == whole.state()["iiter"]
+    fw, fp = whole.fields(), part.fields()
+    for k in ("c", "cdry", "cwet", "vset"):
+        assert np.array_equal(fw[k].view(np.uint64), fp[k].view(np.uint64)), k
