@@ -58,6 +58,7 @@ struct Scen {
 
 struct f3d_batch {
   cudaStream_t stream = nullptr;
+  BatchFork fork;  // second stream of the odd-nx part of the step kernel
   int cap = 0;
   std::vector<Scen> slot;
   std::vector<int> active;  // running slots in batch order
@@ -162,7 +163,7 @@ int enqueue_step(f3d_batch* b, int commit_only_fused) {
   BK(cudaMemsetAsync(b->d_counter, 0, 2 * sizeof(int), b->stream));
   if (!commit_only_fused) launch_setsrc_batch(b->d_aux, b->d_bstep, n, b->max_nc, b->max_nsou, b->stream);
   launch_step_fused_batch(b->shape, b->grid, b->d_item_off, n, b->split, b->total, b->d_counter, b->d_bstep,
-                          b->d_iiter0, commit_only_fused ? 0 : 1, b->max_nz, b->d_maps, b->stream);
+                          b->d_iiter0, commit_only_fused ? 0 : 1, b->max_nz, b->d_maps, b->stream, &b->fork);
   if (!commit_only_fused) {
     launch_cmass2d_batch(b->d_aux, b->d_bstep, n, b->d_red, b->stream);
     launch_batch_advance(b->d_bstep, n, b->stream);
@@ -220,6 +221,9 @@ int f3d_batch_create(int max_scenarios, f3d_batch** out) {
   const int n = max_scenarios;
   bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess;
   ok = ok && cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaStreamCreateWithFlags(&b->fork.s2, cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&b->fork.a, cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&b->fork.b, cudaEventDisableTiming) == cudaSuccess;
   ok = ok && cudaMalloc(&b->d_aux, sizeof(BatchAux) * n) == cudaSuccess;
   ok = ok && cudaMalloc(&b->d_item_off, sizeof(int) * (n + 1)) == cudaSuccess;
   ok = ok && cudaMalloc(&b->d_bstep, sizeof(int) * n) == cudaSuccess;
@@ -259,7 +263,11 @@ int f3d_batch_destroy(f3d_batch* b) {
   cudaFreeHost(b->h_item_off);
   cudaFreeHost(b->h_bstep);
   cudaFreeHost(b->h_iiter0);
+  if (b->fork.s2) cudaStreamSynchronize(b->fork.s2);
   if (b->ev) cudaEventDestroy(b->ev);
+  if (b->fork.a) cudaEventDestroy(b->fork.a);
+  if (b->fork.b) cudaEventDestroy(b->fork.b);
+  if (b->fork.s2) cudaStreamDestroy(b->fork.s2);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return F3D_OK;

@@ -375,8 +375,8 @@ void sizloop_fused(f3d_ctx* x) {
   const FusedArgs a = f3d::ctx_fused_args(x);
   {
     ProfScope ps(x, "step_fused");
-    if (x->opt_tile == 3)
-      launch_step_fused2(a, x->maps2, s);
+    if (x->opt_tile == 3)  // the 112-register build while a look-ahead update runs beside it
+      launch_step_fused2(a, x->maps2, s, x->pref_ready && cudaEventQuery(x->ev_pref) == cudaErrorNotReady);
     else
       launch_step_fused(a, x->opt_tile, s);
   }

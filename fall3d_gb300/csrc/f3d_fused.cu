@@ -82,16 +82,8 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
   const bool edge = !(gx0 >= 1 && gx0 + HX - 1 <= nx && gy0 >= 1 && gy0 + HY - 1 <= ny);
 
   for (int k = threadIdx.x; k <= nz; k += NT) {
-    ZT32 z;
     const float dzk = a.dz[k];
-    const float dzkm = k > 0 ? a.dz[k - 1] : dzk;
-    z.dzz = 2.0f / (dzk + dzkm);
-    z.dzk = 1.0f / dzk;
-    z.dzk_1 = 1.0f / dzkm;
-    z.dzm1 = dzkm;
-    z.l_dz = 1.0f / dzk;
-    z.l_dzdz = 2.0f / (dzk + dzkm);
-    tab[k] = z;
+    tab[k] = make_zt32(dzk, k > 0 ? a.dz[k - 1] : dzk, a.dt);
   }
   const bool wet = a.wet_class && a.wet_class[cls];
   for (int o = threadIdx.x; o < TX * TY; o += NT) {
@@ -117,6 +109,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
   const float dt = a.dt;
   const float dznz = 1.0f / a.dz[nz];
   const float auxvx = a.auxvx, auxvy = a.auxvy;
+  const float dtdx2h = 0.5f * a.dtdx2, dtdy2h = 0.5f * a.dtdy2;
   const int cb0 = gi + (nx + 2) * (gy0 + warp);  // c(gi, gj, 0) of row r = 0
   const int mb0 = (gi - 1) + nx * (gy0 + warp - 1);
 
@@ -186,7 +179,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
     o_0[r] = c1;
     o_p1[r] = c2;
     vk0[r] = vk1;
-    zwork(gb, c1, c2, vk1, vk1, tab[1], dt, w1k[r], w2k[r]);
+    zwork(gb, c1, c2, vk1, vk1, tab[1], w1k[r], w2k[r]);
     w2km[r] = w2k[r];
     rc[r] = gb;  // diffz window: c(0) is the bottom ghost
     if (gi >= i0 && gi <= oi1 && gj >= j0 && gj <= oj1) {
@@ -250,7 +243,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
                 if (gi == nx && gj == ny) cout[d.C(nx + 1, ny + 1, nz + 1)] = clip0(o_p1[r]);
               }
             }
-            zwork(o_0[r], o_p1[r], o_p2, vkp, vk0[r], zn, dt, w1n, w2n);
+            zwork(o_0[r], o_p1[r], o_p2, vkp, vk0[r], zn, w1n, w2n);
           } else {  // t == nz: work(nz+1,1) (advctzc.f90:58-64)
             w1n = dt * vk0[r] * (gtop[r] - o_0[r]) * dznz;
             w2n = w2k[r];
@@ -376,31 +369,19 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
       rc[r] = (STEADY || t <= nz) ? s2[r] : gtop[r];
       // 1/rho at k and k+1, K*rho at k (carried) and k+1
       const float lb = sb[F_L1 * NP + p];
-      float work;
       if (STEADY || (k > 1 && k < nz)) {
         const float lc = sb[F_L * NP + p], pc = sb[F_PZ * NP + p];
-        const float gradt = 0.5f * (pc + pb[r]) * (rc[r] * lc - rb[r] * lb) * zk.l_dz;
-        work = dt * (gradt - fprev[r]) * zk.l_dzdz;
-        fprev[r] = gradt;
+        s3[r] = diffz_mid(pc, pb[r], rc[r], lc, rb[r], lb, fprev[r], zk);
         pb[r] = pc;
       } else if (k == 1) {
         const float lc = sb[F_L * NP + p], pc = sb[F_PZ * NP + p];
-        const float qt = rc[r] * lc - rb[r] * lb;
-        const float gradt = pc * qt * tab[1].l_dz;
-        const float g = pb[r] * (rb[r] * lb - ra[r] * lb) * tab[0].l_dz;
-        const float gradb = g > 0.0f ? g : 0.0f;  // MAX(0,g): 0 for NaN
-        work = dt * (gradt - gradb) * tab[1].l_dzdz;
-        fprev[r] = 0.5f * (pc + pb[r]) * qt * tab[1].l_dz;
+        s3[r] = diffz_bottom(pc, pb[r], rc[r], lc, rb[r], lb, ra[r], fprev[r], tab[0], tab[1]);
         pb[r] = pc;
       } else {  // k == nz
         const int m = ((kin >> r & 1u) ? mb0 + NW * r * nx : 0) + (nz - 2) * pl;
         const float la = __ldg(a.lrho + m), pa = __ldg(a.pkz + m);
-        const float g = pb[r] * (rc[r] * lb - rb[r] * lb) * tab[nz].l_dz;
-        const float gradt = g < 0.0f ? g : 0.0f;
-        const float gradb = pa * (rb[r] * lb - ra[r] * la) * tab[nz - 1].l_dz;
-        work = dt * (gradt - gradb) * tab[nz].l_dz;
+        s3[r] = diffz_top(pa, la, pb[r], rc[r], rb[r], lb, ra[r], tab[nz - 1], tab[nz]);
       }
-      s3[r] = rb[r] + work;
       if constexpr (EDGE) {
         if (!(kin >> r & 1u)) s3[r] = gprev[r];  // ghost value of plane k (unchanged by the sweeps)
         gprev[r] = s2[r];
@@ -417,11 +398,11 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
         const float lm = shup(l0), lp = shdn(l0);
         const float Pm = shup(P0), Pp = shdn(P0);
         if constexpr (EDGE) {
-          float u = diff_mid(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2);
-          if (gi == 1 || gi == nx) u = diff_cell(gi == 1, gi == nx, cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2);
+          float u = diff_mid(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, dtdx2h);
+          if (gi == 1 || gi == nx) u = diff_cell(gi == 1, gi == nx, cm, c0, cp, lm, l0, lp, Pm, P0, Pp, dtdx2h);
           out[r] = (kin >> r & 1u) ? u : c0;
         } else {
-          out[r] = diff_mid(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2);
+          out[r] = diff_mid(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, dtdx2h);
         }
       }
     };
@@ -439,10 +420,10 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
         if constexpr (EDGE) {
           const int gj = gy0 + hy;
           const float u = diff_cell(gj == 1, gj == ny, P1s[hm], in[r], P1s[hp], L[hm], L[p], L[hp], PY[hm],
-                                    PY[p], PY[hp], a.dtdy2);
+                                    PY[p], PY[hp], dtdy2h);
           out[r] = (kin >> r & 1u) ? u : in[r];
         } else {
-          out[r] = diff_mid(P1s[hm], in[r], P1s[hp], L[hm], L[p], L[hp], PY[hm], PY[p], PY[hp], a.dtdy2);
+          out[r] = diff_mid(P1s[hm], in[r], P1s[hp], L[hm], L[p], L[hp], PY[hm], PY[p], PY[hp], dtdy2h);
         }
       }
     };
@@ -521,7 +502,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
         const float2 O0 = pk(o_0, q), O1 = pk(o_p1, q), VK0 = pk(vk0, q);
         const float2 W1K = pk(w1k, q), W2KM = pk(w2km, q), W2K = pk(w2k, q);
         float2 w1n, w2n;
-        zwork2(O0, O1, o2, vkp, VK0, zn, dt, w1n, w2n);
+        zwork2(O0, O1, o2, vkp, VK0, zn, w1n, w2n);
         s1v[q] = line_update2(O0, VK0, W1K, w1n, W2K, W2KM, w2n);
         up(w2km, q, W2K);
         up(w2k, q, w2n);
@@ -588,12 +569,10 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
       up(rb, q, RB);
       up(rc, q, RC);
       const float2 lb = ld2(sb + F_L1 * NP, p0), lc = ld2(sb + F_L * NP, p0), pc = ld2(sb + F_PZ * NP, p0);
-      const float2 gradt =
-          mul2(mul2(mul2(splat(0.5f), add2(pc, pk(pb, q))), sub2(mul2(RC, lc), mul2(RB, lb))), splat(zk.l_dz));
-      const float2 work = mul2(mul2(splat(dt), sub2(gradt, pk(fprev, q))), splat(zk.l_dzdz));
-      up(fprev, q, gradt);
+      float2 fp = pk(fprev, q);
+      s3v[q] = diffz_mid2(pc, pk(pb, q), RC, lc, RB, lb, fp, zk);
+      up(fprev, q, fp);
       up(pb, q, pc);
-      s3v[q] = add2(RB, work);
     }
     // D: diffx and diffy
     auto dif_x2 = [&](const float2* in, float2* out) {
@@ -601,7 +580,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
       for (int q = 0; q < RP; ++q) {
         const int p0 = rowpos(q);
         const float2 l0 = ld2(sb + F_L1 * NP, p0), P0 = ld2(sb + F_PX * NP, p0), c0 = in[q];
-        out[q] = diff_mid2(shup2(c0), c0, shdn2(c0), shup2(l0), l0, shdn2(l0), shup2(P0), P0, shdn2(P0), a.dtdx2);
+        out[q] = diff_mid2(shup2(c0), c0, shdn2(c0), shup2(l0), l0, shdn2(l0), shup2(P0), P0, shdn2(P0), dtdx2h);
       }
     };
     auto dif_y2 = [&](const float2* in, float2* out) {
@@ -618,7 +597,7 @@ __device__ __forceinline__ void fused_tile(const FusedArgs& a, const float* c_in
       for (int q = 0; q < RP; ++q) {
         const int p0 = rowpos(q);
         out[q] = diff_mid2(ld2(P1s - HX, p0), in[q], ld2(P1s + HX, p0), ld2(L - HX, p0), ld2(L, p0), ld2(L + HX, p0),
-                           ld2(PY - HX, p0), ld2(PY, p0), ld2(PY + HX, p0), a.dtdy2);
+                           ld2(PY - HX, p0), ld2(PY, p0), ld2(PY + HX, p0), dtdy2h);
       }
     };
     float2 s3a[RP], s4v[RP];
@@ -794,10 +773,11 @@ int fused_batch_grid(int shape, int max_nz) {
 
 void launch_step_fused_batch(int shape, int grid, const int* item_off, int nscen, int split, int total,
                              int* counter, const int* bstep, const int* iiter0, int commit, int max_nz,
-                             const F2Maps* maps, cudaStream_t s) {
+                             const F2Maps* maps, cudaStream_t s, const BatchFork* fork) {
   switch (shape) {
     case 3:
-      launch_step_fused2_batch(grid, item_off, nscen, split, total, counter, bstep, iiter0, commit, max_nz, maps, s);
+      launch_step_fused2_batch(grid, item_off, nscen, split, total, counter, bstep, iiter0, commit, max_nz, maps, s,
+                               fork);
       break;
     case 1:
       launch_fused_batch_t<64, 16>(grid, item_off, nscen, counter, bstep, iiter0, commit, max_nz, s);

@@ -67,7 +67,9 @@ inline int halo_pitch(int nx) { return (nx + 2 + 3) & ~3; }
 // tile region (x by y) / threads: 0 = 32x32 / 256 (default), 1 = 32x64 / 512,
 // 2 = 32x32 / 512, 3 = 64x32 / 512 with two columns per lane.
 void launch_step_fused(const FusedArgs& a, int shape, cudaStream_t s);
-void launch_step_fused2(const FusedArgs& a, const F2Maps& maps, cudaStream_t s);
+// beside != 0: the 112-register build, which leaves room for a look-ahead
+// meteo update's settling chain on the same SMs (same results)
+void launch_step_fused2(const FusedArgs& a, const F2Maps& maps, cudaStream_t s, int beside = 0);
 // met fields (nx,ny,nz) -> halo layout of row pitch hp (ghost entries untouched)
 void launch_to_halo(Dims d, int hp, int nfield, const float* const* src, float* const* dst, cudaStream_t s);
 // tiles of one class of an nx x ny grid for a tile shape
@@ -82,15 +84,22 @@ int upload_batch_args2(const FusedArgs* h, int n, cudaStream_t s);  // the shape
 int fused2_batch_grid(int max_nz);
 // items [0, split) belong to scenarios with an even nx (two counters)
 // maps: the scenarios' tensor maps (device array in batch order)
+// fork: when both parts exist, the odd-nx part runs on fork->s2 as a
+// parallel branch (fork->a recorded on s, fork->b on s2, s waits for it), so
+// that its blocks fill the SMs the even-nx part's last blocks leave free
+struct BatchFork {
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+};
 void launch_step_fused2_batch(int grid, const int* item_off, int nscen, int split, int total, int* counter,
                               const int* bstep, const int* iiter0, int commit, int max_nz, const F2Maps* maps,
-                              cudaStream_t s);
+                              cudaStream_t s, const BatchFork* fork = nullptr);
 // sets the kernel's shared-memory limit and returns its persistent grid (-1 on error)
 int fused_batch_grid(int shape, int max_nz);
 // counter: two ints; split / total: see launch_step_fused2_batch (shape 3)
 void launch_step_fused_batch(int shape, int grid, const int* item_off, int nscen, int split, int total,
                              int* counter, const int* bstep, const int* iiter0, int commit, int max_nz,
-                             const F2Maps* maps, cudaStream_t s);
+                             const F2Maps* maps, cudaStream_t s, const BatchFork* fork = nullptr);
 void launch_vk32(long long n, int nc, const float* vz, const float* vset, float* vk, cudaStream_t s);
 void launch_wet_lambda(long long n, double dt, const double* prate, double* lam, cudaStream_t s);
 void launch_fp32_coeffs(long long n, const double* rho, const double* rkh1, const double* rkhor,

@@ -140,16 +140,8 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   for (int k = threadIdx.x; k <= nz; k += NT) {
-    ZT32 z;
     const float dzk = a.dz[k];
-    const float dzkm = k > 0 ? a.dz[k - 1] : dzk;
-    z.dzz = 2.0f / (dzk + dzkm);
-    z.dzk = 1.0f / dzk;
-    z.dzk_1 = 1.0f / dzkm;
-    z.dzm1 = dzkm;
-    z.l_dz = 1.0f / dzk;
-    z.l_dzdz = 2.0f / (dzk + dzkm);
-    tab[k] = z;
+    tab[k] = make_zt32(dzk, k > 0 ? a.dz[k - 1] : dzk, a.dt);
   }
   const bool wet = a.wet_class && a.wet_class[cls];
   __shared__ int s_kzmax;  // the highest wet layer of the tile: above it the wet code is skipped
@@ -179,6 +171,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
   const float dt = a.dt;
   const float dznz = 1.0f / a.dz[nz];
   const float auxvx = a.auxvx, auxvy = a.auxvy;
+  const float dtdx2h = 0.5f * a.dtdx2, dtdy2h = 0.5f * a.dtdy2;
 
   // ------------------------------------------------ per-position state
   // bit 2r+c: row r (gj = gy0 + 2*warp + r), column c (gi + c); a warp owns
@@ -306,7 +299,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
       cmp(o_p1[r], c) = c2;
       cmp(vk0[r], c) = vk1;
       float w1, w2;
-      zwork(gb, c1, c2, vk1, vk1, tab[1], dt, w1, w2);
+      zwork(gb, c1, c2, vk1, vk1, tab[1], w1, w2);
       cmp(w1k[r], c) = w1;
       cmp(w2k[r], c) = w2;
       cmp(w2km[r], c) = w2;
@@ -389,7 +382,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
               }
               gtop[r] = o_p2;
             }
-            zwork2(o_0[r], o_p1[r], o_p2, vkp, vk0[r], zn, dt, w1n, w2n);
+            zwork2(o_0[r], o_p1[r], o_p2, vkp, vk0[r], zn, w1n, w2n);
           } else {  // t == nz: work(nz+1,1) (advctzc.f90:58-64)
             w1n = mul2(mul2(mul2(splat(dt), vk0[r]), sub2(gtop[r], o_0[r])), splat(dznz));
             w2n = w2k[r];
@@ -524,22 +517,13 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
       rc[r] = (STEADY || t <= nz) ? s2[r] : gtop[r];  // c(nz+1) is the top ghost (diffz.f90:54)
       const float2 lb = lds2(at(F_L1, r));
       lbv[r] = lb;
-      float2 work;
       if (STEADY || (k > 1 && k < nz)) {
         const float2 lc = lds2(at(F_L, r)), pc = lds2(at(F_PZ, r));
-        const float2 gradt =
-            mul2(mul2(mul2(splat(0.5f), add2(pc, pb[r])), sub2(mul2(rc[r], lc), mul2(rb[r], lb))), splat(zk.l_dz));
-        work = mul2(mul2(splat(dt), sub2(gradt, fprev[r])), splat(zk.l_dzdz));
-        fprev[r] = gradt;
+        s3[r] = diffz_mid2(pc, pb[r], rc[r], lc, rb[r], lb, fprev[r], zk);
         pb[r] = pc;
       } else if (k == 1) {
         const float2 lc = lds2(at(F_L, r)), pc = lds2(at(F_PZ, r));
-        const float2 qt = sub2(mul2(rc[r], lc), mul2(rb[r], lb));
-        const float2 gradt = mul2(mul2(pc, qt), splat(tab[1].l_dz));
-        const float2 g = mul2(mul2(pb[r], sub2(mul2(rb[r], lb), mul2(ra[r], lb))), splat(tab[0].l_dz));
-        const float2 gradb = make_float2(g.x > 0.0f ? g.x : 0.0f, g.y > 0.0f ? g.y : 0.0f);  // MAX(0,g)
-        work = mul2(mul2(splat(dt), sub2(gradt, gradb)), splat(tab[1].l_dzdz));
-        fprev[r] = mul2(mul2(mul2(splat(0.5f), add2(pc, pb[r])), qt), splat(tab[1].l_dz));
+        s3[r] = diffz_bottom2(pc, pb[r], rc[r], lc, rb[r], lb, ra[r], fprev[r], tab[0], tab[1]);
         pb[r] = pc;
       } else {  // k == nz
         float2 la, pa;
@@ -550,12 +534,8 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
           cmp(la, c) = __ldg(a.lrhoh + hh);
           cmp(pa, c) = __ldg(a.pkzh + hh);
         }
-        const float2 g = mul2(mul2(pb[r], sub2(mul2(rc[r], lb), mul2(rb[r], lb))), splat(tab[nz].l_dz));
-        const float2 gradt = make_float2(g.x < 0.0f ? g.x : 0.0f, g.y < 0.0f ? g.y : 0.0f);
-        const float2 gradb = mul2(mul2(pa, sub2(mul2(rb[r], lb), mul2(ra[r], la))), splat(tab[nz - 1].l_dz));
-        work = mul2(mul2(splat(dt), sub2(gradt, gradb)), splat(tab[nz].l_dz));
+        s3[r] = diffz_top2(pa, la, pb[r], rc[r], rb[r], lb, ra[r], tab[nz - 1], tab[nz]);
       }
-      s3[r] = add2(rb[r], work);
       if constexpr (EDGE) {
         s3[r] = sel2(km(r, 0), km(r, 1), s3[r], gprev[r]);  // ghosts keep their value
         gprev[r] = s2[r];
@@ -570,20 +550,20 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
           // the face flux 0.5*(P(q)+P(q+1))*(c(q+1)/rho(q+1) - c(q)/rho(q)) is gradr at q and
           // gradl at q+1 (diffx.f90:34-40): computed once per face, the left one by shuffle
           const float2 q0 = mul2(c0, l0);
-          const float2 fr = mul2(mul2(splat(0.5f), add2(right2(P0), P0)), sub2(right2(q0), q0));
-          out[r] = add2(c0, mul2(splat(a.dtdx2), sub2(fr, left2(fr))));
+          const float2 fr = diff_face2(right2(P0), P0, right2(q0), q0);
+          out[r] = diff_apply2(dtdx2h, fr, left2(fr), c0);
           continue;
         }
         const float2 cm = left2(c0), cp = right2(c0), lm = left2(l0), lp = right2(l0), Pm = left2(P0),
                      Pp = right2(P0);
-        float2 u = diff_mid2(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, a.dtdx2);
+        float2 u = diff_mid2(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, dtdx2h);
         if constexpr (EDGE) {
 #pragma unroll
           for (int c = 0; c < 2; ++c) {
             const int g = gi + c;
             if (g == 1 || g == nx)
               cmp(u, c) = diff_cell(g == 1, g == nx, cmp(cm, c), cmp(c0, c), cmp(cp, c), cmp(lm, c), cmp(l0, c),
-                                    cmp(lp, c), cmp(Pm, c), cmp(P0, c), cmp(Pp, c), a.dtdx2);
+                                    cmp(lp, c), cmp(Pm, c), cmp(P0, c), cmp(Pp, c), dtdx2h);
           }
           out[r] = sel2(km(r, 0), km(r, 1), u, c0);
         } else {
@@ -610,11 +590,11 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
         const float2 qp[RPW] = {q[1], lds2(P1 + 2 * HX)};
         // three faces: below the pair, between its rows (gradr of row 0 and
         // gradl of row 1, the same operations on the same values), above it
-        const float2 fb = mul2(mul2(splat(0.5f), add2(P0v[0], Pmv[0])), sub2(q[0], qm[0]));
-        const float2 fm = mul2(mul2(splat(0.5f), add2(Ppv[0], P0v[0])), sub2(qp[0], q[0]));
-        const float2 ft = mul2(mul2(splat(0.5f), add2(Ppv[1], P0v[1])), sub2(qp[1], q[1]));
-        out[0] = add2(in[0], mul2(splat(a.dtdy2), sub2(fm, fb)));
-        out[1] = add2(in[1], mul2(splat(a.dtdy2), sub2(ft, fm)));
+        const float2 fb = diff_face2(P0v[0], Pmv[0], q[0], qm[0]);
+        const float2 fm = diff_face2(Ppv[0], P0v[0], qp[0], q[0]);
+        const float2 ft = diff_face2(Ppv[1], P0v[1], qp[1], q[1]);
+        out[0] = diff_apply2(dtdy2h, fm, fb, in[0]);
+        out[1] = diff_apply2(dtdy2h, ft, fm, in[1]);
         return;
       }
 #pragma unroll
@@ -635,13 +615,13 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
 #pragma unroll
             for (int c = 0; c < 2; ++c)
               cmp(u, c) = diff_cell(gj == 1, gj == ny, cmp(cm, c), cmp(in[r], c), cmp(cp, c), cmp(lm, c),
-                                    cmp(lbv[r], c), cmp(lp, c), cmp(Pm, c), cmp(P0, c), cmp(Pp, c), a.dtdy2);
+                                    cmp(lbv[r], c), cmp(lp, c), cmp(Pm, c), cmp(P0, c), cmp(Pp, c), dtdy2h);
           } else {
-            u = diff_mid2(cm, in[r], cp, lm, lbv[r], lp, Pm, P0, Pp, a.dtdy2);
+            u = diff_mid2(cm, in[r], cp, lm, lbv[r], lp, Pm, P0, Pp, dtdy2h);
           }
           out[r] = sel2(km(r, 0), km(r, 1), u, in[r]);
         } else {
-          out[r] = diff_mid2(cm, in[r], cp, lm, lbv[r], lp, Pm, P0, Pp, a.dtdy2);
+          out[r] = diff_mid2(cm, in[r], cp, lm, lbv[r], lp, Pm, P0, Pp, dtdy2h);
         }
       }
     };
@@ -772,10 +752,19 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
 }
 
 template <bool P8>
-// At most 112 registers: four warps of it take 14336 of an SM sub-partition's
-// 16384 registers, which leaves one 64-register warp of the settling-velocity
-// chain room beside it on each sub-partition (a look-ahead meteo update).
-__global__ void __maxnreg__(112) k_step_fused2(const FusedArgs a, const __grid_constant__ F2Maps maps) {
+__global__ void __launch_bounds__(NT, 1) k_step_fused2(const FusedArgs a, const __grid_constant__ F2Maps maps) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  fused2_tile<P8>(a, &maps, a.c_in, a.c_out, a.xfirst, 1, (int)(blockIdx.x % a.ncls),
+                        (int)(blockIdx.x / a.ncls), smem_raw);
+}
+
+// The same step with at most 112 registers, launched while a look-ahead
+// meteo update runs on the context's second stream: four warps of it take
+// 14336 of an SM sub-partition's 16384 registers, which leaves one
+// 64-register warp of the settling-velocity chain room beside it on each
+// sub-partition.  Same operations, same results.
+template <bool P8>
+__global__ void __maxnreg__(112) k_step_fused2_beside(const FusedArgs a, const __grid_constant__ F2Maps maps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   fused2_tile<P8>(a, &maps, a.c_in, a.c_out, a.xfirst, 1, (int)(blockIdx.x % a.ncls),
                         (int)(blockIdx.x / a.ncls), smem_raw);
@@ -831,16 +820,17 @@ __global__ void k_to_halo(Dims d, int hp, const float* src, float* dst) {
 
 }  // namespace
 
-void launch_step_fused2(const FusedArgs& a, const F2Maps& maps, cudaStream_t s) {
+void launch_step_fused2(const FusedArgs& a, const F2Maps& maps, cudaStream_t s, int beside) {
   const int tiles = ((a.d.nx + TX - 1) / TX) * ((a.d.ny + TY - 1) / TY);
   const size_t sm = fused2_smem(a.d.nz);
-  if (a.pair_aligned) {
-    cudaFuncSetAttribute(k_step_fused2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_step_fused2<true><<<tiles * a.ncls, NT, sm, s>>>(a, maps);
-  } else {
-    cudaFuncSetAttribute(k_step_fused2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_step_fused2<false><<<tiles * a.ncls, NT, sm, s>>>(a, maps);
-  }
+  auto go = [&](auto kernel) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    kernel<<<tiles * a.ncls, NT, sm, s>>>(a, maps);
+  };
+  if (a.pair_aligned)
+    beside ? go(k_step_fused2_beside<true>) : go(k_step_fused2<true>);
+  else
+    beside ? go(k_step_fused2_beside<false>) : go(k_step_fused2<false>);
   count_launch();
 }
 
@@ -916,16 +906,27 @@ int fused2_batch_grid(int max_nz) {
 
 void launch_step_fused2_batch(int grid, const int* item_off, int nscen, int split, int total, int* counter,
                               const int* bstep, const int* iiter0, int commit, int max_nz, const F2Maps* maps,
-                              cudaStream_t s) {
+                              cudaStream_t s, const BatchFork* fork) {
   const size_t sm = fused2_smem(max_nz);
+  const bool both = split > 0 && total > split && fork && fork->s2;
+  cudaStream_t s_odd = s;
+  if (both) {  // the two parts are independent (their own scenarios and counters)
+    cudaEventRecord(fork->a, s);
+    cudaStreamWaitEvent(fork->s2, fork->a, 0);
+    s_odd = fork->s2;
+  }
   if (split > 0) {
     k_step_fused2_batch<true><<<grid, NT, sm, s>>>(item_off, nscen, 0, split, counter, bstep, iiter0, commit, maps);
     count_launch();
   }
   if (total > split) {
-    k_step_fused2_batch<false><<<grid, NT, sm, s>>>(item_off, nscen, split, total, counter + 1, bstep, iiter0,
-                                                     commit, maps);
+    k_step_fused2_batch<false><<<grid, NT, sm, s_odd>>>(item_off, nscen, split, total, counter + 1, bstep, iiter0,
+                                                         commit, maps);
     count_launch();
+  }
+  if (both) {
+    cudaEventRecord(fork->b, fork->s2);
+    cudaStreamWaitEvent(s, fork->b, 0);
   }
 }
 

@@ -1,10 +1,13 @@
 // f3d_fused_math.cuh -- device arithmetic shared by the fused step kernels
 // (f3d_fused.cu: one column per lane; f3d_fused2.cu: two columns per lane).
 //
-// Every formula keeps the reference's binary64 operation order in binary32
-// (sizloop's routines, cited at each function); the float2 versions apply
-// the same operations to both values of a pair, so all kernel variants give
-// the same bits for the same cell.
+// Every formula is the reference's (sizloop's routines, cited at each
+// function) in binary32, with products that share a factor contracted into
+// one fused multiply-add (__fmaf_rn, explicit, so that no compiler choice
+// enters) and the plane's and the step's constant factors multiplied once;
+// the float2 versions apply the scalar ones to both values of a pair, and
+// every kernel variant calls these functions, so all of them give the same
+// bits for the same cell.
 #pragma once
 
 #include <type_traits>
@@ -18,7 +21,27 @@ constexpr unsigned FULL = 0xffffffffu;
 
 struct ZT32 {
   float dzz, dzk, dzk_1, dzm1, l_dz, l_dzdz;
+  // the factors with dt of this plane (the same in every kernel)
+  float dt_dzz, dt_dzk_1, w2f, hl_dz, dt_l_dzdz, dt_l_dz;
 };
+
+// Per-plane factors of advctzc.f90:19-40 (dz(k), dz(k-1)) and diffz.f90:22-62.
+__device__ __forceinline__ ZT32 make_zt32(float dzk, float dzkm, float dt) {
+  ZT32 z;
+  z.dzz = 2.0f / (dzk + dzkm);
+  z.dzk = 1.0f / dzk;
+  z.dzk_1 = 1.0f / dzkm;
+  z.dzm1 = dzkm;
+  z.l_dz = 1.0f / dzk;
+  z.l_dzdz = 2.0f / (dzk + dzkm);
+  z.dt_dzz = dt * z.dzz;
+  z.dt_dzk_1 = dt * z.dzk_1;
+  z.w2f = ((dt * 0.5f) * z.dzm1) * z.dzz;
+  z.hl_dz = 0.5f * z.l_dz;
+  z.dt_l_dzdz = dt * z.l_dzdz;
+  z.dt_l_dz = dt * z.l_dz;
+  return z;
+}
 
 // 0.5*(SIGN(1,dr)+SIGN(1,dl))*MIN(|dr|,|dl|) (advctx.f90:40): +-min when
 // the signs agree, +0 when they differ.  Exact for every non-NaN dr, dl
@@ -31,23 +54,24 @@ __device__ __forceinline__ float minmod(float dr, float dl) {
   return diff ? 0.0f : __uint_as_float(__float_as_uint(m) | sr);
 }
 
-__device__ __forceinline__ void zwork(float cm, float c0, float cp, float vk, float vk_1,
-                                      const ZT32& z, float dt, float& w1, float& w2) {
-  const float vk_12 = 0.5f * (vk + vk_1);
-  w1 = dt * (vk * c0 - vk_1 * cm) * z.dzz;
+// work(k,1), work(k,2) of advctzc.f90:36-44: dt*(vk*c0 - vk_1*cm)*dzz and
+// dt*0.5*dz(k-1)*(1 - |vk_12|*dt/dz(k-1))*sigma*|vk_12|*dzz.
+__device__ __forceinline__ void zwork(float cm, float c0, float cp, float vk, float vk_1, const ZT32& z,
+                                      float& w1, float& w2) {
+  const float avk = fabsf(0.5f * (vk + vk_1));
+  w1 = z.dt_dzz * __fmaf_rn(vk, c0, -(vk_1 * cm));
   const float sigma = minmod((cp - c0) * z.dzk, (c0 - cm) * z.dzk_1);
-  const float Crk = fabsf(vk_12) * dt * z.dzk_1;
-  w2 = dt * 0.5f * z.dzm1 * (1.0f - Crk) * sigma * fabsf(vk_12) * z.dzz;
+  w2 = ((z.w2f * __fmaf_rn(-avk, z.dt_dzk_1, 1.0f)) * sigma) * avk;
 }
 
-// work(q,1), work(q,2) of advctx.f90:24-44 at line position q.
+// work(q,1), work(q,2) of advctx.f90:24-44 at line position q:
+// auxv*(vq*c0 - vq_1*cm) and dt*0.5*(1 - auxv*|vq_12|)*sigma*|vq_12|.
 __device__ __forceinline__ void line_work(float cm, float c0, float cp, float vq, float vq_1,
                                           float auxv, float invd, float dt, float& w1, float& w2) {
-  const float vq_12 = 0.5f * (vq + vq_1);
-  w1 = auxv * (vq * c0 - vq_1 * cm);
+  const float avq = fabsf(0.5f * (vq + vq_1));
+  w1 = auxv * __fmaf_rn(vq, c0, -(vq_1 * cm));
   const float sigma = minmod((cp - c0) * invd, (c0 - cm) * invd);
-  const float Cri = auxv * fabsf(vq_12);
-  w2 = dt * 0.5f * (1.0f - Cri) * sigma * fabsf(vq_12);
+  w2 = (((dt * 0.5f) * __fmaf_rn(-auxv, avq, 1.0f)) * sigma) * avq;
 }
 
 // The update of advctx.f90:48-54 (and advctzc.f90:66-72).
@@ -59,17 +83,24 @@ __device__ __forceinline__ float line_update(float c0, float vq, float w1, float
   return c0 - a - b;
 }
 
-// diffx/diffy cell of Sources/diffx.f90:20-55 with l = 1/rho, P = rkh*rho.
-// MAX(0,g) / MIN(0,g) of the reference keep 0 for a NaN g.
+// diffx/diffy cell of Sources/diffx.f90:20-55 with l = 1/rho, P = rkh*rho
+// and dtdx2h = 0.5*dt/dx^2 (the 0.5 of the face average folded in): a face
+// flux is (P(q)+P(q+1))*(c(q+1)*l(q+1) - c(q)*l(q)), the same value for the
+// two cells that share it.  MAX(0,g) / MIN(0,g) of the reference keep 0 for
+// a NaN g.
+__device__ __forceinline__ float diff_face(float Pa, float Pb, float qa, float qb) { return (Pa + Pb) * (qa - qb); }
 __device__ __forceinline__ float diff_mid(float cm, float c0, float cp, float lm, float l0, float lp,
-                                          float Pm, float P0, float Pp, float dtdx2) {
-  const float gradr = 0.5f * (Pp + P0) * (cp * lp - c0 * l0);
-  const float gradl = 0.5f * (P0 + Pm) * (c0 * l0 - cm * lm);
-  return c0 + dtdx2 * (gradr - gradl);
+                                          float Pm, float P0, float Pp, float dtdx2h) {
+  const float c0l0 = c0 * l0;
+  const float gradr = diff_face(Pp, P0, cp * lp, c0l0);
+  const float gradl = diff_face(P0, Pm, c0l0, cm * lm);
+  return __fmaf_rn(dtdx2h, gradr - gradl, c0);
 }
+// the first and last cell of a line (diffx.f90:22-33, 44-55): faces
+// without the average, so the full dt/dx^2 = 2*dtdx2h
 __device__ __forceinline__ float diff_cell(bool first, bool last, float cm, float c0, float cp,
                                            float lm, float l0, float lp, float Pm, float P0,
-                                           float Pp, float dtdx2) {
+                                           float Pp, float dtdx2h) {
   float gradr, gradl;
   if (first) {
     gradr = Pp * (cp * lp - c0 * l0);
@@ -80,9 +111,39 @@ __device__ __forceinline__ float diff_cell(bool first, bool last, float cm, floa
     gradr = g < 0.0f ? g : 0.0f;
     gradl = Pm * (c0 * l0 - cm * lm);
   } else {
-    return diff_mid(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, dtdx2);
+    return diff_mid(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, dtdx2h);
   }
-  return c0 + dtdx2 * (gradr - gradl);
+  return __fmaf_rn(2.0f * dtdx2h, gradr - gradl, c0);
+}
+
+// diffz.f90:22-62 at plane k with c(k-1) = ra, c(k) = rb, c(k+1) = rc,
+// l = 1/rho at k (lb), k+1 (lc) and k-1 (la), P = rkver*rho at k (pb),
+// k+1 (pc) and k-1 (pa).  An interior plane: the face flux above k (kept in
+// fprev for the next plane) minus the one below.
+__device__ __forceinline__ float diffz_mid(float pc, float pb, float rc, float lc, float rb, float lb,
+                                           float& fprev, const ZT32& zk) {
+  const float gradt = ((pc + pb) * __fmaf_rn(rc, lc, -(rb * lb))) * zk.hl_dz;
+  const float r = __fmaf_rn(zk.dt_l_dzdz, gradt - fprev, rb);
+  fprev = gradt;
+  return r;
+}
+// the first plane (diffz.f90:24-33): the ground face MAX(0, ...)
+__device__ __forceinline__ float diffz_bottom(float pc, float pb, float rc, float lc, float rb, float lb, float ra,
+                                              float& fprev, const ZT32& z0, const ZT32& z1) {
+  const float qt = __fmaf_rn(rc, lc, -(rb * lb));
+  const float gradt = (pc * qt) * z1.l_dz;
+  const float g = (pb * __fmaf_rn(rb, lb, -(ra * lb))) * z0.l_dz;
+  const float gradb = g > 0.0f ? g : 0.0f;
+  fprev = ((pc + pb) * qt) * z1.hl_dz;
+  return __fmaf_rn(z1.dt_l_dzdz, gradt - gradb, rb);
+}
+// the last plane (diffz.f90:50-61): the top face MIN(0, ...)
+__device__ __forceinline__ float diffz_top(float pa, float la, float pb, float rc, float rb, float lb, float ra,
+                                           const ZT32& znm1, const ZT32& znz) {
+  const float g = (pb * __fmaf_rn(rc, lb, -(rb * lb))) * znz.l_dz;
+  const float gradt = g < 0.0f ? g : 0.0f;
+  const float gradb = (pa * __fmaf_rn(rb, lb, -(ra * la))) * znm1.l_dz;
+  return __fmaf_rn(znz.dt_l_dz, gradt - gradb, rb);
 }
 
 __device__ __forceinline__ float clip0(float x) { return x > 0.0f ? x : 0.0f; }  // MAX(0,x)
@@ -112,42 +173,53 @@ __device__ __forceinline__ float2 abs2(float2 v) { return make_float2(fabsf(v.x)
 __device__ __forceinline__ float2 shup2(float2 v) { return make_float2(shup(v.x), shup(v.y)); }
 __device__ __forceinline__ float2 shdn2(float2 v) { return make_float2(shdn(v.x), shdn(v.y)); }
 
-__device__ __forceinline__ void zwork2(float2 cm, float2 c0, float2 cp, float2 vk, float2 vk_1,
-                                       const ZT32& z, float dt, float2& w1, float2& w2) {
-  const float2 vk_12 = mul2(splat(0.5f), add2(vk, vk_1));
-  w1 = mul2(mul2(splat(dt), sub2(mul2(vk, c0), mul2(vk_1, cm))), splat(z.dzz));
-  const float2 dr = mul2(sub2(cp, c0), splat(z.dzk)), dl = mul2(sub2(c0, cm), splat(z.dzk_1));
-  const float2 sigma = make_float2(minmod(dr.x, dl.x), minmod(dr.y, dl.y));
-  const float2 avk = abs2(vk_12);
-  const float2 Crk = mul2(mul2(avk, splat(dt)), splat(z.dzk_1));
-  w2 = mul2(mul2(mul2(mul2(splat(dt * 0.5f * z.dzm1), sub2(splat(1.0f), Crk)), sigma), avk), splat(z.dzz));
+__device__ __forceinline__ void zwork2(float2 cm, float2 c0, float2 cp, float2 vk, float2 vk_1, const ZT32& z,
+                                       float2& w1, float2& w2) {
+  zwork(cm.x, c0.x, cp.x, vk.x, vk_1.x, z, w1.x, w2.x);
+  zwork(cm.y, c0.y, cp.y, vk.y, vk_1.y, z, w1.y, w2.y);
 }
 
 __device__ __forceinline__ void line_work2(float2 cm, float2 c0, float2 cp, float2 vq, float2 vq_1,
                                            float auxv, float invd, float dt, float2& w1, float2& w2) {
-  const float2 vq_12 = mul2(splat(0.5f), add2(vq, vq_1));
-  w1 = mul2(splat(auxv), sub2(mul2(vq, c0), mul2(vq_1, cm)));
-  const float2 dr = mul2(sub2(cp, c0), splat(invd)), dl = mul2(sub2(c0, cm), splat(invd));
-  const float2 sigma = make_float2(minmod(dr.x, dl.x), minmod(dr.y, dl.y));
-  const float2 avq = abs2(vq_12);
-  const float2 Cri = mul2(splat(auxv), avq);
-  w2 = mul2(mul2(mul2(splat(dt * 0.5f), sub2(splat(1.0f), Cri)), sigma), avq);
+  line_work(cm.x, c0.x, cp.x, vq.x, vq_1.x, auxv, invd, dt, w1.x, w2.x);
+  line_work(cm.y, c0.y, cp.y, vq.y, vq_1.y, auxv, invd, dt, w1.y, w2.y);
 }
 
 __device__ __forceinline__ float2 line_update2(float2 c0, float2 vq, float2 w1, float2 w1p, float2 w2,
                                                float2 w2m, float2 w2p) {
-  const float2 dm = sub2(w2, w2m), dp = sub2(w2p, w2);
-  const float2 a = make_float2(vq.x > 0.0f ? w1.x : w1p.x, vq.y > 0.0f ? w1.y : w1p.y);
-  const float2 b = make_float2(vq.x > 0.0f ? dm.x : dp.x, vq.y > 0.0f ? dm.y : dp.y);
-  return sub2(sub2(c0, a), b);
+  return make_float2(line_update(c0.x, vq.x, w1.x, w1p.x, w2.x, w2m.x, w2p.x),
+                     line_update(c0.y, vq.y, w1.y, w1p.y, w2.y, w2m.y, w2p.y));
+}
+
+__device__ __forceinline__ float2 diff_face2(float2 Pa, float2 Pb, float2 qa, float2 qb) {
+  return make_float2(diff_face(Pa.x, Pb.x, qa.x, qb.x), diff_face(Pa.y, Pb.y, qa.y, qb.y));
 }
 
 __device__ __forceinline__ float2 diff_mid2(float2 cm, float2 c0, float2 cp, float2 lm, float2 l0, float2 lp,
-                                            float2 Pm, float2 P0, float2 Pp, float dtdx2) {
-  const float2 c0l0 = mul2(c0, l0);
-  const float2 gradr = mul2(mul2(splat(0.5f), add2(Pp, P0)), sub2(mul2(cp, lp), c0l0));
-  const float2 gradl = mul2(mul2(splat(0.5f), add2(P0, Pm)), sub2(c0l0, mul2(cm, lm)));
-  return add2(c0, mul2(splat(dtdx2), sub2(gradr, gradl)));
+                                            float2 Pm, float2 P0, float2 Pp, float dtdx2h) {
+  return make_float2(diff_mid(cm.x, c0.x, cp.x, lm.x, l0.x, lp.x, Pm.x, P0.x, Pp.x, dtdx2h),
+                     diff_mid(cm.y, c0.y, cp.y, lm.y, l0.y, lp.y, Pm.y, P0.y, Pp.y, dtdx2h));
+}
+
+// c0 + dtdx2h*(fr - fl) for a pair, the update of diff_mid from its faces
+__device__ __forceinline__ float2 diff_apply2(float dtdx2h, float2 fr, float2 fl, float2 c0) {
+  return make_float2(__fmaf_rn(dtdx2h, fr.x - fl.x, c0.x), __fmaf_rn(dtdx2h, fr.y - fl.y, c0.y));
+}
+
+__device__ __forceinline__ float2 diffz_mid2(float2 pc, float2 pb, float2 rc, float2 lc, float2 rb, float2 lb,
+                                             float2& fprev, const ZT32& zk) {
+  return make_float2(diffz_mid(pc.x, pb.x, rc.x, lc.x, rb.x, lb.x, fprev.x, zk),
+                     diffz_mid(pc.y, pb.y, rc.y, lc.y, rb.y, lb.y, fprev.y, zk));
+}
+__device__ __forceinline__ float2 diffz_bottom2(float2 pc, float2 pb, float2 rc, float2 lc, float2 rb, float2 lb,
+                                                float2 ra, float2& fprev, const ZT32& z0, const ZT32& z1) {
+  return make_float2(diffz_bottom(pc.x, pb.x, rc.x, lc.x, rb.x, lb.x, ra.x, fprev.x, z0, z1),
+                     diffz_bottom(pc.y, pb.y, rc.y, lc.y, rb.y, lb.y, ra.y, fprev.y, z0, z1));
+}
+__device__ __forceinline__ float2 diffz_top2(float2 pa, float2 la, float2 pb, float2 rc, float2 rb, float2 lb,
+                                             float2 ra, const ZT32& znm1, const ZT32& znz) {
+  return make_float2(diffz_top(pa.x, la.x, pb.x, rc.x, rb.x, lb.x, ra.x, znm1, znz),
+                     diffz_top(pa.y, la.y, pb.y, rc.y, rb.y, lb.y, ra.y, znm1, znz));
 }
 
 // Staged fields of iteration t (plane index in parentheses).
