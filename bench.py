@@ -495,6 +495,16 @@ def run_ours(args, rank, world, local_rank):
             fb["members_alone"] = alone
             fb["over_members_alone"] = fb["value"] / alone["value"]
             line["forms"]["fp32_batched"] = fb
+            # the batch machinery on grids of the single-context size: four
+            # scenarios of the benchmarked workload (seeds 1-4) batched and alone
+            from fall3d_gb300 import synth as _synth
+
+            big = [_synth.make_scenario(WORKLOAD, seed=i + 1, max_snapshots=2) for i in range(4)]
+            fu = serve.ensemble(steps=10, scen=big)
+            fa = serve.ensemble_alone(steps=10, scen=big)
+            line["forms"]["fp32_batched_4x" + WORKLOAD] = {
+                "value": fu["value"], "members_alone": fa["value"], "over_members_alone": fu["value"] / fa["value"],
+                "over_single_context": fu["value"] / (value / world), "tile_shape": fu["tile_shape"]}
         except Exception as e:
             line["forms"]["fp32_batched"] = {"error": str(e)}
         try:

@@ -26,10 +26,13 @@ import fall3d_gb300 as F
 from fall3d_gb300 import synth
 
 
-def ensemble(members=64, steps=40, run_h=12.0, seed=0, tune=True, warm=3):
-    """Batch of ``members`` ensemble members: ``warm`` batch steps (meteo
-    updates, autotune), then ``steps`` timed batch steps."""
-    scen = [synth.ensemble_member(seed + i, run_h=run_h, max_snapshots=2) for i in range(members)]
+def ensemble(members=64, steps=40, run_h=12.0, seed=0, tune=True, warm=3, scen=None):
+    """Batch of ``members`` ensemble members (or of the scenarios ``scen``):
+    ``warm`` batch steps (meteo updates, autotune), then ``steps`` timed
+    batch steps."""
+    if scen is None:
+        scen = [synth.ensemble_member(seed + i, run_h=run_h, max_snapshots=2) for i in range(members)]
+    members = len(scen)
     ctxs = [F.Context(s, F.PREC_FP32) for s in scen]
     b = F.Batch(members)
     for g in ctxs:
@@ -59,15 +62,18 @@ def ensemble(members=64, steps=40, run_h=12.0, seed=0, tune=True, warm=3):
     return out
 
 
-def ensemble_alone(members=64, steps=40, run_h=12.0, seed=0, warm=3):
-    """The members of ``ensemble`` each alone in its own context, one after
-    another (``warm`` steps, then ``steps`` timed steps each): the
-    single-context rate on the batch's work, cell-class-steps/s."""
+def ensemble_alone(members=64, steps=40, run_h=12.0, seed=0, warm=3, scen=None):
+    """The members of ``ensemble`` (or the scenarios ``scen``) each alone in
+    its own context, one after another (``warm`` steps, then ``steps`` timed
+    steps each): the single-context rate on the batch's work,
+    cell-class-steps/s."""
     import torch
 
+    if scen is None:
+        scen = [synth.ensemble_member(seed + i, run_h=run_h, max_snapshots=2) for i in range(members)]
+    members = len(scen)
     cc_total, t_total = 0, 0.0
-    for i in range(members):
-        s = synth.ensemble_member(seed + i, run_h=run_h, max_snapshots=2)
+    for s in scen:
         g = F.Context(s, F.PREC_FP32)
         g.source(0)
         g.meteo(0)
