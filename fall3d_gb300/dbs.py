@@ -20,10 +20,17 @@ and the transport model reads, restated without the netCDF library.
   in mm/s and vz(:,:,1) is not zeroed here, since the device's meteo update
   applies reamet.f90:146,153 itself.
 
+* ``debug_dbs`` is SetDbs's DEBUG meteorological model
+  (Utilities/SetDbs/read_DEBUG_data.f90, ``TYPE_DATA = debug``) with the
+  friction velocity and Monin-Obukhov length of ``get_par_abl``
+  (Utilities/SetDbs/get_par_ABL.f90): the fields a DBS made from it holds.
+
 The file layer is scipy's implementation of the netCDF classic formats
 (scipy.io.netcdf_file), which reads and writes the 64-bit-offset variant.
 """
 from __future__ import annotations
+
+import math
 
 import numpy as np
 
@@ -225,3 +232,63 @@ def read_dbs(path, zlayer, wetdep=True, time_lag=0.0):
         return out, warnings
     finally:
         ds.close()
+
+
+def _f90_max(a, b):
+    """gfortran's MAX(a, b): b where b > a or a is a NaN."""
+    return b if (b > a or math.isnan(a)) else a
+
+
+def get_par_abl(z0, z1, tz0, tz1, pz0, pz1, u, v):
+    """Utilities/SetDbs/get_par_ABL.f90: the friction velocity and the
+    Monin-Obukhov length from two levels z0 < z1 (temperatures in K,
+    pressures in Pa, the wind at z1) by the bulk Richardson number, in the
+    reference's operation order (its exponent 0.285 is a binary32 literal,
+    and the unstable branch's Gh uses the Gm updated just before it).
+    Returns (ustar, rmonin)."""
+    g, k = 9.81, 0.4
+    e = float(np.float32(0.285))
+    thz0 = tz0 * math.pow(1.01e5 / pz0, e)  # :34-35
+    thz1 = tz1 * math.pow(1.01e5 / pz1, e)
+    umod = _f90_max(math.sqrt(u * u + v * v), 1e-4)  # :39
+    ri = ((g * (z1 - z0)) * (thz1 - thz0)) / (((umod * umod) * 0.5) * (tz0 + tz1))  # :43
+    if ri >= 0.0:  # stable (:47-51)
+        gm = 1.0 + 4.7 * ri
+        gm = 1.0 / (gm * gm)
+        gh = gm
+    else:  # unstable (:53-59)
+        gm = math.log(z1 / z0)
+        gm = 1.0 + (((70.0 * k) * k) * math.sqrt((abs(ri) * z1) / z0)) / (gm * gm)
+        gh = 1.0 + (((50.0 * k) * k) * math.sqrt((abs(ri) * z1) / z0)) / (gm * gm)
+        gm = 1.0 - (9.4 * ri) / gm
+        gh = 1.0 - (9.4 * ri) / gh
+    ustar = math.log(z1 / z0)  # :63-64
+    ustar = ((k * umod) * math.sqrt(gm)) / ustar
+    thstar = math.log(z1 / z0)  # :68-70
+    thstar = ((((k * k) * umod) * (thz1 - thz0)) * gh) / ((ustar * thstar) * thstar)
+    thstar = _f90_max(thstar, 1e-4)
+    rmonin = (((ustar * ustar) * 0.5) * (thz0 + thz1)) / ((k * g) * thstar)  # :74
+    return ustar, rmonin
+
+
+def debug_dbs(nx, ny, zlayer, times):
+    """The met series of SetDbs's DEBUG model (read_DEBUG_data.f90 with its
+    default, non-standard atmosphere and no wind rotation) for a DBS on the
+    levels zlayer at the times (s): topography 0, u = 10 m/s, v = w = 0,
+    T = Tv = Tp = 273 K, p = 1e5 Pa, rho = 1, qv = 0, PBLH = 1000 m, LDU =
+    -999, ust and the Monin-Obukhov length L of each column from
+    get_par_abl(1, zlayer(2), T(1), T(2), p(1), p(2), u(1), v(1)) (:97-102);
+    RMOL, ZNT and PRATE keep SetDbs's initial 0 (Master.f90:178-179).
+    Returns a dict for write_dbs (binary64 values; the file stores them in
+    binary32)."""
+    nt, nz = len(times), len(zlayer)
+    shape3, shape2 = (nt, nz, ny, nx), (nt, ny, nx)
+    T = np.full(shape3, 273.0)
+    P = np.full(shape3, 1e5)
+    # every column holds the same values, so one evaluation serves them all
+    ust, lmo = get_par_abl(1.0, float(zlayer[1]), 273.0, 273.0, 1e5, 1e5, 10.0, 0.0)
+    return {"U": np.full(shape3, 10.0), "V": np.zeros(shape3), "W": np.zeros(shape3), "T": T, "TP": T.copy(),
+            "P": P, "QV": np.zeros(shape3), "RHO": np.ones(shape3), "PBLH": np.full(shape2, 1000.0),
+            "UST": np.full(shape2, ust), "L": np.full(shape2, lmo), "RMOL": np.zeros(shape2),
+            "ZNT": np.zeros(shape2), "PRATE": np.zeros(shape2), "LDU": np.full((ny, nx), -999.0),
+            "times": np.asarray(times, dtype=np.float64)}

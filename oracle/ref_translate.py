@@ -1460,6 +1460,7 @@ UTILITIES = {
                 {"setfrac", "m0_fi_gaussian", "fer", "getmem"}),
     "setsrc": ("SetSrc", ["KindType.f90", "Master.f90"], ["solvesuzuki.f90", "getsrc.f90"],
                {"solvesuzuki", "getsrc", "getshape"}),
+    "setdbs": ("SetDbs", ["KindType.f90"], ["get_par_ABL.f90"], {"get_par_abl"}),
 }
 
 

@@ -91,3 +91,37 @@ def test_read_dbs_interpolates_between_levels(tmp_path):
     assert not warn
     want = np.array([lin(0.0), lin(500.0), lin(1500.0), lin(3000.0), lin(4000.0)])
     assert np.allclose(out["u"][0, :, 0, 0], want, rtol=1e-6)
+
+
+def test_get_par_abl_matches_the_reference():
+    """fall3d_gb300.dbs.get_par_abl against the reference's own
+    Utilities/SetDbs/get_par_ABL.f90 (tests/golden/setdbs_abl.npz, made by
+    tests/golden/make_setdbs_golden.py from the translated routine), bit for
+    bit, over stable and unstable columns, calm air and equal temperatures."""
+    d = np.load(GOLD.replace("dbs_plane.npz", "setdbs_abl.npz"))
+    n = len(d["z0"])
+    assert n >= 400
+    ri_signs = set()
+    for i in range(n):
+        args = [float(d[k][i]) for k in ("z0", "z1", "tz0", "tz1", "pz0", "pz1", "u", "v")]
+        ust, rmo = dbs.get_par_abl(*args)
+        assert np.float64(ust).view(np.uint64) == d["ustar"][i].view(np.uint64), i
+        assert np.float64(rmo).view(np.uint64) == d["rmonin"][i].view(np.uint64), i
+        ri_signs.add(args[3] * (1.01e5 / args[5]) ** 0.285 > args[2] * (1.01e5 / args[4]) ** 0.285)
+    assert ri_signs == {True, False}  # both branches exercised
+
+
+def test_debug_dbs_is_read_back(tmp_path):
+    """A DBS of SetDbs's DEBUG model (read_DEBUG_data.f90) written and read on
+    the model levels: constant fields, the columns' ust from get_par_abl,
+    RMOL 0 (SetDbs leaves it at its initial value), PBLH 1000 m."""
+    zl = np.array([0.0, 250.0, 700.0, 1500.0, 3000.0])
+    met = dbs.debug_dbs(6, 5, zl, [0, 3600])
+    path = tmp_path / "debug.nc"
+    dbs.write_dbs(path, met, zl.astype(np.float32))
+    out, warn = dbs.read_dbs(path, zl, wetdep=True)
+    assert not warn
+    assert np.all(out["u"] == 10.0) and np.all(out["v"] == 0.0) and np.all(out["t"] == 273.0)
+    assert np.all(out["rho"] == 1.0) and np.all(out["pblh"] == 1000.0) and np.all(out["rmol"] == 0.0)
+    ust, _ = dbs.get_par_abl(1.0, 250.0, 273.0, 273.0, 1e5, 1e5, 10.0, 0.0)
+    assert np.all(out["ust"] == np.float64(np.float32(ust)))
