@@ -13,7 +13,7 @@ setbcc, advection, diffusion, wet and dry deposition, clip, cmass2d).
              context's stream over K steps; the state (0.4 GB of c alone) is
              larger than the 126 MB L2, so no flush is needed between steps.
 ``e2e``      the same metric through the C ABI's time loop (f3d_run) from
-             host buffers over four DBS intervals (2 h simulated):
+             host buffers over eight DBS intervals (4 h simulated):
              meteorology and sources uploaded by the loop when their
              intervals begin, each meteo update after the first computed
              while the previous interval steps (F3D_OPT_PREFETCH; the same
@@ -67,7 +67,7 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-E2E_INTERVALS = 4  # DBS intervals of the end-to-end window
+E2E_INTERVALS = 8  # DBS intervals of the end-to-end window (4 h of the 24-h forecast)
 
 
 def _scenario(max_snapshots=E2E_INTERVALS + 1):
