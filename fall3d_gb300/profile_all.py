@@ -7,6 +7,8 @@ per-kernel DRAM table is measured on:
   (per-routine binary64 sweeps, per-routine binary32 sweeps, the fused step
   of every tile shape), the budgets, every output variable and a flight
   level cut;
+* a run of the precision form across a DBS boundary through f3d_run (the
+  look-ahead meteo update: the settling chain beside the step kernel);
 * a batch of four ensemble members (setsrc/cmass2d of every member, the
   persistent step kernel, the batch-step counters);
 * a 64x56x20 grid with the gravity current and with aggregation in transport
@@ -59,6 +61,14 @@ def run(workload="cfg1"):
     s = synth.make_scenario(workload, seed=0, max_snapshots=2)
     _context_kernels(s, F.PREC_FP64)
     _context_kernels(s, F.PREC_FP32)
+    # f3d_run across a DBS boundary: the look-ahead update of the second
+    # snapshot (k_chain_beside, and the 112-register step kernel for steps
+    # launched while it runs)
+    s3 = synth.make_scenario(workload, seed=0, max_snapshots=3)
+    t_dbs = float(s3.met["times"][1])
+    g = F.Context(s3, F.PREC_FP32)
+    g.run(beg_time=t_dbs - 30.0, end_time=t_dbs + 30.0)
+    g.close()
     # batched form
     b = F.Batch(8)
     ctxs = [F.Context(synth.ensemble_member(100 + i, run_h=1.0, max_snapshots=2), F.PREC_FP32) for i in range(4)]
