@@ -132,6 +132,7 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
   const int sft = gx0 - xs;       // the region's offset in a box row (0 or 2)
   const int pl = nx * ny;
   const bool edge = !(gx0 >= 1 && gx0 + HX - 1 <= nx && gy0 >= 1 && gy0 + HY - 1 <= ny);
+  const bool xedge = gx0 <= 1 || gx0 + HX - 1 >= nx;  // the region holds column 1 or nx
 
   const unsigned mbar0 = (unsigned)__cvta_generic_to_shared(mbar);
   if (threadIdx.x == 0) {
@@ -546,29 +547,28 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
         const float2 l0 = lbv[r], P0 = lds2(at(F_PX, r)), c0 = in[r];
-        if constexpr (!EDGE) {
-          // the face flux 0.5*(P(q)+P(q+1))*(c(q+1)/rho(q+1) - c(q)/rho(q)) is gradr at q and
-          // gradl at q+1 (diffx.f90:34-40): computed once per face, the left one by shuffle
-          const float2 q0 = mul2(c0, l0);
-          const float2 fr = diff_face2(right2(P0), P0, right2(q0), q0);
-          out[r] = diff_apply2(dtdx2h, fr, left2(fr), c0);
-          continue;
-        }
-        const float2 cm = left2(c0), cp = right2(c0), lm = left2(l0), lp = right2(l0), Pm = left2(P0),
-                     Pp = right2(P0);
-        float2 u = diff_mid2(cm, c0, cp, lm, l0, lp, Pm, P0, Pp, dtdx2h);
+        // the face flux (P(q)+P(q+1))*(c(q+1)/rho(q+1) - c(q)/rho(q)) is gradr at q and
+        // gradl at q+1 (diffx.f90:34-40): computed once per face, the left one by shuffle
+        const float2 q0 = mul2(c0, l0), qp = right2(q0), Pp = right2(P0);
+        const float2 fr = diff_face2(Pp, P0, qp, q0);
+        float2 u = diff_apply2(dtdx2h, fr, left2(fr), c0);
         if constexpr (EDGE) {
+          if (xedge) {  // the line's first and last cells (diffx.f90:22-33, 44-55)
+            const float2 cm = left2(c0), cp = right2(c0), qm = left2(q0), Pm = left2(P0);
 #pragma unroll
-          for (int c = 0; c < 2; ++c) {
-            const int g = gi + c;
-            if (g == 1 || g == nx)
-              cmp(u, c) = diff_cell(g == 1, g == nx, cmp(cm, c), cmp(c0, c), cmp(cp, c), cmp(lm, c), cmp(l0, c),
-                                    cmp(lp, c), cmp(Pm, c), cmp(P0, c), cmp(Pp, c), dtdx2h);
+            for (int c = 0; c < 2; ++c) {
+              const int g = gi + c;
+              if (g == 1)
+                cmp(u, c) = diff_first_q(cmp(qp, c), cmp(q0, c), cmp(cm, c), cmp(l0, c), cmp(P0, c), cmp(Pp, c),
+                                         cmp(c0, c), dtdx2h);
+              else if (g == nx)
+                cmp(u, c) = diff_last_q(cmp(q0, c), cmp(qm, c), cmp(cp, c), cmp(l0, c), cmp(P0, c), cmp(Pm, c),
+                                        cmp(c0, c), dtdx2h);
+            }
           }
-          out[r] = sel2(km(r, 0), km(r, 1), u, c0);
-        } else {
-          out[r] = u;
+          u = sel2(km(r, 0), km(r, 1), u, c0);  // ghosts and outside positions keep their value
         }
+        out[r] = u;
       }
     };
     auto dif_y = [&](const float2* in, float2* out) {
@@ -576,16 +576,20 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
       const float2 P0v[RPW] = {lds2(at(F_PY, 0)), lds2(at(F_PY, 1))};
       const float2 Pmv[RPW] = {lds2(at(F_PY, 0) - RS), P0v[0]};
       const float2 Ppv[RPW] = {P0v[1], lds2(at(F_PY, 1) + RS)};
-      if constexpr (!EDGE) {
-        // neighbours read c/rho: the products c*(1/rho) of diffy.f90:34-40,
-        // each computed once by its owner
-        float2 q[RPW];
+      // neighbours read c/rho: the products c*(1/rho) of diffy.f90:34-40,
+      // each computed once by its owner; a ghost row (edge tiles) holds c
+      // itself, which is what the line's first and last cells read of it
+      const int gj0 = gy0 + 2 * warp;  // the pair's first row
+      float2 q[RPW];
+      bool ghost[RPW];
 #pragma unroll
-        for (int r = 0; r < RPW; ++r) {
-          q[r] = mul2(in[r], lbv[r]);
-          sts2(P1 + r * HX, q[r]);
-        }
-        __syncthreads();
+      for (int r = 0; r < RPW; ++r) {
+        q[r] = mul2(in[r], lbv[r]);
+        ghost[r] = EDGE && (gj0 + r == 0 || gj0 + r == ny + 1);  // uniform across the warp
+        sts2(P1 + r * HX, ghost[r] ? in[r] : q[r]);
+      }
+      __syncthreads();
+      if constexpr (!EDGE) {
         const float2 qm[RPW] = {lds2(P1 - HX), q[0]};
         const float2 qp[RPW] = {q[1], lds2(P1 + 2 * HX)};
         // three faces: below the pair, between its rows (gradr of row 0 and
@@ -595,33 +599,29 @@ __device__ __forceinline__ void fused2_tile(const FusedArgs& a, const F2Maps* ma
         const float2 ft = diff_face2(Ppv[1], P0v[1], qp[1], q[1]);
         out[0] = diff_apply2(dtdy2h, fm, fb, in[0]);
         out[1] = diff_apply2(dtdy2h, ft, fm, in[1]);
-        return;
-      }
+      } else {
+        // the stored values of the rows below and above each row
+        const float2 vmv[RPW] = {lds2(P1 - HX), ghost[0] ? in[0] : q[0]};
+        const float2 vpv[RPW] = {ghost[1] ? in[1] : q[1], lds2(P1 + 2 * HX)};
 #pragma unroll
-      for (int r = 0; r < RPW; ++r) sts2(P1 + r * HX, in[r]);
-      __syncthreads();
-      const float2 cmv[RPW] = {lds2(P1 - HX), in[0]};
-      const float2 cpv[RPW] = {in[1], lds2(P1 + 2 * HX)};
-      const float2 lmv[RPW] = {lds2(at(F_L1, 0) - RS), lbv[0]};
-      const float2 lpv[RPW] = {lbv[1], lds2(at(F_L1, 1) + RS)};
-#pragma unroll
-      for (int r = 0; r < RPW; ++r) {
-        const float2 cm = cmv[r], cp = cpv[r];
-        const float2 lm = lmv[r], lp = lpv[r], Pm = Pmv[r], P0 = P0v[r], Pp = Ppv[r];
-        if constexpr (EDGE) {
-          const int gj = gy0 + 2 * warp + r;
+        for (int r = 0; r < RPW; ++r) {
+          const int gj = gj0 + r;
           float2 u;
-          if (gj == 1 || gj == ny) {  // uniform across the warp
+          if (gj == 1) {  // the first row (diffy.f90:22-33): the row below is the ghost, stored as c
 #pragma unroll
             for (int c = 0; c < 2; ++c)
-              cmp(u, c) = diff_cell(gj == 1, gj == ny, cmp(cm, c), cmp(in[r], c), cmp(cp, c), cmp(lm, c),
-                                    cmp(lbv[r], c), cmp(lp, c), cmp(Pm, c), cmp(P0, c), cmp(Pp, c), dtdy2h);
-          } else {
-            u = diff_mid2(cm, in[r], cp, lm, lbv[r], lp, Pm, P0, Pp, dtdy2h);
+              cmp(u, c) = diff_first_q(cmp(vpv[r], c), cmp(q[r], c), cmp(vmv[r], c), cmp(lbv[r], c),
+                                       cmp(P0v[r], c), cmp(Ppv[r], c), cmp(in[r], c), dtdy2h);
+          } else if (gj == ny) {  // the last row (diffy.f90:44-55): the row above is the ghost
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+              cmp(u, c) = diff_last_q(cmp(q[r], c), cmp(vmv[r], c), cmp(vpv[r], c), cmp(lbv[r], c),
+                                      cmp(P0v[r], c), cmp(Pmv[r], c), cmp(in[r], c), dtdy2h);
+          } else {  // an inner row: its two faces
+            u = diff_apply2(dtdy2h, diff_face2(Ppv[r], P0v[r], vpv[r], q[r]), diff_face2(P0v[r], Pmv[r], q[r], vmv[r]),
+                            in[r]);
           }
           out[r] = sel2(km(r, 0), km(r, 1), u, in[r]);
-        } else {
-          out[r] = diff_mid2(cm, in[r], cp, lm, lbv[r], lp, Pm, P0, Pp, dtdy2h);
         }
       }
     };

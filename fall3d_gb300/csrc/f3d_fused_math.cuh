@@ -116,6 +116,25 @@ __device__ __forceinline__ float diff_cell(bool first, bool last, float cm, floa
   return __fmaf_rn(2.0f * dtdx2h, gradr - gradl, c0);
 }
 
+// diff_cell from the products q = c*l of the cell's neighbours inside the
+// line and the ghost's c: the first cell (qp = c(2)*l(2), q0 = c(1)*l(1),
+// cm = c(0)) and the last (q0, qm = c(n-1)*l(n-1), cp = c(n+1)); the same
+// operations on the same values as diff_cell.
+__device__ __forceinline__ float diff_first_q(float qp, float q0, float cm, float l0, float P0, float Pp, float c0,
+                                              float dtdx2h) {
+  const float gradr = Pp * (qp - q0);
+  const float g = P0 * (q0 - cm * l0);
+  const float gradl = g > 0.0f ? g : 0.0f;
+  return __fmaf_rn(2.0f * dtdx2h, gradr - gradl, c0);
+}
+__device__ __forceinline__ float diff_last_q(float q0, float qm, float cp, float l0, float P0, float Pm, float c0,
+                                             float dtdx2h) {
+  const float g = P0 * (cp * l0 - q0);
+  const float gradr = g < 0.0f ? g : 0.0f;
+  const float gradl = Pm * (q0 - qm);
+  return __fmaf_rn(2.0f * dtdx2h, gradr - gradl, c0);
+}
+
 // diffz.f90:22-62 at plane k with c(k-1) = ra, c(k) = rb, c(k+1) = rc,
 // l = 1/rho at k (lb), k+1 (lc) and k-1 (la), P = rkver*rho at k (pb),
 // k+1 (pc) and k-1 (pa).  An interior plane: the face flux above k (kept in
