@@ -62,3 +62,19 @@ def test_class_groups_step_the_serial_run():
         part = run(ic_loc, nc_loc)
         sl = slice(ic_loc - 1, ic_loc - 1 + nc_loc)
         assert np.array_equal(part[sl].view(np.uint64), serial[sl].view(np.uint64)), (ic_loc, nc_loc)
+
+
+@pytest.mark.skipif(not _have_reference(), reason="translated reference unavailable")
+def test_class_parallel_timing_runs_every_group():
+    """The forked class groups of bench.py's reference arm: every group runs
+    the same number of timed steps and reports back; the work is the
+    serial run's (all classes, every step)."""
+    s = synth.make_scenario("tiny", seed=3, max_snapshots=2)
+    nc = s.grid["nc"]
+    r = ref_driver.time_class_parallel(s, 3, steps=4, serial_steps=1, budget_s=5.0)
+    par, ser = r["parallel"], r["serial"]
+    assert par["groups"] == 3 and 2 <= par["steps"] <= 4
+    cells = s.grid["nx"] * s.grid["ny"] * s.grid["nz"]
+    assert par["cell_class_steps"] == cells * nc * par["steps"]
+    assert ser["cell_class_steps"] == cells * nc
+    assert par["seconds"] > 0.0 and par["slowest_group_s"] <= par["seconds"] and r["meteo_s"] > 0.0
