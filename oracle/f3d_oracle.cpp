@@ -1,9 +1,9 @@
 /*
  * f3d_oracle.cpp -- CPU oracle of the FALL3D 7.0 transport step.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA library
- * in fall3d_gb300/: only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline may load it, and the library never does.
+ * TEST INFRASTRUCTURE ONLY.  This file checks the results of the CUDA
+ * library in fall3d_gb300/: only tests/, __graft_entry__.smoke() and
+ * bench.py's CPU baseline may load it, and the library never does.
  *
  * It restates, routine by routine and in the reference's own operation
  * order, the binary64 Fortran of lmingari/Fall3D (FALL3D 7.0, 2013):

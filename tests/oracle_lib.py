@@ -1,6 +1,6 @@
 """ctypes binding of the CPU oracle (oracle/f3d_oracle.cpp) for the tests,
-smoke() and bench.py's CPU baseline.  The oracle is the checker, never the
-product path."""
+smoke() and bench.py's CPU baseline.  The oracle checks the library's
+results; the library never calls it."""
 from __future__ import annotations
 
 import ctypes as C
