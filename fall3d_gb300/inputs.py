@@ -21,6 +21,10 @@ host.
   ``solvesuzuki`` (Utilities/SetSrc/solvesuzuki.f90) and ``getsrc``
   (Utilities/SetSrc/getsrc.f90: bilinear spreading over the four nodes
   around each column point, linear between the two model levels).
+* ``setpsi`` / ``get_gama`` (Sources/setpsi.f90, called at
+  Sources/readat.f90:248): the shape factor of each class for the settling
+  model of the .inp, gama by the reference's bisection on the prolate
+  ellipsoid's area.
 * ``scenario_from_files``: a Scenario for fall3d_gb300.Context from an .inp,
   a .grn and a .src file (grid from the .inp GRID block as reagrd.f90 derives
   it from the DBS properties), with the meteorology of a DBS file
@@ -469,7 +473,7 @@ def scenario_from_files(inp_path: str, grn_path: str, src_path: str, seed: int =
     g["diam"] = grn["diam_mm"] / 1e3
     g["rhop"] = grn["rhop"]
     g["sphe"] = np.minimum(grn["sphe"], 1.0)
-    g["psi"] = synth.setpsi(g["modv"], g["sphe"], g["diam"])
+    g["psi"] = setpsi(g["modv"], g["sphe"], g["diam"])  # Sources/readat.f90:248
     g["np"] = nc
     s.src = {k: srcd[k] for k in ("t1", "t2", "nsou", "isrc", "jsrc", "ksrc", "tmrat")}
     s.info["zs"] = list(srcd["zs"])
@@ -483,3 +487,50 @@ def scenario_from_files(inp_path: str, grn_path: str, src_path: str, seed: int =
         s.met = met
         s.info["dbs_warnings"] = warnings
     return s
+
+
+def get_gama(diam, sphe):
+    """Sources/setpsi.f90 get_gama: the axis ratio a/c of the prolate
+    ellipsoid with the particle's volume and the area its sphericity gives,
+    by bisection on [1e-3, 1] (at most 1000 halvings, until the area is
+    within 1e-8), in the reference's operation order (diameter in m, scaled
+    by 1e3; (0.5 d)**3 as (0.5 d)*((0.5 d)*(0.5 d)))."""
+    d = diam * 1e3
+    gmin, gmax = 1e-3, 1.0
+    pi = 4.0 * math.atan(1.0)
+    t = 0.5 * d
+    vp = ((4.0 * pi) * (t * (t * t))) / 3.0
+    ap = (math.pow(pi, 1.0 / 3.0) * math.pow(6.0 * vp, 2.0 / 3.0)) / sphe
+    for it in range(1, 1001):
+        gama = 0.5 * (gmin + gmax)
+        e = math.acos(gama)
+        ao = ((((0.5 * pi) * d) * d) * math.pow(gama, -(4.0 / 3.0))) * ((gama * gama) + (e / math.tan(e)))
+        if ao < ap:
+            gmax = gama
+        else:
+            gmin = gama
+        if it > 1 and abs(ao - ap) < 1e-8:
+            return gama
+    raise RuntimeError("Subroutine get_gama: convergence not achieved")
+
+
+def setpsi(modv, sphe, diam):
+    """Sources/setpsi.f90 setpsi: the shape factor of each class for the
+    settling model modv: 1 (Arastoopour) 1, 2 (Ganser) the sphericity,
+    3 (Wilson) 0.5*(1 + 1/gama) for an oblate (gama >= 1) and gama for a
+    prolate particle, 4 (Dellino) the sphericity over the circularity (1, or
+    sqrt(gama) for a prolate particle), gama from get_gama."""
+    sphe = np.asarray(sphe, dtype=np.float64)
+    diam = np.asarray(diam, dtype=np.float64)
+    if modv == 1:
+        return np.ones_like(sphe)
+    if modv == 2:
+        return sphe.copy()
+    out = np.zeros_like(sphe)
+    for ic in range(len(sphe)):
+        gama = get_gama(float(diam[ic]), float(sphe[ic]))
+        if modv == 3:
+            out[ic] = 0.5 * (1.0 + 1.0 / gama) if gama >= 1.0 else gama
+        elif modv == 4:
+            out[ic] = sphe[ic] / 1.0 if gama >= 1.0 else sphe[ic] / math.sqrt(gama)
+    return out

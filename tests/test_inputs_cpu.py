@@ -154,3 +154,16 @@ def test_scenario_from_files_runs_in_the_oracle(tmp_path):
     o = O.OracleCtx(s, nthreads=4)
     log = o.run(max_steps=4)
     assert o.state()["iiter"] == 4 and log["massvol"][-1] > 0.0
+
+
+def test_setpsi_matches_the_reference():
+    """inputs.setpsi (with get_gama's bisection) against the reference's own
+    Sources/setpsi.f90 (tests/golden/setpsi.npz, made by
+    tests/golden/make_setpsi_golden.py), bit for bit, for the four settling
+    models."""
+    import os
+
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "setpsi.npz"))
+    for modv in (1, 2, 3, 4):
+        psi = I.setpsi(modv, d["sphe"], d["diam"])
+        assert np.array_equal(psi.view(np.uint64), d[f"psi{modv}"].view(np.uint64)), modv
