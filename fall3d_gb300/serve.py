@@ -3,6 +3,8 @@
 ensemble   a batch of ensemble members (nx, ny ~ U[64,320], nz ~ U[20,60],
            4-20 classes, ...) advanced together through f3d_batch_* for a
            bounded number of batch steps: cell-class-steps/s of the batch.
+ensemble_run  the same members each run to its end in one batch (the whole
+           job), then each alone through f3d_run, compared bit for bit.
 serving    forecast requests (each an ensemble member with a duration
            U[dmin, dmax] h) arriving as a Poisson stream, submitted to the
            continuous-batching server (f3d_server_*) at their arrival times
@@ -12,6 +14,7 @@ serving    forecast requests (each an ensemble member with a duration
            timed; a FIFO of the measured service times on the same arrivals).
 
     python -m fall3d_gb300.serve ensemble [--members 64] [--steps 40]
+    python -m fall3d_gb300.serve ensemble-run [--members 64] [--run-h 12] [--met-dt-h-run 3]
     python -m fall3d_gb300.serve serving [--rate 2] [--window 600] [--cap-gb 150]
 """
 from __future__ import annotations
@@ -93,6 +96,60 @@ def ensemble_alone(members=64, steps=40, run_h=12.0, seed=0, warm=3, scen=None):
     return dict(members=members, steps=steps, seconds=t_total, value=cc_total / t_total)
 
 
+def ensemble_run(members=64, run_h=12.0, met_dt_h=3.0, seed=0, alone=True):
+    """The whole batched job: ``members`` ensemble members each run to its
+    end (every source interval and meteo update; met snapshots every
+    ``met_dt_h`` hours over the whole run) in one batch, timed from the
+    first batch step to the last, autotune included; then, with ``alone``,
+    each member run to its end in its own context through f3d_run, timed,
+    and compared with its batched result (step count, c, cdry and cwet bit
+    for bit)."""
+    scen = [synth.ensemble_member(seed + i, run_h=run_h, met_dt_h=met_dt_h) for i in range(members)]
+    ctxs = [F.Context(s, F.PREC_FP32) for s in scen]
+    b = F.Batch(members)
+    slots = [b.add(g) for g in ctxs]
+    b.sync()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        b.step()
+    tuned = b.autotune(reps=2)
+    b.run()
+    b.sync()
+    t = time.perf_counter() - t0
+    bs, cc, _ = b.stats()
+    done = 0
+    for sl in slots:
+        try:
+            done += int(b.poll(sl)[0] == F.Batch.DONE)
+        except F.F3DError:  # the member's own error (its source or meteo update failed)
+            pass
+    cells = [s.grid["nx"] * s.grid["ny"] * s.grid["nz"] * s.grid["nc"] for s in scen]
+    out = dict(members=members, run_h=run_h, met_interval_h=met_dt_h, done=done, batch_steps=bs, seconds=t, value=cc / t,
+               cell_class_steps=cc, cell_classes=int(sum(cells)), tile_shape=tuned[0])
+    if alone:
+        t_alone, same, steps = 0.0, 0, []
+        for i, s in enumerate(scen):
+            g = F.Context(s, F.PREC_FP32)
+            g.sync()
+            t1 = time.perf_counter()
+            g.run()
+            g.sync()
+            t_alone += time.perf_counter() - t1
+            sa, sb = g.state(), ctxs[i].state()
+            fa, fb = g.fields(), ctxs[i].fields()
+            steps.append(sa["iiter"])
+            same += int(sa["iiter"] == sb["iiter"] and sa["time"] == sb["time"] and
+                        all(np.array_equal(fa[k], fb[k], equal_nan=True) for k in ("c", "cdry", "cwet")))
+            g.close()
+        out["alone"] = dict(seconds=t_alone, value=cc / t_alone, members_bitwise_equal=same,
+                            steps_min=int(min(steps)), steps_max=int(max(steps)))
+        out["batched_over_alone"] = t_alone / t
+    b.close()
+    for g in ctxs:
+        g.close()
+    return out
+
+
 def fp64_sequential(scens, arrivals):
     """The same requests one after another in the plain FP64 form: each is
     run to its end (context creation, f3d_run with its meteorology and
@@ -172,7 +229,7 @@ def serving(rate=2.0, window=600.0, cap_gb=150.0, dmin=3.0, dmax=48.0, met_dt_h=
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["ensemble", "serving"])
+    ap.add_argument("mode", choices=["ensemble", "ensemble-run", "serving"])
     ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--rate", type=float, default=2.0)
@@ -182,9 +239,13 @@ def main():
     ap.add_argument("--dmax", type=float, default=48.0)
     ap.add_argument("--met-dt-h", type=float, default=12.0)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--run-h", type=float, default=12.0)
+    ap.add_argument("--met-dt-h-run", type=float, default=3.0, help="met interval of ensemble-run")
     args = ap.parse_args()
     if args.mode == "ensemble":
         print(json.dumps(ensemble(args.members, args.steps, seed=args.seed)))
+    elif args.mode == "ensemble-run":
+        print(json.dumps(ensemble_run(args.members, args.run_h, args.met_dt_h_run, seed=args.seed)))
     else:
         print(json.dumps(serving(args.rate, args.window, args.cap_gb, args.dmin, args.dmax, args.met_dt_h,
                                  args.seed)))
