@@ -150,15 +150,13 @@ def make_classes(nc, phimin, phimax, rho_coarse=2500.0, rho_fine=1000.0,
 
 
 def setpsi(modv, sphe, diam):
-    """Shape factor psi of Sources/setpsi.f90:27-58: 1 (ARASTOOPOUR) or the
-    sphericity (GANSER).  For WILSON and DELLINO the reference derives psi from
-    get_gama's axis ratio; the synthetic scenarios use a fixed psi = 0.75
-    there (psi is an input of the transport path either way)."""
-    if modv == MODV_ARASTOOPOUR:
-        return np.ones_like(sphe)
-    if modv == MODV_GANSER:
-        return sphe.copy()
-    return np.full_like(sphe, 0.75)
+    """Shape factor psi of Sources/setpsi.f90:27-58, as the reference derives
+    it from the classes (Sources/readat.f90:248): 1 (ARASTOOPOUR), the
+    sphericity (GANSER), and from get_gama's axis ratio for WILSON and
+    DELLINO (fall3d_gb300.inputs.setpsi)."""
+    from fall3d_gb300 import inputs
+
+    return inputs.setpsi(modv, np.asarray(sphe, dtype=np.float64), np.asarray(diam, dtype=np.float64))
 
 
 def suzuki_column(ns, H, A, lam, M0, fc):
