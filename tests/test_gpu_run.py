@@ -17,7 +17,7 @@ import pytest
 import fall3d_gb300 as F
 from fall3d_gb300 import synth
 import oracle_lib as O
-from helpers import assert_close, assert_same_bits, compare_runs
+from helpers import assert_same_bits, compare_runs
 
 pytestmark = pytest.mark.gpu
 
