@@ -92,6 +92,7 @@ def load(build_if_missing: bool = False):
         "f3d_source": [VP, I, VP, VP, VP, VP],
         "f3d_step": [VP],
         "f3d_budget": [VP, DP, DP, DP, DP],
+        "f3d_count_nonfinite": [VP, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
         "f3d_get_state": [VP, IP, DP, DP, DP, DP, DP, DP],
         "f3d_set_time": [VP, D, I],
         "f3d_download": [VP, VP, VP, VP, VP, VP],
@@ -459,6 +460,12 @@ class Context:
         v = [C.c_double() for _ in range(4)]
         _check(self.lib.f3d_budget(self.h, *[C.byref(x) for x in v]))
         return dict(zip(("massvol", "massdep", "massdry", "masswet"), (x.value for x in v)))
+
+    def count_nonfinite(self):
+        """(NaN or infinite values in c, in cdry + cwet) on the device."""
+        a, b = C.c_longlong(), C.c_longlong()
+        _check(self.lib.f3d_count_nonfinite(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def outputs(self):
         a = [np.zeros((self.ny, self.nx)) for _ in range(3)]

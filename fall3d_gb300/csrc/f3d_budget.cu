@@ -446,6 +446,39 @@ void launch_cmass2d_batch(const BatchAux* tab, const int* bstep, int nscen, void
   count_launch(2);
 }
 
+// ------------------------------------------------ non-finite values
+// Adds to *count the number of NaN or infinite values among a[0..n): the
+// exponent field all ones, tested on the bit pattern.  A grid-stride loop of
+// 8 blocks per SM, one atomic add per warp that found any.
+__device__ __forceinline__ bool nonfinite_bits(float v) {
+  return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u;
+}
+__device__ __forceinline__ bool nonfinite_bits(double v) {
+  return ((unsigned long long)__double_as_longlong(v) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+}
+template <class T>
+__global__ void k_count_nonfinite(const T* __restrict__ a, long long n, unsigned long long* count) {
+  unsigned long long k = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    k += nonfinite_bits(a[i]) ? 1ull : 0ull;
+  for (int o = 16; o > 0; o >>= 1) k += __shfl_down_sync(0xffffffffu, k, o);
+  if ((threadIdx.x & 31) == 0 && k) atomicAdd(count, k);
+}
+
+template <class T>
+void launch_count_nonfinite(const T* a, long long n, unsigned long long* count, cudaStream_t s) {
+  if (n <= 0) return;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (n + 255) / 256;
+  const int blocks = (int)std::min<long long>(want, 8LL * std::max(sms, 1));
+  k_count_nonfinite<T><<<blocks, 256, 0, s>>>(a, n, count);
+  count_launch();
+}
+template void launch_count_nonfinite<float>(const float*, long long, unsigned long long*, cudaStream_t);
+template void launch_count_nonfinite<double>(const double*, long long, unsigned long long*, cudaStream_t);
+
 template void launch_cmass2d<double>(const double*, const double*, const double*, const double*,
                                      const double*, Dims, int, int, int, int, double, double,
                                      const double*, double, void*, double*, cudaStream_t);

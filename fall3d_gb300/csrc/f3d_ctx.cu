@@ -49,6 +49,8 @@ int* small_step_status(f3d_ctx* x) { return reinterpret_cast<int*>(x->small + 26
 double* small_pref_cd(f3d_ctx* x) { return x->small + 32; }
 unsigned long long* small_pref_dtcn(f3d_ctx* x) { return reinterpret_cast<unsigned long long*>(x->small + 33); }
 int* small_pref_status(f3d_ctx* x) { return reinterpret_cast<int*>(x->small + 34); }
+// the non-finite counts of f3d_count_nonfinite: in c, in cdry + cwet
+unsigned long long* small_nonfinite(f3d_ctx* x) { return reinterpret_cast<unsigned long long*>(x->small + 40); }
 
 template <class T>
 int dalloc(f3d_ctx* x, T** p, size_t n) {
@@ -960,6 +962,26 @@ int f3d_budget(f3d_ctx* x, double* massvol, double* massdep, double* massdry, do
   if (massdep) *massdep = h[1];
   if (massdry) *massdry = h[2];
   if (masswet) *masswet = h[3];
+  return F3D_OK;
+}
+
+int f3d_count_nonfinite(f3d_ctx* x, long long* in_c, long long* in_deposits) {
+  if (!x) return f3d::ctx_error(F3D_ERR_ARG, "NULL context");
+  const Dims d = x->d;
+  const long long hb = (long long)d.halo() * x->g.nc, dep = (long long)d.plane() * (x->g.nc + 1);
+  unsigned long long* cnt = small_nonfinite(x);
+  CK(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), x->stream));
+  if (x->prec == F3D_PREC_FP32)
+    launch_count_nonfinite<float>(x->c32, hb, cnt, x->stream);
+  else
+    launch_count_nonfinite<double>(x->c64, hb, cnt, x->stream);
+  launch_count_nonfinite<double>(x->cdry, dep, cnt + 1, x->stream);
+  launch_count_nonfinite<double>(x->cwet, dep, cnt + 1, x->stream);
+  unsigned long long h[2];
+  CK(cudaMemcpyAsync(h, cnt, sizeof h, cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  if (in_c) *in_c = (long long)h[0];
+  if (in_deposits) *in_deposits = (long long)h[1];
   return F3D_OK;
 }
 

@@ -99,7 +99,7 @@ struct f3d_ctx {
   // scratch
   void* red_scratch = nullptr;
   void* vset_scratch = nullptr;
-  double* small = nullptr;  // [0] outmass, [1..4] budget, [8] cd, [16] dtcn bits, [24] status
+  double* small = nullptr;  // [0] outmass, [1..4] budget, [8] cd, [16] dtcn bits, [24] status, [40..41] non-finite counts
   // host scalars of the time loop
   double time = 0.0, dt = 1.0, dtc = 0.0, erumass = 0.0, flowrate = 0.0;
   int iiter = 0, have_met = 0;

@@ -139,6 +139,9 @@ void launch_cmass3d(const T* c, const double* cload, const double* cdry, const d
                     double* out, cudaStream_t s);
 void launch_getc0(double* cdry, double* cwet, double* cload, Dims d, int nc, int np,
                   cudaStream_t s);
+// *count += the number of NaN or infinite values among a[0..n).
+template <class T>
+void launch_count_nonfinite(const T* a, long long n, unsigned long long* count, cudaStream_t s);
 // Largest dtcni of finddt.f90:26-57 as a binary64 bit pattern in *dtcn_bits
 // (which must hold +0.0 on entry).
 void launch_finddt(Dims d, int nc, double dX1, double dX2, const double* dz, const double* vx,

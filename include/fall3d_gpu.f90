@@ -531,6 +531,13 @@ module fall3d_gpu
       real(c_double), intent(inout) :: massdry
       real(c_double), intent(inout) :: masswet
     end function f3d_budget
+    function f3d_count_nonfinite(ctx, in_c, in_deposits) bind(C, name="f3d_count_nonfinite")
+      import
+      integer(c_int) :: f3d_count_nonfinite
+      type(c_ptr), value :: ctx
+      integer(c_long_long), intent(inout) :: in_c
+      integer(c_long_long), intent(inout) :: in_deposits
+    end function f3d_count_nonfinite
     function f3d_get_state(ctx, iiter, time, dt, dtc, erumass, outmass, flowrate) bind(C, name="f3d_get_state")
       import
       integer(c_int) :: f3d_get_state
