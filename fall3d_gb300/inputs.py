@@ -202,8 +202,13 @@ def read_grn(path: str) -> dict:
     then diameter (mm), density, sphericity and fraction per class)."""
     with open(path) as f:
         toks = f.read().split()
-    nc = int(toks[0])
-    rows = np.array([[_fortran_real(t) for t in toks[1 + 4 * i:5 + 4 * i]] for i in range(nc)])
+    try:  # a short or garbled file is the reader's error 101
+        nc = int(toks[0])
+        if nc < 0 or len(toks) < 1 + 4 * nc:
+            raise IndexError
+        rows = np.array([[_fortran_real(t) for t in toks[1 + 4 * i:5 + 4 * i]] for i in range(nc)]).reshape(nc, 4)
+    except (IndexError, ValueError):
+        raise ValueError(f"get_granulometry_value: error reading the granulometry file {path}") from None
     return dict(nc=nc, diam_mm=rows[:, 0], rhop=rows[:, 1], sphe=rows[:, 2], fc=rows[:, 3])
 
 
@@ -258,19 +263,26 @@ def read_src(path: str) -> dict:
     pos = 0
     t1, t2, nsou, isrc, jsrc, ksrc, zs, tm = [], [], [], [], [], [], [], []
     nc_all = None
+    tcur = 0
     while pos < len(toks):
-        a, b = int(toks[pos]), int(toks[pos + 1])
-        ns, nc = int(toks[pos + 2]), int(toks[pos + 3])
-        pos += 5  # MFR
-        nc_all = nc if nc_all is None else nc_all
-        rates = np.zeros((ns, nc))
-        for q in range(ns):
-            zs.append(_fortran_real(toks[pos + 2]))
-            isrc.append(int(toks[pos + 3]))
-            jsrc.append(int(toks[pos + 4]))
-            ksrc.append(int(toks[pos + 5]))
-            rates[q] = [_fortran_real(t) for t in toks[pos + 6:pos + 6 + nc]]
-            pos += 6 + nc
+        try:  # an incomplete or garbled interval record is the reader's error 101
+            a, b = int(toks[pos]), int(toks[pos + 1])
+            tcur = a
+            ns, nc = int(toks[pos + 2]), int(toks[pos + 3])
+            if ns < 0 or nc < 0 or pos + 5 + ns * (6 + nc) > len(toks):
+                raise IndexError
+            pos += 5  # MFR
+            nc_all = nc if nc_all is None else nc_all
+            rates = np.zeros((ns, nc))
+            for q in range(ns):
+                zs.append(_fortran_real(toks[pos + 2]))
+                isrc.append(int(toks[pos + 3]))
+                jsrc.append(int(toks[pos + 4]))
+                ksrc.append(int(toks[pos + 5]))
+                rates[q] = [_fortran_real(t) for t in toks[pos + 6:pos + 6 + nc]]
+                pos += 6 + nc
+        except (IndexError, ValueError):
+            raise ValueError(f"get_source_value: error reading the source file at time {tcur:6d}") from None
         t1.append(a)
         t2.append(b)
         nsou.append(ns)

@@ -167,3 +167,33 @@ def test_setpsi_matches_the_reference():
     for modv in (1, 2, 3, 4):
         psi = I.setpsi(modv, d["sphe"], d["diam"])
         assert np.array_equal(psi.view(np.uint64), d[f"psi{modv}"].view(np.uint64)), modv
+
+
+def test_short_or_garbled_files_are_read_errors(tmp_path):
+    """A .grn or .src file cut short, or with a word that is not a number,
+    is the readers' read error (libMaster/get_granulometry_value.f90:79-82,
+    get_source_value.f90:80-85), with the reference's message, not a Python
+    index error."""
+    g = I.setfrac(4, 0.0, 3.0, 1200.0, 2300.0, 0.9, 0.9, [1.5], [1.0])
+    p = str(tmp_path / "run.grn")
+    I.write_grn(p, g["diam_mm"], g["rhop"], g["sphe"], g["fc"])
+    text = open(p).read()
+    for bad in (text[: len(text) // 2], text.replace(text.split()[3], "x.y", 1), "", "3\n"):
+        open(p, "w").write(bad)
+        with pytest.raises(ValueError, match="error reading the granulometry file"):
+            I.read_grn(p)
+    rates = np.array([[1.0, 2.0], [3.0, 4.0]])
+    rec = dict(t1=0, t2=3600, x=[14.0, 14.1], y=[37.0, 37.1], z=[100.0, 200.0], i=[1, 2], j=[1, 2],
+               k=[1, 2], rates=rates)
+    rec2 = dict(rec, t1=3600, t2=7200)
+    q = str(tmp_path / "run.src")
+    I.write_src(q, [rec, rec2])
+    text = open(q).read()
+    assert I.read_src(q)["nsou"].tolist() == [2, 2]
+    lines = text.splitlines(keepends=True)
+    open(q, "w").write("".join(lines[:-1]))  # the second interval's last source line missing
+    with pytest.raises(ValueError, match=r"error reading the source file at time\s+3600"):
+        I.read_src(q)
+    open(q, "w").write(text.replace(text.split()[1], "abc", 1))
+    with pytest.raises(ValueError, match="error reading the source file"):
+        I.read_src(q)
