@@ -43,6 +43,7 @@ def _context_kernels(s, prec, steps=2):
     else:
         g.step(steps)
     g.budget()
+    g.count_nonfinite()
     for var, index in ((F.OUT_LOAD, 0), (F.OUT_WET, 0), (F.OUT_THICK, 0), (F.OUT_COL_MASS, 0),
                        (F.OUT_PM_COL, 10), (F.OUT_C_GRND, 0), (F.OUT_PM_GRND, 10), (F.OUT_AOT05, 0),
                        (F.OUT_CON, 0)):
