@@ -164,11 +164,19 @@ def fp64_sequential(scens, arrivals):
         g.outputs()
         g.close()
         service.append(time.perf_counter() - t0)
+    lat, fin = fifo_latencies(arrivals, service)
+    return np.array(service), lat, fin
+
+
+def fifo_latencies(arrivals, service):
+    """One server taking requests in arrival order: request i finishes at
+    finish_i = max(finish_{i-1}, arrival_i) + service_i; returns the
+    latencies finish_i - arrival_i and the last finish time."""
     fin, lat = 0.0, []
     for a, sv in zip(arrivals, service):
         fin = max(fin, a) + sv
         lat.append(fin - a)
-    return np.array(service), np.array(lat), fin
+    return np.array(lat), fin
 
 
 def serving(rate=2.0, window=600.0, cap_gb=150.0, dmin=3.0, dmax=48.0, met_dt_h=12.0, seed=0,
