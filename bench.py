@@ -250,6 +250,25 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def captured_traffic(kernel, workload=WORKLOAD, root=ROOT):
+    """DRAM bytes (read + write) of one launch of ``kernel`` from the
+    committed ncu capture (profiles/ncu_traffic.json), valid only while the
+    step kernel's source is the one that was captured (its SHA-256 is stored
+    beside the figure); returns (bytes or None, where the figure comes from)."""
+    tpath = os.path.join(root, "profiles", "ncu_traffic.json")
+    if not os.path.exists(tpath):
+        return None, "no capture"
+    try:
+        rec = json.load(open(tpath)).get(workload, {})
+        kpath = os.path.join(root, "fall3d_gb300", "csrc", "f3d_fused2.cu")
+        sha = hashlib.sha256(open(kpath, "rb").read()).hexdigest()
+    except (OSError, ValueError):
+        return None, "no capture"
+    if rec.get("kernel_sha256") != sha:
+        return None, "stale: the kernel source changed since the capture"
+    return rec.get(kernel), "ncu capture of this kernel source"
+
+
 def max_over_ranks_of(x, dist=None, device="cpu"):
     """The largest of every rank's x (the job's time is its slowest rank's)."""
     if dist is None:
@@ -415,21 +434,7 @@ def run_ours(args, rank, world, local_rank):
         alg_bytes = bpc * cells
         avg_ms = dom_ms / dom_n
         achieved = alg_bytes / (avg_ms / 1e3) / 1e9
-        # DRAM bytes of one launch from the committed ncu capture, valid only
-        # while the kernel's source is the one that was captured
-        traffic, traffic_note = None, "no capture"
-        tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-        if os.path.exists(tpath):
-            try:
-                rec = json.load(open(tpath)).get(WORKLOAD, {})
-                kpath = os.path.join(ROOT, "fall3d_gb300", "csrc", "f3d_fused2.cu")
-                sha = hashlib.sha256(open(kpath, "rb").read()).hexdigest()
-                if rec.get("kernel_sha256") == sha:
-                    traffic, traffic_note = rec.get(dom_name), "ncu capture of this kernel source"
-                else:
-                    traffic_note = "stale: the kernel source changed since the capture"
-            except Exception:
-                traffic = None
+        traffic, traffic_note = captured_traffic(dom_name)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_note, "kernel": dom_name,
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,

@@ -49,3 +49,28 @@ def test_two_gloo_ranks_take_the_slowest_time():
         assert p.exitcode == 0
     assert [r[1] for r in res] == [15.0, 15.0]
     assert res[0][2] == pytest.approx(1000 * 20 * 2 / 0.015)
+
+
+def test_captured_traffic_is_used_only_for_the_captured_source(tmp_path):
+    """bench.py's roofline.traffic: the committed ncu figure of the step
+    kernel counts only while the kernel's source has the SHA-256 stored with
+    it."""
+    import hashlib
+    import json
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    (tmp_path / "profiles").mkdir()
+    (tmp_path / "fall3d_gb300" / "csrc").mkdir(parents=True)
+    k = tmp_path / "fall3d_gb300" / "csrc" / "f3d_fused2.cu"
+    assert bench.captured_traffic("step_fused", "cfg1", str(tmp_path)) == (None, "no capture")
+    k.write_text("// kernel v1\n")
+    sha = hashlib.sha256(k.read_bytes()).hexdigest()
+    (tmp_path / "profiles" / "ncu_traffic.json").write_text(
+        json.dumps({"cfg1": {"step_fused": 123456789, "kernel_sha256": sha}}))
+    t, note = bench.captured_traffic("step_fused", "cfg1", str(tmp_path))
+    assert t == 123456789 and "this kernel source" in note
+    k.write_text("// kernel v2\n")
+    t, note = bench.captured_traffic("step_fused", "cfg1", str(tmp_path))
+    assert t is None and note.startswith("stale")
