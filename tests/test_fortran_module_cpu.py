@@ -70,3 +70,80 @@ def test_every_constant_is_a_parameter():
     f = {n: int(v) for n, v in re.findall(r"integer\(c_int\), parameter :: (F3D_\w+) = (-?\d+)", _f90())}
     assert c, "no constants parsed from the header"
     assert f == c, sorted(set(c.items()) ^ set(f.items()))
+
+
+def _c_params():
+    """name -> list of (by_value, kind) per parameter of the header's
+    functions; kind is the C base type (int, double, long long, char,
+    void, or the struct / handle name)."""
+    src = open(os.path.join(ROOT, "include", "fall3d_gpu.h")).read()
+    body = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for _, name, args in re.findall(r"^(int|long long|const char\*)\s+(f3d_\w+)\s*\(([^;]*?)\);", body,
+                                    flags=re.M | re.S):
+        a = " ".join(args.split())
+        params = []
+        if a not in ("", "void"):
+            for p in a.split(","):
+                p = p.replace("const ", "").strip()
+                stars = p.count("*")
+                base = p.replace("*", " ").split()
+                base = " ".join(base[:-1])  # drop the parameter name
+                params.append((stars, base))
+        out[name] = params
+    return out
+
+
+def _f90_params():
+    """name -> list of (by_value, fortran type) per dummy argument, in the
+    order of the function statement."""
+    text = re.sub(r"&\s*\n\s*", "", _f90())
+    out = {}
+    for m in re.finditer(r"function (f3d_\w+)\(([^)]*)\) bind\(C, name=\"\w+\"\)\n(.*?)end function \1", text,
+                         flags=re.S):
+        name, args, block = m.group(1), m.group(2), m.group(3)
+        decl = {}
+        for line in block.splitlines():
+            line = line.split("!")[0].strip()
+            if "::" not in line:
+                continue
+            spec, names = [x.strip() for x in line.split("::")]
+            typ = spec.split(",")[0].strip()
+            attrs = [x.strip() for x in spec.split(",")[1:]]
+            for nm in names.split(","):
+                nm = nm.strip()
+                arr = nm.endswith("(*)")
+                decl[nm.replace("(*)", "").lower()] = ("value" in attrs, typ, arr)
+        out[name] = [decl[a.strip().lower()] for a in args.split(",") if a.strip()]
+    return out
+
+
+# C base type -> the Fortran type of a value or of the pointee
+_KIND = {"int": "integer(c_int)", "double": "real(c_double)", "float": "real(c_float)", "long long": "integer(c_long_long)",
+         "char": "character(kind=c_char)"}
+
+
+def test_every_argument_is_passed_as_the_header_declares():
+    """By value in C <=> VALUE in Fortran, with the same kind; a pointer to a
+    scalar or array <=> a by-reference dummy of the pointee's kind (or an
+    opaque type(c_ptr), value); the context and batch / server handles
+    <=> type(c_ptr), value; a handle's address (f3d_ctx** and the like) <=>
+    type(c_ptr) by reference; a struct pointer <=> the bind(C) derived type
+    by reference."""
+    c, f = _c_params(), _f90_params()
+    assert set(c) == set(f)
+    handles = {"f3d_ctx", "f3d_batch", "f3d_server"}
+    bad = []
+    for name, cps in c.items():
+        for i, ((stars, base), (val, typ, arr)) in enumerate(zip(cps, f[name])):
+            if stars == 0:
+                ok = val and typ == _KIND.get(base)
+            elif base in handles or base == "void":
+                ok = (stars == 1 and val and typ == "type(c_ptr)") or (stars == 2 and not val and typ == "type(c_ptr)")
+            elif base.startswith("f3d_"):
+                ok = not val and typ == f"type({base})"
+            else:
+                ok = (not val and typ == _KIND.get(base)) or (val and typ == "type(c_ptr)")
+            if not ok:
+                bad.append((name, i, stars, base, val, typ))
+    assert not bad, bad
