@@ -41,3 +41,37 @@ def test_version_string():
 
     build.build()
     assert "sm_103a" in F.version()
+
+
+def test_ctypes_signatures_match_the_header():
+    """The Python mirror declares every entry point with the header's
+    argument count, by-value scalars with their C type and pointers as
+    pointers (a wrong count or a by-value double passed as an int would
+    corrupt the call silently)."""
+    import ctypes as C
+
+    import fall3d_gb300 as F
+    from fall3d_gb300 import build
+
+    build.build()
+    lib = F.load()
+    txt = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "fall3d_gpu.h")).read(), flags=re.S)
+    scalar = {"int": C.c_int, "double": C.c_double, "long long": C.c_longlong, "float": C.c_float}
+    bad = []
+    for _, name, args in re.findall(r"^(int|long long|const char\*)\s+(f3d_\w+)\s*\(([^;]*?)\);", txt,
+                                    flags=re.M | re.S):
+        a = " ".join(args.split())
+        params = [] if a in ("", "void") else [p.replace("const ", "").strip() for p in a.split(",")]
+        at = getattr(lib, name).argtypes
+        if at is None or len(at) != len(params):
+            bad.append((name, "count", None if at is None else len(at), len(params)))
+            continue
+        for i, (p, t) in enumerate(zip(params, at)):
+            base = " ".join(p.replace("*", " ").split()[:-1])
+            if "*" in p:
+                ok = t in (C.c_void_p, C.c_char_p) or (isinstance(t, type) and issubclass(t, C._Pointer))
+            else:
+                ok = t is scalar.get(base)
+            if not ok:
+                bad.append((name, i, p, t))
+    assert not bad, bad
