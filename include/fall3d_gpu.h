@@ -350,7 +350,10 @@ typedef struct f3d_ctx f3d_ctx;
 
 int f3d_ctx_create(const f3d_grid* grid, f3d_ctx** out);
 int f3d_ctx_destroy(f3d_ctx* ctx);
-/* Device bytes held by a context of this grid (admission control). */
+/* Device bytes held by a context of this grid (admission control): the
+ * context as f3d_ctx_create makes it and the batched and serving forms use
+ * it.  The second coefficient set of f3d_run's look-ahead meteo update
+ * (F3D_OPT_PREFETCH) is not included. */
 int f3d_ctx_footprint(const f3d_grid* grid, long long* bytes);
 
 /* Sources/meteo.f90:19-149 on the device for one DBS snapshot: reamet's
