@@ -75,3 +75,37 @@ def test_ctypes_signatures_match_the_header():
             if not ok:
                 bad.append((name, i, p, t))
     assert not bad, bad
+
+
+def test_a_c_host_compiles_and_links_against_the_library(tmp_path):
+    """The header is plain C (C99, -pedantic, no warnings) and a C program
+    that takes the address of every declared entry point links against the
+    library and runs (no compute call: it only prints the library version
+    string's length) -- what a C or Fortran host does when it binds the ABI."""
+    import shutil
+    import subprocess
+
+    from fall3d_gb300 import build
+
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    lib = build.build()
+    names = _declared()
+    src = tmp_path / "host.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <string.h>\n#include "fall3d_gpu.h"\n'
+        "typedef void (*fn)(void);\n"
+        "int main(void) {\n"
+        f"  fn table[] = {{ {', '.join(f'(fn){n}' for n in names)} }};\n"
+        "  printf(\"%d %d\\n\", (int)(sizeof table / sizeof table[0]), (int)strlen(f3d_version()) > 0);\n"
+        "  return 0;\n}\n")
+    exe = tmp_path / "host"
+    libdir = os.path.dirname(lib)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-Wno-cast-function-type",
+                        "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-L", libdir,
+                        "-l:" + os.path.basename(lib), "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == [str(len(names)), "1"]
