@@ -109,3 +109,22 @@ def test_a_c_host_compiles_and_links_against_the_library(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0, out.stderr
     assert out.stdout.split() == [str(len(names)), "1"]
+
+
+def test_the_product_does_not_use_the_oracle():
+    """The library and its Python mirror neither import, load nor name a
+    path of oracle/ (the oracle is test infrastructure): no import of an
+    oracle module, no oracle/ path and no liboracle in the package, the
+    header or the CUDA sources."""
+    pkg = os.path.join(ROOT, "fall3d_gb300")
+    files = [os.path.join(dp, f) for dp, _, fs in os.walk(pkg) for f in fs
+             if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")) and "_build" not in dp]
+    files += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    pat = re.compile(r"import\s+(oracle_lib|ref_driver|ref_translate)|from\s+(oracle|ref_driver|ref_translate)\b|"
+                     r"oracle/|liboracle|f3d_oracle|oracle_lib")
+    hits = []
+    for f in files:
+        for i, line in enumerate(open(f, errors="replace"), 1):
+            if pat.search(line):
+                hits.append(f"{os.path.relpath(f, ROOT)}:{i}: {line.strip()}")
+    assert not hits, hits
